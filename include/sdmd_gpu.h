@@ -1,0 +1,228 @@
+/*
+ * sdmd_gpu.h -- C ABI of the GB300 event-loop engine for sDMD.
+ *
+ * The engine replaces the reference's event loop below ThreadProcess()
+ * (src/ToolFunctions.c:12-20): Prepare() (src/SGThread.c:21-64), SingleThreadRun()
+ * (src/SGThread.c:67-155), Predict() (src/SGThread.c:158-211), the CBT event queue
+ * (src/CBT.c) and event execution (src/Events.c).  Parsing, model building and the
+ * output writers stay on the host.
+ *
+ * Conventions
+ *   - Atom ids are 1..N exactly as in the reference (atom[1..atomnum]); every
+ *     per-atom array below has N+1 entries and entry 0 is unused.
+ *   - Vectors are SoA (x[], y[], z[]), FP64, in the reference's units (A, u,
+ *     kcal/mol, 48.88 fs time unit).
+ *   - Every function returns SDMD_OK (0) or a negative SDMD_E* code; device-side
+ *     physics errors carry (system, atom, event#) retrievable with
+ *     sdmd_gpu_last_error().  No function exits the process.
+ *   - Handles are not thread-safe; one host thread per handle, one CUDA stream
+ *     per handle.  No pointer into caller memory is retained past a call.
+ */
+#ifndef SDMD_GPU_H
+#define SDMD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDMD_ABI_VERSION 1
+
+/* ---- status codes ---------------------------------------------------------- */
+#define SDMD_OK              0
+#define SDMD_EINVAL         -1   /* bad argument / inconsistent sizes            */
+#define SDMD_ENOMEM         -2   /* device or host allocation failed             */
+#define SDMD_ECUDA          -3   /* CUDA runtime error                           */
+#define SDMD_ENODEV         -4   /* no CUDA device                               */
+#define SDMD_ENEGTIME       -10  /* predicted event time < 0 (src/TimePrediction.c:168-173) */
+#define SDMD_ENAN           -11  /* NaN phi in a velocity update (src/Events.c:1008-1011)   */
+#define SDMD_EWALL          -12  /* atom outside the wall (src/TimePrediction.c:700-701)    */
+#define SDMD_ELINK          -13  /* cell-list corruption (src/Events.c:182-192)             */
+#define SDMD_EHBMAP         -14  /* HB bookkeeping inconsistent (src/Events.c:313-321)      */
+#define SDMD_ECAPACITY      -15  /* a fixed device capacity was exceeded                  */
+#define SDMD_ETIMEOUT       -16  /* a bounded device-side wait ran out                     */
+#define SDMD_EUNSUPPORTED   -17  /* configuration outside the engine's scope              */
+#define SDMD_EEVENTTYPE     -18  /* invalid event type popped (src/Events.c:104-108)       */
+
+/* ---- event / sub-event enums (values of src/DMD.h:162-190) ----------------- */
+enum {
+    SDMD_EV_COLLISION = 0, SDMD_EV_BOND = 1, SDMD_EV_HB = 2, SDMD_EV_HBNEIGHBOR = 3,
+    SDMD_EV_THERMOSTAT = 4, SDMD_EV_WALL = 5, SDMD_EV_PCC = 10, SDMD_EV_INVALID = 15
+};
+enum {
+    SDMD_SUB_CORE = 0, SDMD_SUB_WELL_BOUNCE = 1, SDMD_SUB_WELL_CAPTURE = 2,
+    SDMD_SUB_WELL_ESCAPE = 3, SDMD_SUB_TBD_CAPTURE = 4, SDMD_SUB_TBD_ESCAPE = 5,
+    SDMD_SUB_TBD_HBFORM = 6, SDMD_SUB_TBD_HBBREAK = 7, SDMD_SUB_INVALID = 8
+};
+enum { SDMD_HB_NOEVENT = 0, SDMD_HB_FORM = 1, SDMD_HB_BREAK = 2, SDMD_HB_SKIP = 3 };
+enum { SDMD_WALL_NONE = 0, SDMD_WALL_PARALLEL = 1, SDMD_WALL_CYLINDER = 2, SDMD_WALL_SPHERE = 3 };
+
+#define SDMD_NTYPES   33     /* NATOMTYPE + 1 (src/DMD.h:29) */
+#define SDMD_NTABLES  12     /* table 0: collision pairs; 1..11: HB classes (src/DMD.c:98-99) */
+#define SDMD_INVALID  (-111) /* src/DMD.h:28 */
+#define SDMD_INFINIT  1e8    /* src/DMD.h:26 */
+#define SDMD_ZERO     1e-8   /* src/DMD.h:27 */
+
+/* glibc-compatible additive-feedback RNG state (TYPE_3, degree 31, separation 3):
+ * the stream rand() produces after srand(seed).  The reference draws every
+ * random number through rand() (src/ToolFunctions.c:517-522). */
+typedef struct sdmd_rng {
+    int32_t tab[31];
+    int32_t front, rear;          /* indices into tab */
+} sdmd_rng;
+
+/* Event-type counters, order of src/DMD.c:50-58 */
+typedef struct sdmd_counters {
+    int64_t frame;                /* executed events  (src/SGThread.c:100) */
+    int64_t recal;                /* denied pops      (src/SGThread.c:150) */
+    int64_t collision, bond, hb, hbneighbor, thermostat, pcc, wall;
+    int64_t warnings;             /* warningsum */
+    int32_t hb_formed, alpha_hb_formed;
+} sdmd_counters;
+
+/*
+ * One simulated system (a replica or an independent system of a batch).
+ * Static arrays are read at sdmd_gpu_create/upload; dynamic arrays are read at
+ * upload and written by sdmd_gpu_download.
+ */
+typedef struct sdmd_system {
+    /* ---- sizes ---- */
+    int32_t n_atoms;
+    int32_t cellnum[3];            /* cellnum[1..3] of the reference */
+    int32_t n_bonds, n_cons, n_con_steps, n_conn, n_pair_steps;
+
+    /* ---- parameters (src/Initialization.c:512-730) ---- */
+    double  box[3];                /* boxDimension[1..3] */
+    double  cellsize[3];
+    double  cutoff;                /* cutoffr */
+    double  temperature;           /* targetTemperature (reduced) */
+    double  thermo_freq;           /* thermoF */
+    double  t_end;                 /* timestep: the loop runs while time <= t_end */
+    int32_t thermostat;            /* 0 none, 1 Andersen */
+    int32_t wall;                  /* SDMD_WALL_* ("smooth" walls only) */
+    double  wall_pos[3], wall_vel[3], wall_mass;
+    int32_t wall_type;             /* atom type of the wall pseudo-atom */
+    double  hb_barrier[3];         /* HBPotential BB_v, BS_v, SS_v (src/DMD.h:231-236) */
+
+    /* ---- per-atom static (N+1 entries) ---- */
+    const double  *mass;
+    const int32_t *protein;        /* sequence.proteinNum */
+    const int32_t *aanum;          /* sequence.aminoacidNum (within its protein) */
+    const int32_t *aatype;         /* typeofAA (src/Models.c:65) */
+    const int32_t *hb_neighbor;    /* HB.neighbor */
+    const int32_t *hb_role;        /* HB.role: 'A', 'D', 'S' or 0 */
+    const int32_t *name_code;      /* 1: name "H", 2: name "O", 0: other (alpha-HB count only) */
+
+    /* ---- topology ---- */
+    const int32_t *bond_off;       /* N+2; bonds of atom i: [bond_off[i], bond_off[i+1]) in list order */
+    const int32_t *bond_j;
+    const double  *bond_dmin, *bond_dmax;            /* squared lengths */
+    const int32_t *con_off;        /* N+2; step-potential constraints of atom i */
+    const int32_t *con_j, *con_step_off, *con_step_n;
+    const double  *con_dmin, *con_dmax;              /* squared */
+    const double  *con_step_d, *con_step_e, *con_step_acc;
+    const int32_t *conn_off;       /* N+2; static connection-map bits of atom i (sparse row) */
+    const int32_t *conn_j, *conn_bits;               /* bits: 1 BOND_CONNECT, 2 CONSTRAINT_CONNECT */
+
+    /* ---- pair tables [SDMD_NTABLES][SDMD_NTYPES][SDMD_NTYPES] ---- */
+    const double  *pair_dmin, *pair_dmax;            /* squared */
+    const int32_t *pair_step_off, *pair_step_n;
+    const double  *pair_step_d, *pair_step_e, *pair_step_acc;
+
+    /* ---- dynamic per-atom state (N+1 entries) ---- */
+    double  *x, *y, *z, *vx, *vy, *vz;
+    int32_t *cx, *cy, *cz;         /* cellIndex[1..3] */
+    int32_t *type;                 /* typeofAtom (changes on HB form/break) */
+    int32_t *hb_bond;              /* HB.bondConnection */
+    int32_t *hb_itype;             /* HB.interactionType */
+    int32_t *nb_partner;           /* 4*(N+1): neighborPartner[1..4] of atom i at [4*i .. 4*i+3] */
+    int32_t *nb_status;            /* HBNeighbor.neighborStatus */
+    int32_t *nb_pnum;              /* HBNeighbor.partnerNum */
+    double  *ev_time;              /* event.time (relative to the current time) */
+    int32_t *ev_partner;
+    int64_t *ev_counter, *ev_pcounter;
+    double  *ev_potential;
+    int32_t *ev_type, *ev_sub;
+    int32_t *cell_list;            /* N + ncell + 1: reference celllist (heads at N + cell) */
+
+    /* ---- dynamic scalars ---- */
+    double        time;            /* currenttime */
+    sdmd_rng      rng;
+    sdmd_counters counters;
+} sdmd_system;
+
+/* one record per popped event; same fields as the reference trace */
+typedef struct sdmd_trace_rec {
+    int32_t target, partner, type, sub, executed, hb_itype_after;
+    int32_t t_new_partner, t_new_type, p_new_partner, p_new_type, system, pad;
+    double  dt, time_now;
+    double  vt[3], vp[3];
+    double  t_new_time, p_new_time;
+} sdmd_trace_rec;
+
+/* ---- engine options ---- */
+enum { SDMD_ADVANCE_EAGER = 0,   /* x += v*dt for every atom at every pop (bit-exact with the reference) */
+       SDMD_ADVANCE_LAZY  = 1 }; /* per-atom local time, FP64 global clock */
+enum { SDMD_SCREEN_FP64 = 0,     /* every candidate root in FP64 */
+       SDMD_SCREEN_FP32 = 1 };   /* FP32 screen with a proven margin, FP64 refine */
+
+typedef struct sdmd_opts {
+    int32_t advance;               /* SDMD_ADVANCE_* */
+    int32_t screen;                /* SDMD_SCREEN_* */
+    int32_t threads_per_system;    /* 32 (one warp) .. 256; 0 = autotuned */
+    int32_t device;                /* CUDA device ordinal */
+    int32_t trace_capacity;        /* records kept by sdmd_gpu_run when tracing (0 = off) */
+    int32_t reserved[7];
+} sdmd_opts;
+
+typedef struct sdmd_gpu sdmd_gpu;   /* opaque handle */
+
+typedef struct sdmd_error_info {
+    int32_t code, system, atom;
+    int64_t event;
+} sdmd_error_info;
+
+/* Library / device query.  Returns SDMD_OK if a usable device exists. */
+int         sdmd_gpu_abi_version(void);
+int         sdmd_gpu_device_count(int32_t *count);
+const char *sdmd_gpu_strerror(int code);
+
+/* Create a handle holding n_systems systems on the device and upload their state.
+ * Replaces Prepare()'s allocations (src/SGThread.c:21-64). */
+int  sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems,
+                     const sdmd_opts *opts, sdmd_gpu **out);
+void sdmd_gpu_destroy(sdmd_gpu *h);
+
+/* Full-rebuild sweep: Predict() over atoms 1..N of every system
+ * (src/SGThread.c:47-52), then build each system's event tree (CreateCBT,
+ * src/CBT.c:16-30).  With full_predict == 0 the stored events are kept
+ * (continue mode, src/SGThread.c:54-55) and only the trees are built. */
+int  sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict);
+
+/* Run every system's event loop (src/SGThread.c:75-151) until it has executed
+ * max_events more events or its time exceeds t_end (<= 0: the system's own
+ * t_end), whichever comes first.  Returns after all systems stopped. */
+int  sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end);
+
+/* Copy every system's dynamic state back into the caller's arrays. */
+int  sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_systems);
+
+/* Copy the last n records of the pop trace of system s (when tracing is on). */
+int  sdmd_gpu_trace(sdmd_gpu *h, int32_t s, sdmd_trace_rec *out, int32_t cap, int32_t *n_out);
+
+/* Device time (ms) of the last prepare / run call, measured with CUDA events on
+ * the handle's stream. */
+int  sdmd_gpu_last_ms(sdmd_gpu *h, double *prepare_ms, double *run_ms);
+
+int  sdmd_gpu_last_error(sdmd_gpu *h, sdmd_error_info *info);
+
+/* glibc-compatible rand() stream helpers (host side). */
+void sdmd_rng_seed(sdmd_rng *r, uint32_t seed);
+int32_t sdmd_rng_next(sdmd_rng *r);
+void sdmd_rng_skip(sdmd_rng *r, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SDMD_GPU_H */

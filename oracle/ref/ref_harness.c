@@ -1,0 +1,412 @@
+/*
+ * ref_harness.c -- driver linked against the UNMODIFIED reference sDMD sources
+ * (compiled by oracle/ref/Makefile).  It reproduces the reference's Prepare()
+ * (src/SGThread.c:21-64) and SingleThreadRun() (src/SGThread.c:67-155) call
+ * sequence with the reference's own functions, and dumps:
+ *
+ *   <out>/pre.bin    state after SDEnergyMin/PBC/LinkList, before the full-rebuild
+ *                    Predict sweep (src/SGThread.c:42-52): the hand-off state
+ *   <out>/sweep.bin  every atom's predicted event after Predict(1..N), + rand count
+ *   <out>/trace.bin  one record per popped event of the loop (executed or denied)
+ *   <out>/ckpt_K.bin state after K executed events (K from the command line)
+ *
+ * Usage: sdmd_ref_harness <out_dir> <n_events> <ckpt1,ckpt2,...|-> -- <sDMD args>
+ *
+ * Test infrastructure only: it is how the golden fixtures under tests/golden/ are
+ * produced from the reference itself.
+ */
+#include "DMD.h"
+#include <stdint.h>
+
+/* ---- counting wrapper around glibc rand() (reference built with -Drand=...) ---- */
+static long long g_rand_calls = 0;
+int sdmd_ref_rand(void) { g_rand_calls++; return rand(); }
+
+/* ---- section writer: "SDMD" | name[32] | type char | pad[3] | int64 count | data ---- */
+static FILE *g_out = NULL;
+static void sec(const char *name, char type, long long count, const void *data) {
+    char hdr[40] = {0};
+    memcpy(hdr, "SDMD", 4);
+    strncpy(hdr + 4, name, 31);
+    hdr[36] = type;
+    fwrite(hdr, 1, 40, g_out);
+    fwrite(&count, sizeof(long long), 1, g_out);
+    size_t es = (type == 'd' || type == 'q') ? 8 : (type == 'i' ? 4 : 1);
+    if (count > 0) fwrite(data, es, (size_t)count, g_out);
+}
+static void sec_i(const char *n, int v) { sec(n, 'i', 1, &v); }
+static void sec_q(const char *n, long long v) { sec(n, 'q', 1, &v); }
+static void sec_d(const char *n, double v) { sec(n, 'd', 1, &v); }
+static void sec_s(const char *n, const char *s) { sec(n, 'b', (long long)strlen(s), s); }
+
+static void open_out(const char *dir, const char *file) {
+    char path[2048];
+    snprintf(path, sizeof(path), "%s/%s", dir, file);
+    g_out = fopen(path, "wb");
+    if (!g_out) { perror(path); exit(3); }
+}
+static void close_out(void) { fclose(g_out); g_out = NULL; }
+
+/* dynamic per-atom state (everything the loop mutates) */
+static void dump_dynamic(void) {
+    int N = atomnum;
+    double *d = malloc(sizeof(double) * (N + 1));
+    long long *q = malloc(sizeof(long long) * (N + 1));
+    int *v = malloc(sizeof(int) * (N + 1));
+    char *c = malloc(N + 1);
+#define DUMP_D(name, expr) for (int i = 0; i <= N; i++) d[i] = (expr); sec(name, 'd', N + 1, d)
+#define DUMP_I(name, expr) for (int i = 0; i <= N; i++) v[i] = (expr); sec(name, 'i', N + 1, v)
+#define DUMP_Q(name, expr) for (int i = 0; i <= N; i++) q[i] = (expr); sec(name, 'q', N + 1, q)
+    DUMP_D("x", atom[i].dynamic->coordinate[1]);
+    DUMP_D("y", atom[i].dynamic->coordinate[2]);
+    DUMP_D("z", atom[i].dynamic->coordinate[3]);
+    DUMP_D("vx", atom[i].dynamic->velocity[1]);
+    DUMP_D("vy", atom[i].dynamic->velocity[2]);
+    DUMP_D("vz", atom[i].dynamic->velocity[3]);
+    DUMP_I("cx", atom[i].dynamic->cellIndex[1]);
+    DUMP_I("cy", atom[i].dynamic->cellIndex[2]);
+    DUMP_I("cz", atom[i].dynamic->cellIndex[3]);
+    DUMP_I("type", atom[i].property->typeofAtom);
+    DUMP_I("hb_bond", atom[i].dynamic->HB.bondConnection);
+    DUMP_I("hb_itype", (int)atom[i].dynamic->HB.interactionType);
+    DUMP_I("nb_p1", atom[i].dynamic->HBNeighbor.neighborPartner[1]);
+    DUMP_I("nb_p2", atom[i].dynamic->HBNeighbor.neighborPartner[2]);
+    DUMP_I("nb_p3", atom[i].dynamic->HBNeighbor.neighborPartner[3]);
+    DUMP_I("nb_p4", atom[i].dynamic->HBNeighbor.neighborPartner[4]);
+    DUMP_I("nb_status", atom[i].dynamic->HBNeighbor.neighborStatus);
+    DUMP_I("nb_pnum", atom[i].dynamic->HBNeighbor.partnerNum);
+    DUMP_D("ev_time", atom[i].dynamic->event.time);
+    DUMP_I("ev_partner", atom[i].dynamic->event.partner);
+    DUMP_Q("ev_counter", atom[i].dynamic->event.counter);
+    DUMP_Q("ev_pcounter", atom[i].dynamic->event.partnerCounter);
+    DUMP_D("ev_potential", atom[i].dynamic->event.potential);
+    DUMP_I("ev_type", (int)atom[i].dynamic->event.eventType);
+    DUMP_I("ev_sub", (int)atom[i].dynamic->event.subEventType);
+    sec("celllist", 'i', (long long)atomnum + cellnum[1] * cellnum[2] * cellnum[3] + 1, celllist);
+    sec_d("currenttime", currenttime);
+    sec_q("frame", frame);
+    sec_q("countReCal", countReCal);
+    sec_q("rand_calls", g_rand_calls);
+    long long counts[8] = {collisioneventsum, bondeventsum, HBeventsum, HBNeighboreventsum,
+                           thermostateventsum, pbcandcrosseventsum, walleventsum, CGeventsum};
+    sec("event_counts", 'q', 8, counts);
+    sec_i("HBnumformed", HBnumformed);
+    sec_i("alphaHBformed", alphaHBformed);
+    sec_q("warningsum", warningsum);
+    /* HB / NEIGHBOR bits of the dense connection map, as a sparse (i, j, bits) list,
+       so the sparse HB state can be checked against them */
+    {
+        long long cnt = 0;
+        for (int i = 1; i <= N; i++)
+            for (int j = 1; j <= N; j++)
+                if (connectionMap[i][j] & (HB_CONNECT | NEIGHBOR_CONNECT)) cnt++;
+        int *t = malloc(sizeof(int) * 3 * (cnt + 1));
+        long long k = 0;
+        for (int i = 1; i <= N; i++)
+            for (int j = 1; j <= N; j++)
+                if (connectionMap[i][j] & (HB_CONNECT | NEIGHBOR_CONNECT)) {
+                    t[3 * k] = i; t[3 * k + 1] = j;
+                    t[3 * k + 2] = connectionMap[i][j] & (HB_CONNECT | NEIGHBOR_CONNECT);
+                    k++;
+                }
+        sec("hbmap", 'i', 3 * cnt, t);
+        free(t);
+    }
+    free(d); free(q); free(v); free(c);
+}
+
+/* static topology, tables and parameters */
+static void dump_static(void) {
+    int N = atomnum;
+    int *v = malloc(sizeof(int) * (N + 1));
+    double *d = malloc(sizeof(double) * (N + 1));
+    sec_i("atomnum", N);
+    sec("box", 'd', 3, &boxDimension[1]);
+    sec("cellnum", 'i', 3, &cellnum[1]);
+    sec("cellsize", 'd', 3, &cellsize[1]);
+    sec_d("cutoffr", cutoffr);
+    sec_d("targetTemperature", targetTemperature);
+    sec_d("thermoF", thermoF);
+    sec_d("timestep", timestep);
+    sec_s("thermostatType", thermostatType);
+    sec_s("wallExist", wallExist);
+    sec_s("wallType", wallType);
+    sec_s("Methodtype", Methodtype);
+    sec("HBPotential", 'd', 6, &HBPotential);
+    sec_i("seed", (int)seed);
+    sec_i("numofprotein", numofprotein);
+    DUMP_D("mass", atom[i].property->mass);
+    DUMP_I("protein", atom[i].property->sequence.proteinNum);
+    DUMP_I("aanum", atom[i].property->sequence.aminoacidNum);
+    DUMP_I("typeofAA", atom[i].property->typeofAA);
+    DUMP_I("hb_neighbor", atom[i].dynamic->HB.neighbor);
+    DUMP_I("hb_role", (int)atom[i].dynamic->HB.role);
+    DUMP_I("cons", strcmp(atom[i].property->extraProperty[1], "_CONS") == 0);
+    {
+        char *names = calloc((size_t)(N + 1) * 8, 1);
+        for (int i = 1; i <= N; i++) memcpy(names + 8 * i, atom[i].property->name, 8);
+        sec("name", 'b', (long long)(N + 1) * 8, names);
+        for (int i = 1; i <= N; i++) memcpy(names + 8 * i, atom[i].property->nameofAA, 8);
+        sec("nameofAA", 'b', (long long)(N + 1) * 8, names);
+        free(names);
+    }
+    /* bond lists in linked-list order */
+    {
+        long long nb = 0;
+        for (int i = 1; i <= N; i++)
+            for (struct ConstraintStr *b = atom[i].property->bond; b; b = b->next) nb++;
+        int *off = calloc(N + 2, sizeof(int)), *bj = calloc(nb + 1, sizeof(int));
+        double *bmin = calloc(nb + 1, sizeof(double)), *bmax = calloc(nb + 1, sizeof(double));
+        long long k = 0;
+        for (int i = 1; i <= N; i++) {
+            off[i] = (int)k;
+            for (struct ConstraintStr *b = atom[i].property->bond; b; b = b->next) {
+                bj[k] = b->connection; bmin[k] = b->dmin; bmax[k] = b->dmax; k++;
+            }
+        }
+        off[N + 1] = (int)k;
+        sec("bond_off", 'i', N + 2, off);
+        sec("bond_j", 'i', nb, bj);
+        sec("bond_dmin", 'd', nb, bmin);
+        sec("bond_dmax", 'd', nb, bmax);
+        free(off); free(bj); free(bmin); free(bmax);
+    }
+    /* constraint lists: (j, dmin, dmax, steps) */
+    {
+        long long nc = 0, ns = 0;
+        for (int i = 1; i <= N; i++)
+            for (struct ConstraintStr *c = atom[i].property->constr; c; c = c->next) {
+                nc++;
+                for (struct StepPotenStr *s = c->step; s; s = s->next) ns++;
+            }
+        int *off = calloc(N + 2, sizeof(int)), *cj = calloc(nc + 1, sizeof(int));
+        int *soff = calloc(nc + 1, sizeof(int)), *sn = calloc(nc + 1, sizeof(int));
+        double *cmin = calloc(nc + 1, sizeof(double)), *cmax = calloc(nc + 1, sizeof(double));
+        double *sd = calloc(ns + 1, sizeof(double)), *se = calloc(ns + 1, sizeof(double)),
+               *sa = calloc(ns + 1, sizeof(double));
+        long long k = 0, m = 0;
+        for (int i = 1; i <= N; i++) {
+            off[i] = (int)k;
+            for (struct ConstraintStr *c = atom[i].property->constr; c; c = c->next) {
+                cj[k] = c->connection; cmin[k] = c->dmin; cmax[k] = c->dmax;
+                soff[k] = (int)m; sn[k] = 0;
+                for (struct StepPotenStr *s = c->step; s; s = s->next) {
+                    sd[m] = s->d; se[m] = s->e; sa[m] = s->accumulated; m++; sn[k]++;
+                }
+                k++;
+            }
+        }
+        off[N + 1] = (int)k;
+        sec("con_off", 'i', N + 2, off);
+        sec("con_j", 'i', nc, cj);
+        sec("con_dmin", 'd', nc, cmin);
+        sec("con_dmax", 'd', nc, cmax);
+        sec("con_step_off", 'i', nc, soff);
+        sec("con_step_n", 'i', nc, sn);
+        sec("con_step_d", 'd', ns, sd);
+        sec("con_step_e", 'd', ns, se);
+        sec("con_step_acc", 'd', ns, sa);
+        free(off); free(cj); free(soff); free(sn); free(cmin); free(cmax); free(sd); free(se); free(sa);
+    }
+    /* BOND / CONSTRAINT bits of the dense connection map, sparse (i, j, bits) */
+    {
+        long long cnt = 0;
+        for (int i = 0; i <= N; i++)
+            for (int j = 0; j <= N; j++)
+                if (connectionMap[i][j] & (BOND_CONNECT | CONSTRAINT_CONNECT)) cnt++;
+        int *t = malloc(sizeof(int) * 3 * (cnt + 1));
+        long long k = 0;
+        for (int i = 0; i <= N; i++)
+            for (int j = 0; j <= N; j++)
+                if (connectionMap[i][j] & (BOND_CONNECT | CONSTRAINT_CONNECT)) {
+                    t[3 * k] = i; t[3 * k + 1] = j;
+                    t[3 * k + 2] = connectionMap[i][j] & (BOND_CONNECT | CONSTRAINT_CONNECT);
+                    k++;
+                }
+        sec("connmap", 'i', 3 * cnt, t);
+        free(t);
+    }
+    /* pair tables: table 0 = potentialPairCollision, 1..11 = potentialPairHB[t] */
+    {
+        const int NT = NATOMTYPE + 1;
+        long long ns = 0;
+        for (int t = 0; t < 12; t++)
+            for (int a = 0; a < NT; a++)
+                for (int b = 0; b < NT; b++) {
+                    struct ConstraintStr *c = t == 0 ? &potentialPairCollision[a][b] : &potentialPairHB[t][a][b];
+                    for (struct StepPotenStr *s = c->step; s; s = s->next) ns++;
+                }
+        int *soff = calloc(12 * NT * NT, sizeof(int)), *sn = calloc(12 * NT * NT, sizeof(int));
+        double *pmin = calloc(12 * NT * NT, sizeof(double)), *pmax = calloc(12 * NT * NT, sizeof(double));
+        double *sd = calloc(ns + 1, sizeof(double)), *se = calloc(ns + 1, sizeof(double)),
+               *sa = calloc(ns + 1, sizeof(double));
+        long long m = 0;
+        for (int t = 0; t < 12; t++)
+            for (int a = 0; a < NT; a++)
+                for (int b = 0; b < NT; b++) {
+                    int idx = (t * NT + a) * NT + b;
+                    struct ConstraintStr *c = t == 0 ? &potentialPairCollision[a][b] : &potentialPairHB[t][a][b];
+                    pmin[idx] = c->dmin; pmax[idx] = c->dmax;
+                    soff[idx] = (int)m; sn[idx] = 0;
+                    for (struct StepPotenStr *s = c->step; s; s = s->next) {
+                        sd[m] = s->d; se[m] = s->e; sa[m] = s->accumulated; m++; sn[idx]++;
+                    }
+                }
+        sec("pair_dmin", 'd', 12 * NT * NT, pmin);
+        sec("pair_dmax", 'd', 12 * NT * NT, pmax);
+        sec("pair_step_off", 'i', 12 * NT * NT, soff);
+        sec("pair_step_n", 'i', 12 * NT * NT, sn);
+        sec("pair_step_d", 'd', ns, sd);
+        sec("pair_step_e", 'd', ns, se);
+        sec("pair_step_acc", 'd', ns, sa);
+        free(soff); free(sn); free(pmin); free(pmax); free(sd); free(se); free(sa);
+    }
+    if (wall) {
+        sec("wall_pos", 'd', 3, &wall[0].dynamic->coordinate[1]);
+        sec("wall_vel", 'd', 3, &wall[0].dynamic->velocity[1]);
+        sec_i("wall_type", wall[0].property->typeofAtom);
+        sec_d("wall_mass", wall[0].property->mass);
+    }
+    free(v); free(d);
+}
+
+/* ---- per-pop trace ---- */
+typedef struct {
+    int target, partner, type, sub, executed, hb_itype_after;
+    int t_new_partner, t_new_type, p_new_partner, p_new_type, pad0, pad1;
+    double dt, time_now;
+    double vt[3], vp[3];
+    double t_new_time, p_new_time;
+} trace_rec;
+
+int main(int argc, const char *argv[]) {
+    if (argc < 5 || strcmp(argv[4], "--")) {
+        fprintf(stderr, "usage: %s <out_dir> <n_events> <ckpts|-> -- <sDMD args>\n", argv[0]);
+        return 2;
+    }
+    const char *outdir = argv[1];
+    long n_events = atol(argv[2]);
+    long ckpts[64]; int nck = 0;
+    if (strcmp(argv[3], "-")) {
+        char buf[1024]; snprintf(buf, sizeof(buf), "%s", argv[3]);
+        for (char *tok = strtok(buf, ","); tok && nck < 64; tok = strtok(NULL, ",")) ckpts[nck++] = atol(tok);
+    }
+    /* sDMD sees argv[0] followed by the args after "--" */
+    int sargc = argc - 4;
+    const char **sargv = (const char **)calloc(sargc + 1, sizeof(char *));
+    sargv[0] = argv[0];
+    for (int i = 5; i < argc; i++) sargv[i - 4] = argv[i];
+
+    InputData(sargc, sargv);
+    if (strcmp("new", neworcontinue)) { fprintf(stderr, "harness supports new runs only\n"); return 2; }
+
+    /* ---- Prepare(), src/SGThread.c:21-64, with a dump before the full sweep ---- */
+    InitializeFiles(NULL, fileList);
+    SaveData(lgf, fileList);
+    atomList.ptr = (struct AtomStr **)calloc(atomnum + 1, sizeof(struct AtomStr *));
+    for (int i = 1; i <= atomnum; i++) atomList.ptr[i] = &atom[i];
+    SaveData(sysInfo, fileList);
+    if (strcmp(wallExist, "smooth") == 0) SaveData(wallInfo, fileList);
+    SDEnergyMin(20000, &atomList);
+    PBC("full", NULL, &atomList);
+    LinkList("full", NULL, NULL, &atomList);
+
+    open_out(outdir, "pre.bin");
+    dump_static();
+    dump_dynamic();
+    close_out();
+
+    {
+        int *renew = calloc(atomnum + 2, sizeof(int));
+        for (int i = 1; i <= atomnum; i++) renew[i] = i;
+        Predict(renew, &atomList);
+        free(renew);
+    }
+    open_out(outdir, "sweep.bin");
+    dump_dynamic();
+    close_out();
+
+    CreateCBT();
+    open_out(outdir, "cbt.bin");
+    sec("cbt_node", 'i', 2 * atomnum, CBT.node);
+    sec("cbt_leaf", 'i', atomnum + 1, CBT.leaf);
+    close_out();
+
+    /* ---- SingleThreadRun(), src/SGThread.c:67-155, without dumps/progress ---- */
+    long cap = 1024, ntr = 0;
+    trace_rec *tr = malloc(sizeof(trace_rec) * cap);
+    int renewList[256] = {0};
+    struct AtomListStr *thisList = &atomList;
+    struct AtomStr *target, *partner;
+    int ck = 0;
+    while (currenttime <= timestep && frame < n_events) {
+        AssignJob(&target, &partner, renewList, thisList);
+        UpdateData(thisList->timeInr);
+        TimeForward(thisList->timeInr);
+        currenttime += thisList->timeInr;
+        int hazard = HazardCheck(target, partner, thisList->ptr[target->dynamic->HB.neighbor],
+                                 partner ? thisList->ptr[partner->dynamic->HB.neighbor] : NULL, thisList);
+        if (ntr == cap) { cap *= 2; tr = realloc(tr, sizeof(trace_rec) * cap); }
+        trace_rec *r = &tr[ntr++];
+        memset(r, 0, sizeof(*r));
+        r->target = target->property->num;
+        r->partner = target->dynamic->event.partner;
+        r->type = target->dynamic->event.eventType;
+        r->sub = target->dynamic->event.subEventType;
+        r->dt = thisList->timeInr;
+        r->time_now = currenttime;
+        if (!hazard) {
+            frame++;
+            DoEvent(thisList);
+            target->dynamic->event.counter++;
+            if (renewList[0] == 2 && strcmp(partner->property->extraProperty[1], "_CONS"))
+                partner->dynamic->event.counter++;
+            Predict(renewList, thisList);
+            UpdateCBT(renewList);
+            r->executed = 1;
+        } else {
+            renewList[0] = 1; renewList[2] = 0; renewList[3] = 0;
+            Predict(renewList, thisList);
+            UpdateCBT(renewList);
+            countReCal++;
+        }
+        r->hb_itype_after = target->dynamic->HB.interactionType;
+        for (int n = 0; n < 3; n++) r->vt[n] = target->dynamic->velocity[n + 1];
+        r->t_new_time = target->dynamic->event.time;
+        r->t_new_partner = target->dynamic->event.partner;
+        r->t_new_type = target->dynamic->event.eventType;
+        if (partner) {
+            for (int n = 0; n < 3; n++) r->vp[n] = partner->dynamic->velocity[n + 1];
+            r->p_new_time = partner->dynamic->event.time;
+            r->p_new_partner = partner->dynamic->event.partner;
+            r->p_new_type = partner->dynamic->event.eventType;
+        }
+        if (r->executed && ck < nck && frame == ckpts[ck]) {
+            char name[64];
+            snprintf(name, sizeof(name), "ckpt_%ld.bin", ckpts[ck]);
+            open_out(outdir, name);
+            dump_dynamic();
+            close_out();
+            ck++;
+        }
+    }
+    open_out(outdir, "trace.bin");
+    {
+        int *iv = malloc(sizeof(int) * 12 * (ntr + 1));
+        double *dv = malloc(sizeof(double) * 10 * (ntr + 1));
+        for (long k = 0; k < ntr; k++) {
+            memcpy(iv + 12 * k, &tr[k].target, sizeof(int) * 12);
+            memcpy(dv + 10 * k, &tr[k].dt, sizeof(double) * 10);
+        }
+        sec("trace_i", 'i', 12 * ntr, iv);
+        sec("trace_d", 'd', 10 * ntr, dv);
+        free(iv); free(dv);
+    }
+    close_out();
+    open_out(outdir, "final.bin");
+    dump_dynamic();
+    close_out();
+    printf("harness: %ld pops, %ld executed, %ld denied, rand calls %lld, t=%.6f\n",
+           ntr, frame, countReCal, g_rand_calls, currenttime);
+    return 0;
+}

@@ -1,0 +1,263 @@
+"""Host-side mirror of the C ABI structs in include/sdmd_gpu.h.
+
+`System` owns the numpy arrays of one simulated system (atom ids 1..N, entry 0
+unused, as in the reference's atom[1..atomnum]) and exposes a ctypes
+`sdmd_system` pointing into them.  The arrays are the reference's state
+restated as SoA: `x` is atom[i].dynamic->coordinate[1], `ev_time` is
+atom[i].dynamic->event.time, `cell_list` is the reference's celllist, and so on
+(src/DMD.h:231-466).
+"""
+import ctypes as C
+
+import numpy as np
+
+NTYPES = 33
+NTABLES = 12
+
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+f64p = C.POINTER(C.c_double)
+
+
+class sdmd_rng(C.Structure):
+    _fields_ = [("tab", C.c_int32 * 31), ("front", C.c_int32), ("rear", C.c_int32)]
+
+
+class sdmd_counters(C.Structure):
+    _fields_ = [("frame", C.c_int64), ("recal", C.c_int64), ("collision", C.c_int64), ("bond", C.c_int64),
+                ("hb", C.c_int64), ("hbneighbor", C.c_int64), ("thermostat", C.c_int64), ("pcc", C.c_int64),
+                ("wall", C.c_int64), ("warnings", C.c_int64), ("hb_formed", C.c_int32),
+                ("alpha_hb_formed", C.c_int32)]
+
+
+# (field name, ctypes type); array fields are listed with their numpy dtype below
+_SCALARS_HEAD = [("n_atoms", C.c_int32), ("cellnum", C.c_int32 * 3), ("n_bonds", C.c_int32),
+                 ("n_cons", C.c_int32), ("n_con_steps", C.c_int32), ("n_conn", C.c_int32),
+                 ("n_pair_steps", C.c_int32),
+                 ("box", C.c_double * 3), ("cellsize", C.c_double * 3), ("cutoff", C.c_double),
+                 ("temperature", C.c_double), ("thermo_freq", C.c_double), ("t_end", C.c_double),
+                 ("thermostat", C.c_int32), ("wall", C.c_int32), ("wall_pos", C.c_double * 3),
+                 ("wall_vel", C.c_double * 3), ("wall_mass", C.c_double), ("wall_type", C.c_int32),
+                 ("hb_barrier", C.c_double * 3)]
+
+STATIC_ARRAYS = [("mass", np.float64), ("protein", np.int32), ("aanum", np.int32), ("aatype", np.int32),
+                 ("hb_neighbor", np.int32), ("hb_role", np.int32), ("name_code", np.int32),
+                 ("bond_off", np.int32), ("bond_j", np.int32), ("bond_dmin", np.float64), ("bond_dmax", np.float64),
+                 ("con_off", np.int32), ("con_j", np.int32), ("con_step_off", np.int32), ("con_step_n", np.int32),
+                 ("con_dmin", np.float64), ("con_dmax", np.float64), ("con_step_d", np.float64),
+                 ("con_step_e", np.float64), ("con_step_acc", np.float64),
+                 ("conn_off", np.int32), ("conn_j", np.int32), ("conn_bits", np.int32),
+                 ("pair_dmin", np.float64), ("pair_dmax", np.float64), ("pair_step_off", np.int32),
+                 ("pair_step_n", np.int32), ("pair_step_d", np.float64), ("pair_step_e", np.float64),
+                 ("pair_step_acc", np.float64)]
+
+DYNAMIC_ARRAYS = [("x", np.float64), ("y", np.float64), ("z", np.float64), ("vx", np.float64),
+                  ("vy", np.float64), ("vz", np.float64), ("cx", np.int32), ("cy", np.int32), ("cz", np.int32),
+                  ("type", np.int32), ("hb_bond", np.int32), ("hb_itype", np.int32), ("nb_partner", np.int32),
+                  ("nb_status", np.int32), ("nb_pnum", np.int32), ("ev_time", np.float64),
+                  ("ev_partner", np.int32), ("ev_counter", np.int64), ("ev_pcounter", np.int64),
+                  ("ev_potential", np.float64), ("ev_type", np.int32), ("ev_sub", np.int32),
+                  ("cell_list", np.int32)]
+
+_PTR = {np.float64: f64p, np.int32: i32p, np.int64: i64p}
+
+
+class sdmd_system(C.Structure):
+    _fields_ = (_SCALARS_HEAD
+                + [(n, _PTR[t]) for n, t in STATIC_ARRAYS]
+                + [(n, _PTR[t]) for n, t in DYNAMIC_ARRAYS]
+                + [("time", C.c_double), ("rng", sdmd_rng), ("counters", sdmd_counters)])
+
+
+class sdmd_trace_rec(C.Structure):
+    _fields_ = [("target", C.c_int32), ("partner", C.c_int32), ("type", C.c_int32), ("sub", C.c_int32),
+                ("executed", C.c_int32), ("hb_itype_after", C.c_int32), ("t_new_partner", C.c_int32),
+                ("t_new_type", C.c_int32), ("p_new_partner", C.c_int32), ("p_new_type", C.c_int32),
+                ("system", C.c_int32), ("pad", C.c_int32), ("dt", C.c_double), ("time_now", C.c_double),
+                ("vt", C.c_double * 3), ("vp", C.c_double * 3), ("t_new_time", C.c_double),
+                ("p_new_time", C.c_double)]
+
+
+TRACE_DTYPE = np.dtype([("target", np.int32), ("partner", np.int32), ("type", np.int32), ("sub", np.int32),
+                        ("executed", np.int32), ("hb_itype_after", np.int32), ("t_new_partner", np.int32),
+                        ("t_new_type", np.int32), ("p_new_partner", np.int32), ("p_new_type", np.int32),
+                        ("system", np.int32), ("pad", np.int32), ("dt", np.float64), ("time_now", np.float64),
+                        ("vt", np.float64, 3), ("vp", np.float64, 3), ("t_new_time", np.float64),
+                        ("p_new_time", np.float64)])
+assert TRACE_DTYPE.itemsize == C.sizeof(sdmd_trace_rec)
+
+
+class sdmd_opts(C.Structure):
+    _fields_ = [("advance", C.c_int32), ("screen", C.c_int32), ("threads_per_system", C.c_int32),
+                ("device", C.c_int32), ("trace_capacity", C.c_int32), ("reserved", C.c_int32 * 7)]
+
+
+class sdmd_error_info(C.Structure):
+    _fields_ = [("code", C.c_int32), ("system", C.c_int32), ("atom", C.c_int32), ("event", C.c_int64)]
+
+
+WALL = {"no": 0, "parallel": 1, "cylinder": 2, "sphere": 3}
+
+
+class System:
+    """Arrays of one system plus its ctypes view.  Construct with `from_arrays`."""
+
+    def __init__(self):
+        self.a = {}
+        self.scal = {}
+        self.rng = np.zeros(33, np.int32)
+        self.counters = {}
+        self.time = 0.0
+        self._struct = None
+
+    @property
+    def n(self):
+        return int(self.scal["n_atoms"])
+
+    def copy(self):
+        o = System()
+        o.a = {k: v.copy() for k, v in self.a.items()}
+        o.scal = dict(self.scal)
+        o.rng = self.rng.copy()
+        o.counters = dict(self.counters)
+        o.time = self.time
+        return o
+
+    def struct(self):
+        """ctypes sdmd_system viewing this object's arrays (rebuilt each call; the
+        scalars are copied in, the arrays are shared)."""
+        s = sdmd_system()
+        for k, v in self.scal.items():
+            if isinstance(v, (list, tuple, np.ndarray)):
+                arr = getattr(s, k)
+                for i, x in enumerate(v):
+                    arr[i] = x
+            else:
+                setattr(s, k, v)
+        for name, dt in STATIC_ARRAYS + DYNAMIC_ARRAYS:
+            arr = self.a[name]
+            assert arr.dtype == dt and arr.flags.c_contiguous, name
+            setattr(s, name, arr.ctypes.data_as(_PTR[dt]))
+        s.time = self.time
+        for i in range(31):
+            s.rng.tab[i] = int(self.rng[i])
+        s.rng.front = int(self.rng[31])
+        s.rng.rear = int(self.rng[32])
+        for k, v in self.counters.items():
+            setattr(s.counters, k, int(v))
+        self._struct = s
+        return s
+
+    def pull_scalars(self, s):
+        """Copy dynamic scalars (time, RNG, counters) back from a ctypes struct."""
+        self.time = s.time
+        self.rng[:31] = np.array(s.rng.tab[:], np.int32)
+        self.rng[31] = s.rng.front
+        self.rng[32] = s.rng.rear
+        for k, _ in sdmd_counters._fields_:
+            self.counters[k] = getattr(s.counters, k)
+
+    def state_digest(self):
+        """Everything the loop mutates, for exact comparisons."""
+        keys = ["x", "y", "z", "vx", "vy", "vz", "cx", "cy", "cz", "type", "hb_bond", "hb_itype", "nb_partner",
+                "nb_status", "nb_pnum", "ev_time", "ev_partner", "ev_counter", "ev_pcounter", "ev_potential",
+                "ev_type", "ev_sub", "cell_list"]
+        return {k: self.a[k].copy() for k in keys}
+
+
+def _conn_rows(n, triples):
+    """Sparse (i, j, bits) triples -> CSR (off[N+2], j[], bits[]) rows for i = 0..N."""
+    t = np.asarray(triples, np.int32).reshape(-1, 3)
+    order = np.lexsort((t[:, 1], t[:, 0]))
+    t = t[order]
+    counts = np.bincount(t[:, 0], minlength=n + 1)[: n + 1]
+    off = np.zeros(n + 2, np.int32)
+    off[1:] = np.cumsum(counts)
+    return off, t[:, 1].copy(), t[:, 2].copy()
+
+
+def from_fixture(npz, stage="pre", dynamic_stage=None):
+    """Build a System from a golden fixture (tests/golden/*.npz).  Static data
+    comes from `stage` ("pre"); dynamic state from `dynamic_stage` (default the
+    same stage)."""
+    d = npz
+    g = lambda k: d[f"pre/{k}"]
+    ds = dynamic_stage or stage
+    h = lambda k: d[f"{ds}/{k}"]
+    n = int(g("atomnum")[0])
+    s = System()
+    cellnum = [int(v) for v in g("cellnum")]
+    wall_exist = bytes(g("wallExist")).decode()
+    wall_type = bytes(g("wallType")).decode()
+    wall = 0
+    if wall_exist.startswith("sm"):
+        wall = {"p": 1, "c": 2, "s": 3}.get(wall_type[:1], 0)
+    hbp = g("HBPotential")   # BB_r BB_v SS_r SS_v BS_r BS_v
+    s.scal = dict(n_atoms=n, cellnum=cellnum, box=[float(v) for v in g("box")],
+                  cellsize=[float(v) for v in g("cellsize")], cutoff=float(g("cutoffr")[0]),
+                  temperature=float(g("targetTemperature")[0]), thermo_freq=float(g("thermoF")[0]),
+                  t_end=float(g("timestep")[0]),
+                  thermostat=0 if bytes(g("thermostatType")).decode() == "no" else 1,
+                  wall=wall, wall_pos=[0.0, 0.0, 0.0], wall_vel=[0.0, 0.0, 0.0], wall_mass=0.0, wall_type=0,
+                  hb_barrier=[float(hbp[1]), float(hbp[5]), float(hbp[3])])
+    if wall and "pre/wall_pos" in d.files:
+        s.scal.update(wall_pos=[float(v) for v in g("wall_pos")], wall_vel=[float(v) for v in g("wall_vel")],
+                      wall_mass=float(g("wall_mass")[0]), wall_type=int(g("wall_type")[0]))
+    a = s.a
+    a["mass"] = g("mass").astype(np.float64)
+    a["protein"] = g("protein").astype(np.int32)
+    a["aanum"] = g("aanum").astype(np.int32)
+    a["aatype"] = g("typeofAA").astype(np.int32)
+    a["hb_neighbor"] = g("hb_neighbor").astype(np.int32)
+    a["hb_role"] = g("hb_role").astype(np.int32)
+    names = g("name").reshape(-1, 8)
+    code = np.zeros(n + 1, np.int32)
+    for i in range(1, n + 1):
+        nm = bytes(names[i]).split(b"\0", 1)[0]
+        code[i] = 1 if nm == b"H" else (2 if nm == b"O" else 0)
+    a["name_code"] = code
+    for k in ["bond_off", "bond_j", "con_off", "con_j", "con_step_off", "con_step_n", "pair_step_off", "pair_step_n"]:
+        a[k] = g(k).astype(np.int32)
+    for k in ["bond_dmin", "bond_dmax", "con_dmin", "con_dmax", "con_step_d", "con_step_e", "con_step_acc",
+              "pair_dmin", "pair_dmax", "pair_step_d", "pair_step_e", "pair_step_acc"]:
+        a[k] = g(k).astype(np.float64)
+    a["bond_off"][0] = 0
+    a["con_off"][0] = 0
+    a["conn_off"], a["conn_j"], a["conn_bits"] = _conn_rows(n, g("connmap"))
+    _load_dynamic(s, d, ds)
+    s.rng = d["meta/rng_pre"].astype(np.int32).copy() if ds == "pre" else np.zeros(33, np.int32)
+    for k, v in [("n_bonds", len(a["bond_j"])), ("n_cons", len(a["con_j"])), ("n_con_steps", len(a["con_step_d"])),
+                 ("n_conn", len(a["conn_j"])), ("n_pair_steps", len(a["pair_step_d"]))]:
+        s.scal[k] = int(v)
+    return s
+
+
+def _load_dynamic(s, d, ds):
+    a = s.a
+    h = lambda k: d[f"{ds}/{k}"]
+    for k in ["x", "y", "z", "vx", "vy", "vz", "ev_time", "ev_potential"]:
+        a[k] = h(k).astype(np.float64).copy()
+    for k in ["cx", "cy", "cz", "type", "hb_bond", "hb_itype", "nb_status", "nb_pnum", "ev_partner", "ev_type",
+              "ev_sub", "celllist"]:
+        a["cell_list" if k == "celllist" else k] = h(k).astype(np.int32).copy()
+    a["ev_counter"] = h("ev_counter").astype(np.int64).copy()
+    a["ev_pcounter"] = h("ev_pcounter").astype(np.int64).copy()
+    nb = np.stack([h(f"nb_p{k}") for k in range(1, 5)], axis=1).astype(np.int32)
+    a["nb_partner"] = np.ascontiguousarray(nb.reshape(-1))
+    s.time = float(h("currenttime")[0])
+    ec = h("event_counts")
+    s.counters = dict(frame=int(h("frame")[0]), recal=int(h("countReCal")[0]), collision=int(ec[0]),
+                      bond=int(ec[1]), hb=int(ec[2]), hbneighbor=int(ec[3]), thermostat=int(ec[4]), pcc=int(ec[5]),
+                      wall=int(ec[6]), warnings=int(h("warningsum")[0]), hb_formed=int(h("HBnumformed")[0]),
+                      alpha_hb_formed=int(h("alphaHBformed")[0]))
+
+
+def fixture_dynamic(npz, stage):
+    """Reference dynamic state of a fixture stage as a {name: array} dict in the
+    System naming (for comparisons)."""
+    s = System()
+    _load_dynamic(s, npz, stage)
+    out = dict(s.a)
+    out["_time"] = s.time
+    out["_counters"] = s.counters
+    return out
