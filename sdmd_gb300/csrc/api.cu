@@ -1,0 +1,469 @@
+// api.cu -- the C ABI of include/sdmd_gpu.h.
+//
+// A handle owns one device arena holding every system's SoA arrays, the event
+// trees, per-system scalars (clock, RNG, counters, error word) and the optional
+// pop trace.  Launches go to the handle's own stream and are timed with CUDA
+// events on that stream.  Nothing here falls back to the CPU: without a usable
+// device every entry point returns SDMD_ENODEV / SDMD_ECUDA.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "dev.cuh"
+#include "engine.h"
+#include "sdmd_gpu.h"
+
+using namespace sdmd;
+
+struct SysMeta {
+    int32_t n, ncell, n_bonds, n_cons, n_con_steps, n_conn, n_pair_steps, nbcap;
+};
+
+struct sdmd_gpu {
+    int32_t n_systems = 0;
+    sdmd_opts opts{};
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<DSys> hs;
+    std::vector<SysMeta> meta;
+    DSys *ds = nullptr;
+    unsigned char *arena = nullptr;
+    size_t arena_bytes = 0;
+    int threads = 128;
+    size_t smem = 0;
+    double prep_ms = 0, run_ms = 0;
+    sdmd_error_info err{};
+};
+
+static int cuda_fail(cudaError_t e) {
+    if (e == cudaSuccess) return SDMD_OK;
+    fprintf(stderr, "sdmd_gpu: CUDA error %s\n", cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? SDMD_ENOMEM : SDMD_ECUDA;
+}
+#define CK(x) do { int _r = cuda_fail(x); if (_r) return _r; } while (0)
+
+extern "C" int sdmd_gpu_abi_version(void) { return SDMD_ABI_VERSION; }
+
+extern "C" int sdmd_gpu_device_count(int32_t *count) {
+    int c = 0;
+    cudaError_t e = cudaGetDeviceCount(&c);
+    if (count) *count = (e == cudaSuccess) ? c : 0;
+    if (e != cudaSuccess || c == 0) return SDMD_ENODEV;
+    return SDMD_OK;
+}
+
+extern "C" const char *sdmd_gpu_strerror(int code) {
+    switch (code) {
+        case SDMD_OK: return "ok";
+        case SDMD_EINVAL: return "invalid argument";
+        case SDMD_ENOMEM: return "out of memory";
+        case SDMD_ECUDA: return "CUDA runtime error";
+        case SDMD_ENODEV: return "no CUDA device";
+        case SDMD_ENEGTIME: return "predicted event time is negative";
+        case SDMD_ENAN: return "phi is NaN in a velocity update";
+        case SDMD_EWALL: return "an atom is outside of the wall";
+        case SDMD_ELINK: return "the cell list has errors";
+        case SDMD_EHBMAP: return "HB bookkeeping or pair table is inconsistent";
+        case SDMD_ECAPACITY: return "a fixed device capacity was exceeded";
+        case SDMD_ETIMEOUT: return "a bounded device-side loop ran out (degenerate RNG state or stuck event loop)";
+        case SDMD_EUNSUPPORTED: return "configuration outside the engine's scope";
+        case SDMD_EEVENTTYPE: return "invalid event type popped";
+        default: return "unknown error";
+    }
+}
+
+// ---- validation ---------------------------------------------------------------
+static int validate(const sdmd_system &s) {
+    if (s.n_atoms <= 0 || s.cellnum[0] < 1 || s.cellnum[1] < 1 || s.cellnum[2] < 1) return SDMD_EINVAL;
+    const void *ptrs[] = {s.mass, s.protein, s.aanum, s.aatype, s.hb_neighbor, s.hb_role, s.name_code,
+                          s.bond_off, s.con_off, s.conn_off, s.pair_dmin, s.pair_dmax, s.pair_step_off,
+                          s.pair_step_n, s.x, s.y, s.z, s.vx, s.vy, s.vz, s.cx, s.cy, s.cz, s.type, s.hb_bond,
+                          s.hb_itype, s.nb_partner, s.nb_status, s.nb_pnum, s.ev_time, s.ev_partner,
+                          s.ev_counter, s.ev_pcounter, s.ev_potential, s.ev_type, s.ev_sub, s.cell_list};
+    for (const void *p : ptrs) if (!p) return SDMD_EINVAL;
+    int N = s.n_atoms;
+    if (s.bond_off[N + 1] != s.n_bonds || s.con_off[N + 1] != s.n_cons || s.conn_off[N + 1] != s.n_conn)
+        return SDMD_EINVAL;
+    if ((s.n_bonds && (!s.bond_j || !s.bond_dmin || !s.bond_dmax)) ||
+        (s.n_cons && (!s.con_j || !s.con_dmin || !s.con_dmax || !s.con_step_off || !s.con_step_n)) ||
+        (s.n_conn && (!s.conn_j || !s.conn_bits)))
+        return SDMD_EINVAL;
+    if (s.wall < 0 || s.wall > SDMD_WALL_SPHERE || s.thermostat < 0 || s.thermostat > 1) return SDMD_EUNSUPPORTED;
+    // the RNG must be a reachable glibc state: never all zero
+    bool nz = false;
+    for (int k = 0; k < 31; k++) nz |= s.rng.tab[k] != 0;
+    if (!nz || s.rng.front < 0 || s.rng.front > 30 || s.rng.rear < 0 || s.rng.rear > 30) return SDMD_EINVAL;
+    // every index the kernels dereference must be in range
+    auto atom_ok = [N](int a) { return a >= 0 && a <= N; };
+    for (int k = 0; k < s.n_bonds; k++) if (s.bond_j[k] < 1 || s.bond_j[k] > N) return SDMD_EINVAL;
+    for (int k = 0; k < s.n_cons; k++) {
+        if (s.con_j[k] < 1 || s.con_j[k] > N || s.con_step_n[k] < 0 || s.con_step_off[k] < 0 ||
+            s.con_step_off[k] + s.con_step_n[k] > s.n_con_steps)
+            return SDMD_EINVAL;
+        if (s.con_step_n[k] && (!s.con_step_d || !s.con_step_e || !s.con_step_acc)) return SDMD_EINVAL;
+    }
+    for (int k = 0; k < s.n_conn; k++) if (!atom_ok(s.conn_j[k])) return SDMD_EINVAL;
+    const int NT3 = SDMD_NTABLES * SDMD_NTYPES * SDMD_NTYPES;
+    for (int k = 0; k < NT3; k++) {
+        if (s.pair_step_n[k] < 0 || s.pair_step_off[k] < 0 || s.pair_step_off[k] + s.pair_step_n[k] > s.n_pair_steps)
+            return SDMD_EINVAL;
+    }
+    if (s.n_pair_steps && (!s.pair_step_d || !s.pair_step_e || !s.pair_step_acc)) return SDMD_EINVAL;
+    if (s.bond_off[0] < 0 || s.con_off[0] < 0 || s.conn_off[0] < 0) return SDMD_EINVAL;
+    for (int k = 1; k <= N + 1; k++) {
+        if (s.bond_off[k] < s.bond_off[k - 1] || s.con_off[k] < s.con_off[k - 1] || s.conn_off[k] < s.conn_off[k - 1])
+            return SDMD_EINVAL;
+    }
+    if (s.wall && (s.wall_type < 0 || s.wall_type >= SDMD_NTYPES)) return SDMD_EINVAL;
+    long ncell = (long)s.cellnum[0] * s.cellnum[1] * s.cellnum[2];
+    for (long k = 0; k <= N + ncell; k++) if (!atom_ok(s.cell_list[k])) return SDMD_EINVAL;
+    // every atom must sit in a valid cell, with in-range ids and types
+    for (int i = 1; i <= N; i++) {
+        if (!atom_ok(s.hb_neighbor[i]) || !atom_ok(s.hb_bond[i]) || s.type[i] < 0 || s.type[i] >= SDMD_NTYPES)
+            return SDMD_EINVAL;
+        if (!(s.ev_partner[i] <= 0 || s.ev_partner[i] <= N)) return SDMD_EINVAL;
+        for (int q = 0; q < 4; q++) if (!atom_ok(s.nb_partner[4 * i + q])) return SDMD_EINVAL;
+        if (!(s.mass[i] > 0)) return SDMD_EINVAL;
+        if (s.cx[i] < 0 || s.cx[i] >= s.cellnum[0] || s.cy[i] < 0 || s.cy[i] >= s.cellnum[1] || s.cz[i] < 0 ||
+            s.cz[i] >= s.cellnum[2])
+            return SDMD_EINVAL;
+        if (s.nb_status[i] < 0 || s.nb_status[i] > 4) return SDMD_EINVAL;
+    }
+    return SDMD_OK;
+}
+
+// largest 27-cell neighbourhood population at upload time
+static int max_neighbourhood(const sdmd_system &s) {
+    int N = s.n_atoms, cn0 = s.cellnum[0], cn1 = s.cellnum[1], cn2 = s.cellnum[2];
+    long ncell = (long)cn0 * cn1 * cn2;
+    std::vector<int> occ(ncell + 1, 0);
+    for (long c = 1; c <= ncell; c++) {
+        int k = 0;
+        for (int a = s.cell_list[N + c]; a && k <= N; a = s.cell_list[a]) k++;
+        occ[c] = k;
+    }
+    int best = 0;
+    for (int z = 0; z < cn2; z++)
+        for (int y = 0; y < cn1; y++)
+            for (int x = 0; x < cn0; x++) {
+                int tot = 0;
+                for (int dz = -1; dz <= 1; dz++)
+                    for (int dy = -1; dy <= 1; dy++)
+                        for (int dx = -1; dx <= 1; dx++) {
+                            int a = (x + dx + cn0) % cn0, b = (y + dy + cn1) % cn1, c = (z + dz + cn2) % cn2;
+                            tot += occ[(long)c * cn0 * cn1 + (long)b * cn0 + a + 1];
+                        }
+                if (tot > best) best = tot;
+            }
+    return best;
+}
+
+// ---- arena carving --------------------------------------------------------------
+struct Carver {
+    unsigned char *base;
+    size_t off;
+    template <class T> T *take(size_t count) {
+        off = (off + 255) & ~size_t(255);
+        T *p = reinterpret_cast<T *>(base + off);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+template <class T> static void put(std::vector<std::pair<void *, std::pair<const void *, size_t>>> &cp, T *dst,
+                                   const T *src, size_t count) {
+    if (count && src) cp.push_back({(void *)dst, {(const void *)src, count * sizeof(T)}});
+}
+
+static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
+                     std::vector<std::pair<void *, std::pair<const void *, size_t>>> *copies) {
+    Carver cv{base, 0};
+    const int trace_cap = h->opts.trace_capacity > 0 ? h->opts.trace_capacity : 0;
+    for (int k = 0; k < h->n_systems; k++) {
+        const sdmd_system &s = sys[k];
+        const SysMeta &m = h->meta[k];
+        DSys &d = h->hs[k];
+        size_t N1 = (size_t)m.n + 1, NT3 = (size_t)SDMD_NTABLES * SDMD_NTYPES * SDMD_NTYPES;
+        d.mass = cv.take<double>(N1);
+        d.protein = cv.take<int32_t>(N1); d.aanum = cv.take<int32_t>(N1); d.aatype = cv.take<int32_t>(N1);
+        d.hb_neighbor = cv.take<int32_t>(N1); d.hb_role = cv.take<int32_t>(N1); d.name_code = cv.take<int32_t>(N1);
+        d.bond_off = cv.take<int32_t>(N1 + 1); d.bond_j = cv.take<int32_t>(m.n_bonds + 1);
+        d.bond_dmin = cv.take<double>(m.n_bonds + 1); d.bond_dmax = cv.take<double>(m.n_bonds + 1);
+        d.con_off = cv.take<int32_t>(N1 + 1); d.con_j = cv.take<int32_t>(m.n_cons + 1);
+        d.con_step_off = cv.take<int32_t>(m.n_cons + 1); d.con_step_n = cv.take<int32_t>(m.n_cons + 1);
+        d.con_dmin = cv.take<double>(m.n_cons + 1); d.con_dmax = cv.take<double>(m.n_cons + 1);
+        d.con_step_d = cv.take<double>(m.n_con_steps + 1); d.con_step_e = cv.take<double>(m.n_con_steps + 1);
+        d.con_step_acc = cv.take<double>(m.n_con_steps + 1);
+        d.conn_off = cv.take<int32_t>(N1 + 1); d.conn_j = cv.take<int32_t>(m.n_conn + 1);
+        d.conn_bits = cv.take<int32_t>(m.n_conn + 1);
+        d.pair_dmin = cv.take<double>(NT3); d.pair_dmax = cv.take<double>(NT3);
+        d.pair_step_off = cv.take<int32_t>(NT3); d.pair_step_n = cv.take<int32_t>(NT3);
+        d.pair_step_d = cv.take<double>(m.n_pair_steps + 1); d.pair_step_e = cv.take<double>(m.n_pair_steps + 1);
+        d.pair_step_acc = cv.take<double>(m.n_pair_steps + 1);
+        d.x = cv.take<double>(N1); d.y = cv.take<double>(N1); d.z = cv.take<double>(N1);
+        d.vx = cv.take<double>(N1); d.vy = cv.take<double>(N1); d.vz = cv.take<double>(N1);
+        d.cx = cv.take<int32_t>(N1); d.cy = cv.take<int32_t>(N1); d.cz = cv.take<int32_t>(N1);
+        d.type = cv.take<int32_t>(N1); d.hb_bond = cv.take<int32_t>(N1); d.hb_itype = cv.take<int32_t>(N1);
+        d.nb_partner = cv.take<int32_t>(4 * N1); d.nb_status = cv.take<int32_t>(N1); d.nb_pnum = cv.take<int32_t>(N1);
+        d.ev_time = cv.take<double>(N1); d.ev_partner = cv.take<int32_t>(N1);
+        d.ev_counter = cv.take<int64_t>(N1); d.ev_pcounter = cv.take<int64_t>(N1);
+        d.ev_potential = cv.take<double>(N1); d.ev_type = cv.take<int32_t>(N1); d.ev_sub = cv.take<int32_t>(N1);
+        d.cell_list = cv.take<int32_t>(N1 + m.ncell);
+        d.cbt_node = cv.take<int32_t>(2 * N1 + 2); d.cbt_leaf = cv.take<int32_t>(N1 + 1);
+        d.sc = cv.take<DScal>(1);
+        d.trace = cv.take<sdmd_trace_rec>(trace_cap > 0 ? trace_cap : 1);
+        d.trace_cap = trace_cap;
+        if (copies) {
+            auto &c = *copies;
+            put(c, (double *)d.mass, s.mass, N1);
+            put(c, (int32_t *)d.protein, s.protein, N1); put(c, (int32_t *)d.aanum, s.aanum, N1);
+            put(c, (int32_t *)d.aatype, s.aatype, N1); put(c, (int32_t *)d.hb_neighbor, s.hb_neighbor, N1);
+            put(c, (int32_t *)d.hb_role, s.hb_role, N1); put(c, (int32_t *)d.name_code, s.name_code, N1);
+            put(c, (int32_t *)d.bond_off, s.bond_off, N1 + 1); put(c, (int32_t *)d.bond_j, s.bond_j, (size_t)m.n_bonds);
+            put(c, (double *)d.bond_dmin, s.bond_dmin, (size_t)m.n_bonds);
+            put(c, (double *)d.bond_dmax, s.bond_dmax, (size_t)m.n_bonds);
+            put(c, (int32_t *)d.con_off, s.con_off, N1 + 1); put(c, (int32_t *)d.con_j, s.con_j, (size_t)m.n_cons);
+            put(c, (int32_t *)d.con_step_off, s.con_step_off, (size_t)m.n_cons);
+            put(c, (int32_t *)d.con_step_n, s.con_step_n, (size_t)m.n_cons);
+            put(c, (double *)d.con_dmin, s.con_dmin, (size_t)m.n_cons);
+            put(c, (double *)d.con_dmax, s.con_dmax, (size_t)m.n_cons);
+            put(c, (double *)d.con_step_d, s.con_step_d, (size_t)m.n_con_steps);
+            put(c, (double *)d.con_step_e, s.con_step_e, (size_t)m.n_con_steps);
+            put(c, (double *)d.con_step_acc, s.con_step_acc, (size_t)m.n_con_steps);
+            put(c, (int32_t *)d.conn_off, s.conn_off, N1 + 1); put(c, (int32_t *)d.conn_j, s.conn_j, (size_t)m.n_conn);
+            put(c, (int32_t *)d.conn_bits, s.conn_bits, (size_t)m.n_conn);
+            put(c, (double *)d.pair_dmin, s.pair_dmin, NT3); put(c, (double *)d.pair_dmax, s.pair_dmax, NT3);
+            put(c, (int32_t *)d.pair_step_off, s.pair_step_off, NT3);
+            put(c, (int32_t *)d.pair_step_n, s.pair_step_n, NT3);
+            put(c, (double *)d.pair_step_d, s.pair_step_d, (size_t)m.n_pair_steps);
+            put(c, (double *)d.pair_step_e, s.pair_step_e, (size_t)m.n_pair_steps);
+            put(c, (double *)d.pair_step_acc, s.pair_step_acc, (size_t)m.n_pair_steps);
+        }
+    }
+    return cv.off;
+}
+
+// dynamic arrays of system k: (device pointer, host pointer, bytes) triples
+template <class F> static void for_dynamic(sdmd_gpu *h, int k, const sdmd_system &s, F f) {
+    const DSys &d = h->hs[k];
+    size_t N1 = (size_t)h->meta[k].n + 1;
+    f((void *)d.x, (void *)s.x, N1 * 8); f((void *)d.y, (void *)s.y, N1 * 8); f((void *)d.z, (void *)s.z, N1 * 8);
+    f((void *)d.vx, (void *)s.vx, N1 * 8); f((void *)d.vy, (void *)s.vy, N1 * 8); f((void *)d.vz, (void *)s.vz, N1 * 8);
+    f((void *)d.cx, (void *)s.cx, N1 * 4); f((void *)d.cy, (void *)s.cy, N1 * 4); f((void *)d.cz, (void *)s.cz, N1 * 4);
+    f((void *)d.type, (void *)s.type, N1 * 4); f((void *)d.hb_bond, (void *)s.hb_bond, N1 * 4);
+    f((void *)d.hb_itype, (void *)s.hb_itype, N1 * 4); f((void *)d.nb_partner, (void *)s.nb_partner, 4 * N1 * 4);
+    f((void *)d.nb_status, (void *)s.nb_status, N1 * 4); f((void *)d.nb_pnum, (void *)s.nb_pnum, N1 * 4);
+    f((void *)d.ev_time, (void *)s.ev_time, N1 * 8); f((void *)d.ev_partner, (void *)s.ev_partner, N1 * 4);
+    f((void *)d.ev_counter, (void *)s.ev_counter, N1 * 8); f((void *)d.ev_pcounter, (void *)s.ev_pcounter, N1 * 8);
+    f((void *)d.ev_potential, (void *)s.ev_potential, N1 * 8); f((void *)d.ev_type, (void *)s.ev_type, N1 * 4);
+    f((void *)d.ev_sub, (void *)s.ev_sub, N1 * 4);
+    f((void *)d.cell_list, (void *)s.cell_list, (N1 + h->meta[k].ncell) * 4);
+}
+
+extern "C" void sdmd_gpu_destroy(sdmd_gpu *h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->arena) cudaFree(h->arena);
+    if (h->ds) cudaFree(h->ds);
+    if (h->e0) cudaEventDestroy(h->e0);
+    if (h->e1) cudaEventDestroy(h->e1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, const sdmd_opts *opts, sdmd_gpu **out) {
+    if (!systems || n_systems <= 0 || !out) return SDMD_EINVAL;
+    *out = nullptr;
+    for (int k = 0; k < n_systems; k++) {
+        int r = validate(systems[k]);
+        if (r) return r;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SDMD_ENODEV;
+    sdmd_gpu *h = new sdmd_gpu();
+    if (opts) h->opts = *opts;
+    if (h->opts.device < 0 || h->opts.device >= ndev) { delete h; return SDMD_EINVAL; }
+    if (h->opts.advance != SDMD_ADVANCE_EAGER || h->opts.screen != SDMD_SCREEN_FP64) { delete h; return SDMD_EUNSUPPORTED; }
+    int r = cuda_fail(cudaSetDevice(h->opts.device));
+    if (r) { delete h; return r; }
+    h->n_systems = n_systems;
+    h->hs.resize(n_systems);
+    h->meta.resize(n_systems);
+    int nbcap_max = 0;
+    for (int k = 0; k < n_systems; k++) {
+        const sdmd_system &s = systems[k];
+        SysMeta &m = h->meta[k];
+        m.n = s.n_atoms;
+        m.ncell = s.cellnum[0] * s.cellnum[1] * s.cellnum[2];
+        m.n_bonds = s.n_bonds; m.n_cons = s.n_cons; m.n_con_steps = s.n_con_steps; m.n_conn = s.n_conn;
+        m.n_pair_steps = s.n_pair_steps;
+        int occ = max_neighbourhood(s);
+        m.nbcap = s.n_atoms <= 2048 ? s.n_atoms : std::min(s.n_atoms, std::max(512, 4 * occ + 64));
+        nbcap_max = std::max(nbcap_max, m.nbcap);
+        DSys &d = h->hs[k];
+        memset(&d, 0, sizeof(d));
+        d.n = s.n_atoms; d.ncell = m.ncell;
+        for (int q = 0; q < 3; q++) {
+            d.cn[q] = s.cellnum[q]; d.box[q] = s.box[q]; d.cs[q] = s.cellsize[q];
+            d.wall_pos[q] = s.wall_pos[q]; d.wall_vel[q] = s.wall_vel[q]; d.hb_barrier[q] = s.hb_barrier[q];
+        }
+        d.thermostat = s.thermostat; d.wall = s.wall; d.wall_type = s.wall_type;
+        d.cutoff = s.cutoff; d.temperature = s.temperature; d.thermo_freq = s.thermo_freq; d.t_end = s.t_end;
+        d.nbcap = m.nbcap;
+    }
+    h->smem = fp64_smem_bytes(nbcap_max);
+    h->threads = h->opts.threads_per_system > 0 ? h->opts.threads_per_system : 128;
+    if (h->threads < 32 || h->threads > 1024 || (h->threads & 31)) { delete h; return SDMD_EINVAL; }
+    if (h->smem > 227 * 1024) { delete h; return SDMD_ECAPACITY; }
+    h->arena_bytes = layout(h, systems, nullptr, nullptr) + 256;
+    if ((r = cuda_fail(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) ||
+        (r = cuda_fail(cudaEventCreate(&h->e0))) || (r = cuda_fail(cudaEventCreate(&h->e1))) ||
+        (r = cuda_fail(cudaMalloc(&h->arena, h->arena_bytes))) ||
+        (r = cuda_fail(cudaMalloc(&h->ds, sizeof(DSys) * n_systems)))) {
+        sdmd_gpu_destroy(h);
+        return r;
+    }
+    cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
+    std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
+    layout(h, systems, h->arena, &copies);
+    for (auto &c : copies) cudaMemcpyAsync(c.first, c.second.first, c.second.second, cudaMemcpyHostToDevice, h->stream);
+    std::vector<DScal> sc(n_systems);
+    for (int k = 0; k < n_systems; k++) {
+        const sdmd_system &s = systems[k];
+        for_dynamic(h, k, s, [&](void *dv, void *hp, size_t bytes) {
+            cudaMemcpyAsync(dv, hp, bytes, cudaMemcpyHostToDevice, h->stream);
+        });
+        memset(&sc[k], 0, sizeof(DScal));
+        sc[k].time = s.time; sc[k].rng = s.rng; sc[k].c = s.counters;
+        cudaMemcpyAsync(h->hs[k].sc, &sc[k], sizeof(DScal), cudaMemcpyHostToDevice, h->stream);
+    }
+    cudaMemcpyAsync(h->ds, h->hs.data(), sizeof(DSys) * n_systems, cudaMemcpyHostToDevice, h->stream);
+    if (h->smem > 48 * 1024) {
+        cudaFuncSetAttribute(sweep_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
+        cudaFuncSetAttribute(loop_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
+    }
+    if ((r = cuda_fail(cudaStreamSynchronize(h->stream)))) { sdmd_gpu_destroy(h); return r; }
+    *out = h;
+    return SDMD_OK;
+}
+
+// copy every system's scalar block back and report the first device error
+static int collect_errors(sdmd_gpu *h) {
+    std::vector<DScal> sc(h->n_systems);
+    for (int k = 0; k < h->n_systems; k++)
+        CK(cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < h->n_systems; k++) {
+        if (sc[k].err) {
+            h->err.code = sc[k].err; h->err.system = k; h->err.atom = sc[k].err_atom; h->err.event = sc[k].err_event;
+            return sc[k].err;
+        }
+    }
+    return SDMD_OK;
+}
+
+extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
+    if (!h) return SDMD_EINVAL;
+    CK(cudaSetDevice(h->opts.device));
+    CK(cudaEventRecord(h->e0, h->stream));
+    sweep_kernel_fp64<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->e1, h->stream));
+    CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->prep_ms = ms;
+    return collect_errors(h);
+}
+
+extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
+    if (!h || max_events < 0) return SDMD_EINVAL;
+    CK(cudaSetDevice(h->opts.device));
+    CK(cudaEventRecord(h->e0, h->stream));
+    loop_kernel_fp64<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, max_events, t_end);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->e1, h->stream));
+    CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->run_ms = ms;
+    return collect_errors(h);
+}
+
+extern "C" int sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_systems) {
+    if (!h || !systems || n_systems != h->n_systems) return SDMD_EINVAL;
+    CK(cudaSetDevice(h->opts.device));
+    std::vector<DScal> sc(n_systems);
+    for (int k = 0; k < n_systems; k++) {
+        if (systems[k].n_atoms != h->meta[k].n) return SDMD_EINVAL;
+        for_dynamic(h, k, systems[k], [&](void *dv, void *hp, size_t bytes) {
+            cudaMemcpyAsync(hp, dv, bytes, cudaMemcpyDeviceToHost, h->stream);
+        });
+        cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream);
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < n_systems; k++) {
+        systems[k].time = sc[k].time;
+        systems[k].rng = sc[k].rng;
+        systems[k].counters = sc[k].c;
+    }
+    return SDMD_OK;
+}
+
+extern "C" int sdmd_gpu_trace(sdmd_gpu *h, int32_t s, sdmd_trace_rec *out, int32_t cap, int32_t *n_out) {
+    if (!h || s < 0 || s >= h->n_systems || !out || cap < 0) return SDMD_EINVAL;
+    CK(cudaSetDevice(h->opts.device));
+    DScal sc;
+    CK(cudaMemcpy(&sc, h->hs[s].sc, sizeof(DScal), cudaMemcpyDeviceToHost));
+    int tc = h->hs[s].trace_cap;
+    int64_t have = sc.pops < tc ? sc.pops : tc;
+    int64_t n = have < cap ? have : cap;
+    // the last n records, oldest first
+    for (int64_t q = 0; q < n; q++) {
+        int64_t pop = sc.pops - n + q;
+        CK(cudaMemcpy(&out[q], &h->hs[s].trace[pop % tc], sizeof(sdmd_trace_rec), cudaMemcpyDeviceToHost));
+    }
+    if (n_out) *n_out = (int32_t)n;
+    return SDMD_OK;
+}
+
+extern "C" int sdmd_gpu_last_ms(sdmd_gpu *h, double *prepare_ms, double *run_ms) {
+    if (!h) return SDMD_EINVAL;
+    if (prepare_ms) *prepare_ms = h->prep_ms;
+    if (run_ms) *run_ms = h->run_ms;
+    return SDMD_OK;
+}
+
+extern "C" int sdmd_gpu_last_error(sdmd_gpu *h, sdmd_error_info *info) {
+    if (!h || !info) return SDMD_EINVAL;
+    *info = h->err;
+    return SDMD_OK;
+}
+
+// ---- host-side RNG helpers: glibc srand()/rand() stream -------------------------
+extern "C" void sdmd_rng_seed(sdmd_rng *r, uint32_t seed) {
+    int32_t *t = r->tab;
+    t[0] = seed ? (int32_t)seed : 1;
+    for (int i = 1; i < 31; i++) {   // Lehmer 16807 seeding, Schrage's decomposition
+        long hi = t[i - 1] / 127773, lo = t[i - 1] % 127773;
+        long w = 16807 * lo - 2836 * hi;
+        if (w < 0) w += 2147483647;
+        t[i] = (int32_t)w;
+    }
+    r->front = 3; r->rear = 0;
+    sdmd_rng_skip(r, 310);
+}
+
+extern "C" int32_t sdmd_rng_next(sdmd_rng *r) {
+    uint32_t v = (uint32_t)r->tab[r->front] + (uint32_t)r->tab[r->rear];
+    r->tab[r->front] = (int32_t)v;
+    int32_t out = (int32_t)((v >> 1) & 0x7fffffffu);
+    if (++r->front >= 31) { r->front = 0; ++r->rear; }
+    else if (++r->rear >= 31) r->rear = 0;
+    return out;
+}
+
+extern "C" void sdmd_rng_skip(sdmd_rng *r, int64_t n) {
+    for (int64_t k = 0; k < n; k++) sdmd_rng_next(r);
+}

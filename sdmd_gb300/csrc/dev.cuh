@@ -1,0 +1,354 @@
+// dev.cuh -- device-side system view and the physics of one event loop step.
+//
+// Every function restates a reference routine (file:line given) in FP64 with the
+// reference's association order.  The translation unit is compiled with
+// -fmad=false so that no multiply-add is contracted: results are bit-identical
+// to the reference's x86-64 -O2 build, which has no FMA contraction either.
+#pragma once
+#include <cstdint>
+#include "sdmd_gpu.h"
+
+namespace sdmd {
+
+constexpr double ZERO = SDMD_ZERO;
+constexpr double INFINIT = SDMD_INFINIT;
+constexpr int INVALID = SDMD_INVALID;
+constexpr int NT = SDMD_NTYPES;
+
+// per-system scalars living in device memory
+struct DScal {
+    double time;
+    sdmd_rng rng;
+    sdmd_counters c;
+    int32_t err, err_atom;
+    int64_t err_event;
+    int64_t pops;            // total pops (trace ring position)
+    int32_t cbt_built;
+    int32_t pad;
+};
+
+// one system's device arrays (all 1-based per-atom arrays, entry 0 unused)
+struct DSys {
+    int32_t n, ncell;
+    int32_t cn[3];
+    int32_t thermostat, wall, wall_type;
+    double box[3], cs[3], cutoff, temperature, thermo_freq, t_end;
+    double wall_pos[3], wall_vel[3], hb_barrier[3];
+    // static
+    const double *mass;
+    const int32_t *protein, *aanum, *aatype, *hb_neighbor, *hb_role, *name_code;
+    const int32_t *bond_off, *bond_j;
+    const double *bond_dmin, *bond_dmax;
+    const int32_t *con_off, *con_j, *con_step_off, *con_step_n;
+    const double *con_dmin, *con_dmax, *con_step_d, *con_step_e, *con_step_acc;
+    const int32_t *conn_off, *conn_j, *conn_bits;
+    const double *pair_dmin, *pair_dmax;
+    const int32_t *pair_step_off, *pair_step_n;
+    const double *pair_step_d, *pair_step_e, *pair_step_acc;
+    // dynamic
+    double *x, *y, *z, *vx, *vy, *vz;
+    int32_t *cx, *cy, *cz, *type, *hb_bond, *hb_itype, *nb_partner, *nb_status, *nb_pnum;
+    double *ev_time;
+    int32_t *ev_partner;
+    int64_t *ev_counter, *ev_pcounter;
+    double *ev_potential;
+    int32_t *ev_type, *ev_sub;
+    int32_t *cell_list;
+    int32_t *cbt_node, *cbt_leaf;
+    DScal *sc;
+    sdmd_trace_rec *trace;
+    int32_t trace_cap;
+    int32_t nbcap;           // capacity of the gathered 27-cell neighbour list
+};
+
+// 27-cell scan order of the reference (src/DMD.c:117-121)
+__constant__ int8_t c_nbx[27] = {0, 1, 0, 0, 0, 1, 1, 1, -1, 0, 0, 0, -1, -1, -1, 0, 0, 1, -1, 1, -1, -1, -1, 1, 1, 1, -1};
+__constant__ int8_t c_nby[27] = {0, 0, 1, 0, 1, 0, 1, 1, 0, -1, 0, -1, 0, -1, -1, -1, 1, 0, 0, -1, 1, -1, 1, -1, 1, -1, 1};
+__constant__ int8_t c_nbz[27] = {0, 0, 0, 1, 1, 1, 0, 1, 0, 0, -1, -1, -1, 0, -1, 1, -1, -1, 1, 0, 0, 1, -1, -1, -1, 1, 1};
+
+enum { K_COLLISION = 0, K_CONSTRAINT = 1, K_HB = 2, K_NEIGHBOR = 3 };
+
+// ---------------------------------------------------------------------------
+// glibc-compatible rand(): additive feedback r[i] = r[i-3] + r[i-31] mod 2^32,
+// output r >> 1 (TYPE_3: degree 31, separation 3).
+__device__ inline int32_t rng_next(sdmd_rng &r) {
+    uint32_t v = (uint32_t)r.tab[r.front] + (uint32_t)r.tab[r.rear];
+    r.tab[r.front] = (int32_t)v;
+    int32_t out = (int32_t)((v >> 1) & 0x7fffffffu);
+    if (++r.front >= 31) { r.front = 0; ++r.rear; }
+    else if (++r.rear >= 31) r.rear = 0;
+    return out;
+}
+// RandomValue(0, 1) (src/ToolFunctions.c:517-522)
+__device__ inline double rv01(sdmd_rng &r) { return 0 + (double)rng_next(r) / ((double)2147483647 / (1 - 0)); }
+
+// ---- correctly rounded log: double-double evaluation of e*ln2 + 2*atanh(f) ----
+struct dd { double hi, lo; };
+__device__ inline dd two_sum(double a, double b) {
+    double s = a + b, bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ inline dd quick_two_sum(double a, double b) { double s = a + b; return {s, b - (s - a)}; }
+__device__ inline dd two_prod(double a, double b) { double p = a * b; return {p, fma(a, b, -p)}; }  // exact
+__device__ inline dd dd_add(dd a, dd b) {
+    dd s = two_sum(a.hi, b.hi), t = two_sum(a.lo, b.lo);
+    s.lo += t.hi; s = quick_two_sum(s.hi, s.lo); s.lo += t.lo;
+    return quick_two_sum(s.hi, s.lo);
+}
+__device__ inline dd dd_mul(dd a, dd b) {
+    dd p = two_prod(a.hi, b.hi);
+    p.lo += a.hi * b.lo + a.lo * b.hi;
+    return quick_two_sum(p.hi, p.lo);
+}
+__device__ inline dd inv_odd(int k) {
+    double n = (double)(2 * k + 1), h = 1.0 / n;
+    dd p = two_prod(h, n);
+    double rem = (1.0 - p.hi) - p.lo;
+    return quick_two_sum(h, rem / n);
+}
+// natural log for normal x > 0 (the Box-Muller argument lies in (0, 1))
+__device__ inline double cr_log(double x) {
+    long long bits = __double_as_longlong(x);
+    int e = (int)((bits >> 52) & 0x7ff) - 1023;
+    double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);  // [1, 2)
+    if (m > 1.4142135623730951) { m *= 0.5; e += 1; }
+    double num = m - 1.0;
+    dd den = two_sum(m, 1.0);
+    double q1 = num / den.hi;
+    dd p = dd_mul({q1, 0.0}, den);
+    dd rr = dd_add({num, 0.0}, {-p.hi, -p.lo});
+    dd f = quick_two_sum(q1, rr.hi / den.hi);
+    dd z = dd_mul(f, f);
+    double t = 1.0 / 43.0;
+    for (int k = 20; k >= 11; k--) t = t * z.hi + 1.0 / (double)(2 * k + 1);
+    dd acc = {t, 0.0};
+    for (int k = 10; k >= 0; k--) acc = dd_add(dd_mul(acc, z), inv_odd(k));
+    dd lm = dd_mul(f, acc);
+    lm.hi *= 2.0; lm.lo *= 2.0;
+    const dd LN2 = {0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
+    dd el = dd_add(two_prod((double)e, LN2.hi), {(double)e * LN2.lo, 0.0});
+    dd r = dd_add(el, lm);
+    return r.hi + r.lo;
+}
+// Maxwell_Boltzmann_Distribution (src/ToolFunctions.c:544-569).  The rejection
+// loops are bounded: a healthy stream accepts with probability pi/4 per attempt,
+// so 4096 consecutive rejections only happen for a degenerate (e.g. all-zero)
+// RNG state; *bad is then set and 0 returned instead of spinning.
+__device__ inline double mb_draw(sdmd_rng &r, double mean, double variance, int *bad) {
+    double a, b, s, out = 0;
+    for (int outer = 0; outer < 64; outer++) {
+        int tries = 0;
+        do {
+            a = 2 * rv01(r) - 1;
+            b = 2 * rv01(r) - 1;
+            s = a * a + b * b;
+        } while (s >= 1 && ++tries < 4096);
+        if (s >= 1) { *bad = 1; return 0; }
+        s = sqrt(-2 * cr_log(s) / s);
+        double choose = rv01(r);
+        out = (choose >= 0.5) ? a * s : b * s;
+        if (out != 0) return out * sqrt(variance) + mean;
+    }
+    *bad = 1;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+__device__ inline int cell_lin(const DSys &S, int cx, int cy, int cz) {
+    return cz * S.cn[0] * S.cn[1] + cy * S.cn[0] + cx + 1;
+}
+__device__ inline int nb_cell(const DSys &S, int i, int k) {
+    int c0 = S.cx[i] + c_nbx[k], c1 = S.cy[i] + c_nby[k], c2 = S.cz[i] + c_nbz[k];
+    if (c0 < 0) c0 = S.cn[0] - 1; else if (c0 >= S.cn[0]) c0 = 0;
+    if (c1 < 0) c1 = S.cn[1] - 1; else if (c1 >= S.cn[1]) c1 = 0;
+    if (c2 < 0) c2 = S.cn[2] - 1; else if (c2 >= S.cn[2]) c2 = 0;
+    return cell_lin(S, c0, c1, c2);
+}
+
+// AtomTypeChange (src/ToolFunctions.c:233-270)
+__device__ inline int type_change(int t, int to_hb) {
+    if (to_hb) { if (t == 1) return 3; if (t == 2) return 4; if (t == 26) return 27; }
+    else { if (t == 3) return 1; if (t == 4) return 2; if (t == 27) return 26; }
+    return t;
+}
+__device__ inline int tab_idx(int t, int a, int b) { return (t * NT + a) * NT + b; }
+
+// RightPair (src/ToolFunctions.c:278-292), unrolled recursion
+__device__ inline int right_pair(const DSys &S, int t1, int t2) {
+    if (S.pair_dmin[tab_idx(0, t1, t2)] > 0) return tab_idx(0, t1, t2);
+    int a = type_change(t1, 0), b = type_change(t2, 0);
+    if (S.pair_dmin[tab_idx(0, a, t2)] > 0) return tab_idx(0, a, t2);
+    if (S.pair_dmin[tab_idx(0, t1, b)] > 0) return tab_idx(0, t1, b);
+    if (S.pair_dmin[tab_idx(0, a, b)] > 0) return tab_idx(0, a, b);
+    return -1;
+}
+
+// HBModel (src/Models.c:212-290): class 1..11, -1 "no HB", 0 (with *bad) fatal
+__device__ inline int hb_model(const DSys &S, int a1, int a2, int *bad) {
+    if (S.hb_role[a1] == 'A' || S.hb_role[a1] == 'S') { int t = a1; a1 = a2; a2 = t; }
+    int t1 = type_change(S.type[a1], 0), t2 = type_change(S.type[a2], 0);
+    int aa2 = S.aatype[a2];
+    if (t1 == 2 && t2 == 26) return 1;
+    if (t1 == 2) {
+        switch (aa2) {
+            case 4: case 7: return 2;
+            case 16: case 17: case 19: return 3;
+            case 9: return 4;
+            case 5: return 10;
+            case 3: case 6: return -1;
+            default: break;
+        }
+    } else if (t2 == 26) {
+        return 5;
+    } else if (t1 == 31 && t2 == 31) {
+        return 9;
+    } else if (t1 == 1) {
+        switch (aa2) {
+            case 4: case 7: return 6;
+            case 16: case 17: case 19: return 7;
+            case 9: return 8;
+            case 3: case 6: return 11;
+            default: break;
+        }
+    }
+    *bad = 1;
+    return 0;
+}
+
+// HBBarrier (src/Events.c:1097-1119)
+__device__ inline double hb_barrier(const DSys &S, int a1, int a2) {
+    if (S.hb_role[a1] == 'A' || S.hb_role[a1] == 'S') { int t = a1; a1 = a2; a2 = t; }
+    int t1 = type_change(S.type[a1], 0), t2 = type_change(S.type[a2], 0);
+    if (t1 == 2 && t2 == 26) return S.hb_barrier[0];
+    if (t1 != 2 && t2 != 26) return S.hb_barrier[2];
+    return S.hb_barrier[1];
+}
+
+__device__ inline int conn_bits(const DSys &S, int i, int j) {
+    for (int k = S.conn_off[i], e = S.conn_off[i + 1]; k < e; k++)
+        if (S.conn_j[k] == j) return S.conn_bits[k];
+    return 0;
+}
+
+// FindElemInList(neighborPartner, j, -1, -1, 0) (src/ToolFunctions.c:1062-1087)
+__device__ inline int nb_has(const DSys &S, int i, int j) {
+    const int32_t *l = S.nb_partner + 4 * i;
+    for (int k = 0; k < 4; k++) {
+        int v = l[k];
+        if (v == 0) return 0;
+        if (v == j) return k + 1;
+    }
+    return 0;
+}
+
+struct Lim { double lo, up, lopot, uppot, acc; };
+
+// FindPair (src/ToolFunctions.c:39-224).  Returns coreorShell; *warn counts the
+// reference's warningsum increments; *bad flags a fatal table miss.
+__device__ inline int find_pair(const DSys &S, int a1, int a2, int kind, double direction, double distance2,
+                                Lim &o, int hbpartner, int tc, int wall_type2, int *warn, int *bad) {
+    int cs = -1;
+    double dir = direction < 0 ? 1 : -1;
+    double tol = dir * ZERO;
+    double dmin, dmax;
+    const double *sd, *se, *sa;
+    int sn;
+    if (kind == K_CONSTRAINT) {
+        int k = S.con_off[a1], e = S.con_off[a1 + 1];
+        for (; k < e; k++) if (S.con_j[k] == a2) break;
+        if (k == e) { *bad = 1; return -1; }
+        dmin = S.con_dmin[k]; dmax = S.con_dmax[k]; sn = S.con_step_n[k];
+        int so = S.con_step_off[k];
+        sd = S.con_step_d + so; se = S.con_step_e + so; sa = S.con_step_acc + so;
+    } else {
+        int e;
+        if (kind == K_COLLISION) {
+            int t1 = S.type[a1];
+            if (tc == 1) t1 = type_change(t1, 1);
+            else if (tc == -1) t1 = type_change(t1, 0);
+            int t2 = a2 ? S.type[a2] : wall_type2;
+            e = right_pair(S, t1, t2);
+            if (e < 0) { *bad = 1; return -1; }
+        } else if (kind == K_HB) {
+            int tn = hb_model(S, a1, a2, bad);
+            if (tn < 0) { *bad = 1; tn = 0; }   // the reference indexes table -1 here; refuse instead
+            e = tab_idx(tn, 0, 0);
+        } else {
+            int tn = hb_model(S, a2, hbpartner, bad);
+            if (tn < 0) { *bad = 1; tn = 0; }
+            e = tab_idx(tn, type_change(S.type[a1], 0), type_change(S.type[a2], 0));
+        }
+        dmin = S.pair_dmin[e]; dmax = S.pair_dmax[e]; sn = S.pair_step_n[e];
+        int so = S.pair_step_off[e];
+        sd = S.pair_step_d + so; se = S.pair_step_e + so; sa = S.pair_step_acc + so;
+    }
+    int flag = (sn == 0);
+    if (dmin == 0) { *bad = 1; return -1; }
+    int a1bond = a1 ? S.hb_bond[a1] : 0, a2bond = a2 ? S.hb_bond[a2] : 0;
+    int warnable = !(kind == K_NEIGHBOR && a2bond == 0) && !(kind == K_HB && a1bond == 0);
+    if (distance2 < dmin - ZERO) {
+        o.lo = INFINIT; o.up = INFINIT; o.acc = INFINIT; o.lopot = 0; o.uppot = 0;
+        if (warnable) ++*warn;
+        return cs;
+    }
+    o.lo = dmin; o.lopot = 0;
+    for (int q = 0; q < sn; q++) {
+        double d = sd[q];
+        if (d == 0) break;
+        if (distance2 < d + tol) {
+            o.up = d; o.uppot = -1 * se[q]; o.acc = sa[q];
+            if (q == 0) return 0;
+            if (kind == K_HB && q == sn - 1 && a1bond > 0) return 1;
+            if (kind == K_NEIGHBOR && q == sn - 1 && a2bond > 0) { o.uppot = 0; return 1; }
+            return cs;
+        }
+        o.lo = d; o.lopot = se[q];
+    }
+    if (kind == K_HB && a1bond > 0) ++*warn;
+    if (dmax > 0) {
+        if (distance2 < dmax + ZERO) {
+            o.up = dmax; o.uppot = 0; o.acc = 0;
+            cs = 1;
+            if (flag == 1 && dir == 1) cs = 0;
+            return cs;
+        }
+        o.lo = INFINIT; o.up = INFINIT; o.acc = INFINIT; o.lopot = 0; o.uppot = 0;
+        if (warnable) ++*warn;
+    } else {
+        o.up = INFINIT; o.uppot = INFINIT; o.acc = INFINIT;
+        return 1;
+    }
+    return cs;
+}
+
+struct Kin { double r2, b, v2, rx, ry, rz; };
+
+// PBCShift + CalculateParameters (src/ToolFunctions.c:801-817, src/TimePrediction.c:1081-1090)
+__device__ inline void pair_kin(const DSys &S, int i, int j, Kin &k) {
+    const int ci[3] = {S.cx[i], S.cy[i], S.cz[i]}, cj[3] = {S.cx[j], S.cy[j], S.cz[j]};
+    double sh[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        sh[d] = 0;
+        if (ci[d] != cj[d]) {
+            if (ci[d] == 0 && cj[d] == S.cn[d] - 1) sh[d] = -1 * S.box[d];
+            else if (ci[d] == S.cn[d] - 1 && cj[d] == 0) sh[d] = S.box[d];
+        }
+    }
+    double rx = S.x[i] - (S.x[j] + sh[0]);
+    double ry = S.y[i] - (S.y[j] + sh[1]);
+    double rz = S.z[i] - (S.z[j] + sh[2]);
+    double vx = S.vx[i] - S.vx[j], vy = S.vy[i] - S.vy[j], vz = S.vz[i] - S.vz[j];
+    k.rx = rx; k.ry = ry; k.rz = rz;
+    k.r2 = rx * rx + ry * ry + rz * rz;
+    k.b = rx * vx + ry * vy + rz * vz;
+    k.v2 = vx * vx + vy * vy + vz * vz;
+}
+
+// CalculateDisc / CalculateTime (src/TimePrediction.c:1092-1099)
+__device__ inline double disc(const Kin &k, double shortlim) { return k.b * k.b - k.v2 * (k.r2 - shortlim); }
+__device__ inline double root(const Kin &k, int st, double d2) {
+    return (-1 * k.b + st * sqrt(k.b * k.b - k.v2 * (k.r2 - d2))) / k.v2;
+}
+
+}  // namespace sdmd

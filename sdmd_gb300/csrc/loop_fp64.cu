@@ -1,0 +1,776 @@
+// loop_fp64.cu -- exact FP64 event loop: one CTA per system.
+//
+// Restates SingleThreadRun (src/SGThread.c:67-155) with Predict
+// (src/SGThread.c:158-211), DoEvent (src/Events.c:25-114) and the CBT
+// (src/CBT.c) on the GPU.  Per pop the CTA
+//   1. pops the tree root (AssignJob, src/SGThread.c:237-259),
+//   2. advances every atom and every event time (UpdateData/TimeForward,
+//      src/ToolFunctions.c:23-36) -- all threads,
+//   3. checks the hazard and executes the event -- thread 0,
+//   4. predicts the target (and partner): the bonded, 27-cell collision and HB
+//      candidates are gathered and evaluated by all threads, then thread 0 folds
+//      them into the running minimum in the reference's scan order, which
+//      reproduces JobAssign's strict "<" and CheckDuplication exactly,
+//   5. repairs the tree (UpdateCBTRun, src/CBT.c:56-83) -- thread 0.
+// Compiled with -fmad=false: bit-identical to the reference's FP64 results.
+#include "dev.cuh"
+#include "engine.h"
+
+namespace sdmd {
+
+// slot flags
+enum : int32_t { F_DUP = 1, F_FRESH = 2 };
+
+struct Slots {
+    int32_t *j, *info;      // info: flags | sub << 8 | warnings << 16
+    double *t, *tdup, *pot;
+};
+
+struct Blk {                 // block-uniform scalars in shared memory
+    int32_t err, err_atom;
+    int32_t nnb;
+    int32_t hbmode;          // 0 skip HB, 1 bonded, 2 scan
+    int64_t warn;
+};
+
+__device__ inline void set_err(Blk &B, int code, int atom) {
+    if (B.err == 0) { B.err = code; B.err_atom = atom; }
+}
+
+// ---------------------------------------------------------------------------
+// gather the 27-cell neighbourhood of atom i into nbj[] in scan order
+// (27 cells in src/DMD.c:117-121 order, each list head-first: src/TimePrediction.c:60-80)
+__device__ void gather(const DSys &S, int i, int32_t *nbj, int32_t *cnt, Blk &B) {
+    int tid = threadIdx.x;
+    int head = 0, c = 0;
+    if (tid < 27) {
+        head = S.cell_list[S.n + nb_cell(S, i, tid)];
+        for (int a = head; a; a = S.cell_list[a]) {
+            if (++c > S.n) break;   // a corrupted (cyclic) list cannot spin forever
+        }
+        cnt[tid] = c;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        int tot = 0;
+        for (int k = 0; k < 27; k++) { int v = cnt[k]; cnt[k] = tot; tot += v; }
+        if (tot > S.nbcap) { set_err(B, SDMD_ECAPACITY, i); tot = 0; }
+        B.nnb = tot;
+    }
+    __syncthreads();
+    if (tid < 27 && B.err == 0) {
+        int o = cnt[tid], m = 0;
+        for (int a = head; a && m < c; a = S.cell_list[a]) nbj[o + m++] = a;
+    }
+    __syncthreads();
+}
+
+// ---- candidate evaluation (all threads) -------------------------------------
+__device__ inline void put(Slots &L, int k, int j, int info, double t, double tdup, double pot) {
+    L.j[k] = j; L.info[k] = info; L.t[k] = t; L.tdup[k] = tdup; L.pot[k] = pot;
+}
+
+// BondTime, one bond (src/TimePrediction.c:217-293)
+__device__ void eval_bond(const DSys &S, int i, int q, Slots &L, int k, int *bad) {
+    int j = S.bond_j[q];
+    int info = 0;
+    double tdup = 0;
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
+        info |= F_DUP; tdup = S.ev_time[j];
+    }
+    double lng = S.bond_dmax[q], sht = S.bond_dmin[q];
+    Kin kk; pair_kin(S, i, j, kk);
+    int sub; double t;
+    if (kk.r2 - lng > ZERO && kk.b >= 0) { sub = SDMD_SUB_WELL_BOUNCE; t = 1e-16 * i * j; }
+    else if (!(kk.r2 - lng > ZERO) && sht - kk.r2 > ZERO && kk.b < 0) { sub = SDMD_SUB_CORE; t = 1e-16 * i * j; }
+    else {
+        int st; double d2;
+        if (kk.b < 0 && disc(kk, sht) > 0) { st = -1; d2 = sht; sub = SDMD_SUB_CORE; }
+        else { st = 1; d2 = lng; sub = SDMD_SUB_WELL_BOUNCE; }
+        t = root(kk, st, d2);
+        if (t < 0) t = INFINIT;
+    }
+    put(L, k, j, info | F_FRESH | (sub << 8), t, tdup, 0.0);
+}
+
+// CollisionTime, one candidate j (src/TimePrediction.c:78-179)
+__device__ void eval_collision(const DSys &S, int i, int j, double cut, Slots &L, int k, int *bad) {
+    int info = 0, warn = 0, sub = SDMD_SUB_INVALID;
+    double tdup = 0, t = 0, pot = 0;
+    if (j == i) { put(L, k, j, -1, 0, 0, 0); return; }   // -1: not a candidate at all
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
+        info |= F_DUP; tdup = S.ev_time[j];
+    }
+    int bits = conn_bits(S, i, j);
+    if (!((bits & 1) || S.hb_bond[i] == j || nb_has(S, i, j))) {
+        Kin kk; pair_kin(S, i, j, kk);
+        if (kk.r2 <= cut) {
+            Lim o; int cs; bool go = true;
+            int constrained = bits & 2;
+            if (constrained) {
+                cs = find_pair(S, i, j, K_CONSTRAINT, kk.b, kk.r2, o, 0, 0, 0, &warn, bad);
+            } else {
+                cs = find_pair(S, i, j, K_COLLISION, kk.b, kk.r2, o, 0, 0, 0, &warn, bad);
+                if (o.lopot == 0 && o.uppot == 0) go = false;
+            }
+            if (go) {
+                int st; double d2;
+                if (kk.b < 0 && disc(kk, o.lo) > 0) {
+                    st = -1; d2 = o.lo; pot = o.lopot;
+                    sub = (cs == 0) ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
+                } else {
+                    st = 1; d2 = o.up; pot = o.uppot;
+                    if (constrained) sub = (cs == 1) ? SDMD_SUB_WELL_BOUNCE : SDMD_SUB_TBD_ESCAPE;
+                    else if (cs == 1) go = false;
+                    else sub = SDMD_SUB_TBD_ESCAPE;
+                }
+                if (go) { t = root(kk, st, d2); info |= F_FRESH; }
+            }
+        }
+    }
+    put(L, k, j, info | (sub << 8) | (warn << 16), t, tdup, pot);
+}
+
+__device__ inline bool hb_pair_ok(const DSys &S, int i, int j) {
+    int ri = S.hb_role[i], rj = S.hb_role[j];
+    return (ri == 'A' && rj == 'D') || (ri == 'D' && rj == 'A') ||
+           (ri == 'S' && S.type[j] == 2) || (rj == 'S' && S.type[i] == 2) || (ri == 'S' && rj == 'S');
+}
+
+// CheckPairMatch (src/TimePrediction.c:1119-1138)
+__device__ int pair_match(const DSys &S, int i, int j, int *bad) {
+    int t = hb_model(S, i, j, bad);
+    if (t < 0) return -1;
+    int ti = S.type[i], tj = S.type[j];
+    if (S.pair_step_n[tab_idx(t, ti, tj)] == 0) return -1;
+    int ni = type_change(S.type[S.hb_neighbor[i]], 0), nj = type_change(S.type[S.hb_neighbor[j]], 0);
+    if (S.pair_step_n[tab_idx(t, ti, nj)] == 0 || S.pair_step_n[tab_idx(t, tj, ni)] == 0) return -1;
+    return 0;
+}
+
+// HBTime, unbonded scan over one candidate (src/TimePrediction.c:398-479)
+__device__ void eval_hb_scan(const DSys &S, int i, int j, double cut, Slots &L, int k, int *bad) {
+    if (!(i != j && hb_pair_ok(S, i, j) && S.hb_bond[j] == 0 &&
+          ((S.protein[i] == S.protein[j] && abs(S.aanum[i] - S.aanum[j]) >= 4) || S.protein[i] != S.protein[j]))) {
+        put(L, k, j, -1, 0, 0, 0);
+        return;
+    }
+    int info = 0, warn = 0;
+    double tdup = 0, t = 0, pot = 0;
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
+        info |= F_DUP; tdup = S.ev_time[j];
+    }
+    Kin kk; pair_kin(S, i, j, kk);
+    if (kk.r2 <= cut && pair_match(S, i, j, bad) >= 0) {
+        Lim o;
+        int cs = find_pair(S, i, j, K_HB, kk.b, kk.r2, o, 0, 0, 0, &warn, bad);
+        if (kk.b < 0 && cs == 1 && disc(kk, o.lo) > 0) {
+            pot = o.lopot;
+            t = root(kk, -1, o.lo);
+            if (t < 0) t = INFINIT;
+            info |= F_FRESH;
+        }
+    }
+    put(L, k, j, info | (SDMD_SUB_TBD_HBFORM << 8) | (warn << 16), t, tdup, pot);
+}
+
+// ---- running minimum (thread 0): JobAssign + CheckDuplication ---------------
+// (src/TimePrediction.c:1140-1158, 1101-1117)
+__device__ inline bool job_assign(const DSys &S, int i, int j, double t, double pot, int sub, int type) {
+    if (t > 0 && S.ev_time[i] > t) {
+        S.ev_potential[i] = pot; S.ev_sub[i] = sub; S.ev_time[i] = t; S.ev_type[i] = type;
+        if (j) { S.ev_partner[i] = j; S.ev_pcounter[i] = S.ev_counter[j]; }
+        else S.ev_partner[i] = INVALID;
+        return true;
+    }
+    return false;
+}
+__device__ inline bool dup_assign(const DSys &S, int i, int j, double tdup, int type) {
+    if (S.ev_time[i] > tdup) {
+        S.ev_partner[i] = j; S.ev_potential[i] = S.ev_potential[j]; S.ev_sub[i] = S.ev_sub[j];
+        S.ev_time[i] = tdup; S.ev_type[i] = type; S.ev_pcounter[i] = S.ev_counter[j];
+        return true;
+    }
+    return false;
+}
+__device__ void resolve(const DSys &S, int i, const Slots &L, int n, int type, Blk &B) {
+    for (int k = 0; k < n; k++) {
+        int info = L.info[k];
+        if (info < 0) continue;
+        int j = L.j[k];
+        if ((info & F_DUP) && dup_assign(S, i, j, L.tdup[k], type)) continue;
+        B.warn += (info >> 16) & 0xff;
+        if (info & F_FRESH) job_assign(S, i, j, L.t[k], L.pot[k], (info >> 8) & 0xff, type);
+    }
+}
+
+// ---- scalar predictions (thread 0) -----------------------------------------
+// PBCandCrossCellTime (src/TimePrediction.c:598-632)
+__device__ void pcc_time(const DSys &S, int i) {
+    double best = INFINIT;
+    const double pos[3] = {S.x[i], S.y[i], S.z[i]}, v[3] = {S.vx[i], S.vy[i], S.vz[i]};
+    const int ci[3] = {S.cx[i], S.cy[i], S.cz[i]};
+    for (int d = 0; d < 3; d++) {
+        double lo = ci[d] * S.cs[d], hi = (ci[d] + 1) * S.cs[d], t;
+        if (v[d] > 0) { t = (hi - pos[d] + ZERO) / v[d]; if (best > t && t > 0) best = t; }
+        else if (v[d] < 0) { t = (lo - pos[d] - ZERO) / v[d]; if (best > t && t > 0) best = t; }
+    }
+    job_assign(S, i, 0, best, 0, SDMD_SUB_INVALID, SDMD_EV_PCC);
+}
+
+// ThermostatTime (src/TimePrediction.c:582-595)
+__device__ void thermostat_time(const DSys &S, int i, sdmd_rng &rng, Blk &B) {
+    if (!S.thermostat) return;
+    int bad = 0;
+    double t = mb_draw(rng, 0, 1, &bad);
+    if (bad) { set_err(B, SDMD_ETIMEOUT, i); return; }
+    job_assign(S, i, 0, S.thermo_freq * (t < 0 ? -t : t), 0, SDMD_SUB_INVALID, SDMD_EV_THERMOSTAT);
+}
+
+// HBTime for an HB-bonded atom (src/TimePrediction.c:329-387)
+__device__ void hb_bonded(const DSys &S, int i, Blk &B, int *bad) {
+    int j = S.hb_bond[i];
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
+        dup_assign(S, i, j, S.ev_time[j], SDMD_EV_HB))
+        return;
+    Kin kk; pair_kin(S, i, j, kk);
+    Lim o; int warn = 0;
+    int cs = find_pair(S, i, j, K_HB, kk.b, kk.r2, o, 0, 0, 0, &warn, bad);
+    B.warn += warn;
+    int st, sub; double d2, pot;
+    if (kk.b < 0 && disc(kk, o.lo) > 0) {
+        st = -1; d2 = o.lo; pot = o.lopot; sub = (cs == 0) ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
+    } else {
+        st = 1; d2 = o.up; pot = o.uppot; sub = (cs == 1) ? SDMD_SUB_TBD_HBBREAK : SDMD_SUB_TBD_ESCAPE;
+    }
+    double t = root(kk, st, d2);
+    if (t < 0) t = INFINIT;
+    job_assign(S, i, j, t, pot, sub, SDMD_EV_HB);
+}
+
+// HBNeighborTime (src/TimePrediction.c:486-579)
+__device__ void hbnb_time(const DSys &S, int i, Blk &B, int *bad) {
+    int flag = 0;
+    for (int n = 1; n <= S.nb_status[i]; n++) {
+        int j = S.nb_partner[4 * i + n - 1];
+        if (flag == 0) S.nb_pnum[i] = n;
+        if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HBNEIGHBOR && S.ev_pcounter[j] == S.ev_counter[i] &&
+            dup_assign(S, i, j, S.ev_time[j], SDMD_EV_HBNEIGHBOR)) {
+            S.nb_pnum[i] = n; flag = 1; continue;
+        }
+        Kin kk; pair_kin(S, i, j, kk);
+        int host, nbr, hpart, ri = S.hb_role[i];
+        if ((ri == 'A' || ri == 'D' || ri == 'S') && S.hb_bond[i] && S.hb_neighbor[S.hb_bond[i]] == j) {
+            host = i; nbr = j; hpart = S.hb_bond[i];
+        } else {
+            host = j; nbr = i; hpart = S.hb_bond[j];
+        }
+        Lim o; int warn = 0;
+        int cs = find_pair(S, nbr, host, K_NEIGHBOR, kk.b, kk.r2, o, hpart, 0, 0, &warn, bad);
+        B.warn += warn;
+        int st, sub; double d2, pot;
+        if (kk.b < 0 && disc(kk, o.lo) > 0) {
+            st = -1; d2 = o.lo; pot = o.lopot; sub = (cs == 0) ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
+        } else {
+            st = 1; d2 = o.up; pot = o.uppot; sub = (cs == 1) ? SDMD_SUB_WELL_BOUNCE : SDMD_SUB_TBD_ESCAPE;
+        }
+        double t = root(kk, st, d2);
+        if (t < 0) t = INFINIT;
+        if (job_assign(S, i, j, t, pot, sub, SDMD_EV_HBNEIGHBOR)) { S.nb_pnum[i] = n; flag = 1; }
+    }
+}
+
+// WallTime, smooth walls (src/TimePrediction.c:635-737)
+__device__ void wall_time(const DSys &S, int i, Blk &B, int *bad) {
+    double p[3] = {S.x[i], S.y[i], S.z[i]}, v[3] = {S.vx[i], S.vy[i], S.vz[i]};
+    if (S.wall == SDMD_WALL_PARALLEL) { p[0] = p[2] = 0; v[0] = v[2] = 0; }
+    else if (S.wall == SDMD_WALL_CYLINDER) { p[0] = 0; v[0] = 0; }
+    Kin k;
+    k.rx = p[0] - S.wall_pos[0]; k.ry = p[1] - S.wall_pos[1]; k.rz = p[2] - S.wall_pos[2];
+    double vx = v[0] - S.wall_vel[0], vy = v[1] - S.wall_vel[1], vz = v[2] - S.wall_vel[2];
+    k.r2 = k.rx * k.rx + k.ry * k.ry + k.rz * k.rz;
+    k.b = k.rx * vx + k.ry * vy + k.rz * vz;
+    k.v2 = vx * vx + vy * vy + vz * vz;
+    double L2 = S.box[1];
+    double dist2 = L2 * L2 * 0.25 + k.r2 - L2 * sqrt(k.r2);
+    Lim o; int warn = 0;
+    int cs = find_pair(S, i, 0, K_COLLISION, -1 * k.b, dist2, o, 0, 0, S.wall_type, &warn, bad);
+    B.warn += warn;
+    if (o.lopot == 0 && o.uppot == 0) { set_err(B, SDMD_EWALL, i); return; }
+    int st, sub; double d2, pot;
+    if (k.b < 0 && disc(k, o.lo) > 0) {
+        if (cs == 1) return;
+        sub = SDMD_SUB_TBD_CAPTURE; st = -1;
+        d2 = L2 * L2 * 0.25 + o.up - L2 * sqrt(o.up); pot = o.uppot;
+    } else {
+        sub = (cs == 0) ? SDMD_SUB_WELL_BOUNCE : SDMD_SUB_TBD_ESCAPE; st = 1;
+        d2 = L2 * L2 * 0.25 + o.lo - L2 * sqrt(o.lo); pot = o.lopot;
+    }
+    double t = root(k, st, d2);
+    if (t < 0) t = INFINIT;
+    job_assign(S, i, 0, t, pot, sub, SDMD_EV_WALL);
+}
+
+// ---- Predict for one atom (ResetTarget already applied) ---------------------
+struct Shm {
+    int32_t *nbj, *cnt;
+    Slots L;
+};
+
+__device__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, sdmd_rng &rng) {
+    const int tid = threadIdx.x, T = blockDim.x;
+    int bad = 0;
+    double cut = S.cutoff * 0.90; cut *= cut;
+    // BondTime
+    int b0 = S.bond_off[i], nb = S.bond_off[i + 1] - b0;
+    if (nb > (S.nbcap > 64 ? S.nbcap : 64)) {   // slot capacity
+        if (tid == 0) set_err(B, SDMD_ECAPACITY, i);
+        __syncthreads();
+        return;
+    }
+    for (int k = tid; k < nb; k += T) eval_bond(S, i, b0 + k, M.L, k, &bad);
+    __syncthreads();
+    if (tid == 0) resolve(S, i, M.L, nb, SDMD_EV_BOND, B);
+    // CollisionTime over the gathered 27-cell neighbourhood
+    gather(S, i, M.nbj, M.cnt, B);
+    int nn = B.nnb;
+    for (int k = tid; k < nn; k += T) eval_collision(S, i, M.nbj[k], cut, M.L, k, &bad);
+    __syncthreads();
+    if (tid == 0) {
+        resolve(S, i, M.L, nn, SDMD_EV_COLLISION, B);
+        pcc_time(S, i);
+        thermostat_time(S, i, rng, B);
+        // HBTime prologue: one-shot HBSkip suppression (src/TimePrediction.c:309-327)
+        int mode;
+        if (S.hb_itype[i] == SDMD_HB_SKIP) mode = 0;
+        else if (S.hb_bond[i] > 0) mode = 1;
+        else {
+            int r = S.hb_role[i];
+            mode = (r == 'A' || r == 'D' || r == 'S') ? 2 : 0;
+        }
+        S.hb_itype[i] = SDMD_HB_NOEVENT;
+        B.hbmode = mode;
+        if (mode == 1) hb_bonded(S, i, B, &bad);
+    }
+    __syncthreads();
+    if (B.hbmode == 2) {
+        for (int k = tid; k < nn; k += T) eval_hb_scan(S, i, M.nbj[k], cut, M.L, k, &bad);
+        __syncthreads();
+        if (tid == 0) resolve(S, i, M.L, nn, SDMD_EV_HB, B);
+    }
+    if (tid == 0) {
+        hbnb_time(S, i, B, &bad);
+        if (S.wall) wall_time(S, i, B, &bad);
+    }
+    if (bad) set_err(B, SDMD_EHBMAP, i);
+    __syncthreads();
+}
+
+// ---- events (thread 0) -------------------------------------------------------
+__device__ void imaged(const DSys &S, int t, int a, double p[3]) {
+    const int ct[3] = {S.cx[t], S.cy[t], S.cz[t]}, ca[3] = {S.cx[a], S.cy[a], S.cz[a]};
+    p[0] = S.x[a]; p[1] = S.y[a]; p[2] = S.z[a];
+    for (int d = 0; d < 3; d++) {
+        if (ct[d] != ca[d]) {
+            if (ct[d] == 0 && ca[d] == S.cn[d] - 1) p[d] -= S.box[d];
+            else if (ct[d] == S.cn[d] - 1 && ca[d] == 0) p[d] += S.box[d];
+        }
+    }
+}
+
+// HBEnergyChange (src/Events.c:1027-1095); `acc` carries over between candidates
+// exactly as the reference's local does.
+__device__ double hb_energy_change(const DSys &S, int t, int skip, int to_hb, Blk &B, int *bad) {
+    double cut = S.cutoff * S.cutoff, energy = 0, acc = 0;
+    for (int kc = 0; kc < 27; kc++) {
+        int guard = 0;
+        for (int j = S.cell_list[S.n + nb_cell(S, t, kc)]; j && guard <= S.n; j = S.cell_list[j], guard++) {
+            int bits = conn_bits(S, t, j);
+            if (!(t != j && !(bits & 1) && !(bits & 2) && j != skip)) continue;
+            Kin k; pair_kin(S, t, j, k);
+            if (k.r2 <= cut) {
+                Lim o; int warn = 0;
+                if (!to_hb) { find_pair(S, t, j, K_COLLISION, 0, k.r2, o, 0, -1, 0, &warn, bad); acc = o.acc; }
+                else if (j != S.hb_neighbor[skip]) { find_pair(S, t, j, K_COLLISION, 0, k.r2, o, 0, 1, 0, &warn, bad); acc = o.acc; }
+                B.warn += warn;
+                if (acc == INFINIT) acc = 0;
+                energy += acc;
+            }
+        }
+    }
+    return energy;
+}
+
+// InteractionEvent (src/Events.c:798-1024)
+__device__ void interaction_event(const DSys &S, int t, int p, int ni, int nj, Blk &B, int *bad) {
+    double pi[3] = {S.x[t], S.y[t], S.z[t]}, pj[3];
+    imaged(S, t, p, pj);
+    double r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+    double v[3] = {S.vx[t] - S.vx[p], S.vy[t] - S.vy[p], S.vz[t] - S.vz[p]};
+    double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    double b = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+    double mt = S.mass[t], mp = S.mass[p];
+    double mu = mt * mp / (mt + mp);
+    double pot = S.ev_potential[t];
+    int sv = 0;
+    if (S.ev_type[t] == SDMD_EV_HB && (S.ev_sub[t] == SDMD_SUB_TBD_HBFORM || S.ev_sub[t] == SDMD_SUB_TBD_HBBREAK)) {
+        bool form = S.ev_sub[t] == SDMD_SUB_TBD_HBFORM;
+        if ((nb_has(S, t, nj) || nb_has(S, p, ni)) && form) { S.hb_itype[t] = SDMD_HB_SKIP; return; }
+        double pni[3], pnj[3];
+        imaged(S, t, ni, pni);
+        imaged(S, t, nj, pnj);
+        double rci[3] = {pi[0] - pnj[0], pi[1] - pnj[1], pi[2] - pnj[2]};
+        double rcj[3] = {pj[0] - pni[0], pj[1] - pni[1], pj[2] - pni[2]};
+        double rni2 = rci[0] * rci[0] + rci[1] * rci[1] + rci[2] * rci[2];
+        double rnj2 = rcj[0] * rcj[0] + rcj[1] * rcj[1] + rcj[2] * rcj[2];
+        double acc[6];
+        acc[0] = hb_energy_change(S, t, p, 0, B, bad);
+        acc[1] = hb_energy_change(S, p, t, 0, B, bad);
+        acc[2] = hb_energy_change(S, t, p, 1, B, bad);
+        acc[3] = hb_energy_change(S, p, t, 1, B, bad);
+        Lim o; int warn = 0;
+        find_pair(S, nj, t, K_NEIGHBOR, 0, rni2, o, p, 0, 0, &warn, bad); acc[4] = o.acc;
+        find_pair(S, ni, p, K_NEIGHBOR, 0, rnj2, o, t, 0, 0, &warn, bad); acc[5] = o.acc;
+        B.warn += warn;
+        if (form) {
+            pot -= hb_barrier(S, t, p);
+            pot += (acc[2] - acc[0] + acc[3] - acc[1] + acc[4] + acc[5]);
+        } else {
+            pot += hb_barrier(S, t, p);
+            pot += (acc[0] - acc[2] + acc[1] - acc[3] - acc[4] - acc[5]);
+        }
+        if (pot < -0.5 * INFINIT && !form) { S.hb_itype[t] = SDMD_HB_SKIP; return; }
+        if (pot > 0.5 * INFINIT && form) { S.hb_itype[t] = SDMD_HB_SKIP; return; }
+        if (b * b - 2 * d2 * pot / mu > 0) {
+            if (form) { S.ev_sub[t] = SDMD_SUB_WELL_CAPTURE; S.hb_itype[t] = SDMD_HB_FORM; }
+            else { S.ev_sub[t] = SDMD_SUB_WELL_ESCAPE; S.hb_itype[t] = SDMD_HB_BREAK; }
+        } else {
+            if (form) { S.hb_itype[t] = SDMD_HB_SKIP; return; }
+            pot = 0; S.ev_sub[t] = SDMD_SUB_WELL_BOUNCE; S.hb_itype[t] = SDMD_HB_NOEVENT;
+        }
+    }
+    switch (S.ev_sub[t]) {
+        case SDMD_SUB_CORE: sv = 1; pot = 0; break;
+        case SDMD_SUB_WELL_BOUNCE: sv = b < 0 ? 1 : -1; pot = 0; break;
+        case SDMD_SUB_WELL_CAPTURE: sv = -1; break;
+        case SDMD_SUB_WELL_ESCAPE: sv = b < 0 ? -1 : 1; break;
+        case SDMD_SUB_TBD_CAPTURE:
+            if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = 1; } else sv = -1;
+            break;
+        case SDMD_SUB_TBD_ESCAPE:
+            if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = b < 0 ? 1 : -1; }
+            else sv = b < 0 ? -1 : 1;
+            break;
+        default: set_err(B, SDMD_EEVENTTYPE, t); return;
+    }
+    double phi = (-1 * b + sv * sqrt((b * b - 2 * d2 * pot / mu))) / ((mt + mp) * d2);
+    if (isnan(phi)) { set_err(B, SDMD_ENAN, t); return; }
+    double ft = mp * phi, fp = mt * phi;
+    S.vx[t] = S.vx[t] + ft * r[0]; S.vy[t] = S.vy[t] + ft * r[1]; S.vz[t] = S.vz[t] + ft * r[2];
+    S.vx[p] = S.vx[p] - fp * r[0]; S.vy[p] = S.vy[p] - fp * r[1]; S.vz[p] = S.vz[p] - fp * r[2];
+}
+
+// ListRefresh (src/ToolFunctions.c:572-597) and neighbour-list append
+__device__ void nb_remove(const DSys &S, int a, int value) {
+    int32_t *l = S.nb_partner + 4 * a;
+    int i = nb_has(S, a, value);
+    if (!i) return;
+    int n = i + 1;
+    while (n <= 4 && l[n - 1] != 0) { l[i - 1] = l[n - 1]; i++; n++; }
+    l[i - 1] = 0;
+}
+__device__ void nb_append(const DSys &S, int a, int value, Blk &B) {
+    int k = ++S.nb_status[a];
+    if (k > 4) { set_err(B, SDMD_ECAPACITY, a); return; }
+    S.nb_partner[4 * a + k - 1] = value;
+}
+__device__ inline bool alpha_hb(const DSys &S, int i, int j) {
+    return S.protein[i] == S.protein[j] &&
+           ((S.name_code[i] == 1 && S.name_code[j] == 2 && S.aanum[j] == S.aanum[i] - 4) ||
+            (S.name_code[i] == 2 && S.name_code[j] == 1 && S.aanum[i] == S.aanum[j] - 4));
+}
+
+// HBEvent (src/Events.c:275-393)
+__device__ void hb_event(const DSys &S, DScal &C, int i, int j, int ni, int nj, Blk &B) {
+    int nbi = S.hb_neighbor[i], nbj = S.hb_neighbor[j];
+    if (S.hb_itype[i] == SDMD_HB_FORM) {
+        if (nb_has(S, i, nbj) || nb_has(S, nbj, i) || nb_has(S, j, nbi) || nb_has(S, nbi, j)) {
+            set_err(B, SDMD_EHBMAP, i); return;
+        }
+        S.hb_bond[i] = j; S.hb_bond[j] = i;
+        S.type[i] = type_change(S.type[i], 1); S.type[j] = type_change(S.type[j], 1);
+        nb_append(S, i, nbj, B); nb_append(S, j, nbi, B); nb_append(S, ni, j, B); nb_append(S, nj, i, B);
+        if (alpha_hb(S, i, j)) C.c.alpha_hb_formed++;
+        C.c.hb_formed++;
+    } else if (S.hb_itype[i] == SDMD_HB_BREAK) {
+        S.hb_bond[i] = 0; S.hb_bond[j] = 0;
+        S.type[i] = type_change(S.type[i], 0); S.type[j] = type_change(S.type[j], 0);
+        --S.nb_status[i]; nb_remove(S, i, nbj);
+        --S.nb_status[j]; nb_remove(S, j, nbi);
+        --S.nb_status[ni]; nb_remove(S, ni, j);
+        --S.nb_status[nj]; nb_remove(S, nj, i);
+        if (alpha_hb(S, i, j)) C.c.alpha_hb_formed--;
+        C.c.hb_formed--;
+        if (C.c.hb_formed < C.c.alpha_hb_formed) C.c.warnings++;
+    }
+}
+
+// ThermostatEvent, Andersen (src/Events.c:396-420)
+__device__ void thermostat_event(const DSys &S, int t, sdmd_rng &rng, Blk &B) {
+    double sp[3];
+    for (int d = 0; d < 3; d++) {
+        int bad = 0, tries = 0;
+        do { sp[d] = mb_draw(rng, 0, S.temperature / S.mass[t], &bad); } while (sp[d] == 0 && !bad && ++tries < 64);
+        if (bad || sp[d] == 0) { set_err(B, SDMD_ETIMEOUT, t); return; }
+    }
+    S.vx[t] = sp[0]; S.vy[t] = sp[1]; S.vz[t] = sp[2];
+}
+
+// PBCandCrossCellEvent with PBC("part") and LinkList("part")
+// (src/Events.c:248-272, 207-245, 158-200)
+__device__ void pcc_event(const DSys &S, int t, Blk &B) {
+    int old[3] = {S.cx[t], S.cy[t], S.cz[t]};
+    double pos[3] = {S.x[t], S.y[t], S.z[t]};
+    for (int d = 0; d < 3; d++) {
+        if (old[d] == 0 || old[d] == S.cn[d] - 1) {
+            if (S.wall != SDMD_WALL_SPHERE) {
+                int dims = 3, step = 1;
+                if (S.wall == SDMD_WALL_PARALLEL) step = 2;
+                else if (S.wall == SDMD_WALL_CYLINDER) dims = 1;
+                for (int n = 0; n < dims; n += step) {
+                    if (pos[n] >= S.box[n]) pos[n] -= S.box[n];
+                    else if (pos[n] < 0) pos[n] += S.box[n];
+                }
+            }
+            break;
+        }
+    }
+    S.x[t] = pos[0]; S.y[t] = pos[1]; S.z[t] = pos[2];
+    int N = S.n, oldc = cell_lin(S, old[0], old[1], old[2]);
+    int nc[3];
+    for (int d = 0; d < 3; d++) {
+        nc[d] = (int)(pos[d] / S.cs[d]);
+        if (nc[d] == S.cn[d]) nc[d]--;
+    }
+    S.cx[t] = nc[0]; S.cy[t] = nc[1]; S.cz[t] = nc[2];
+    if (nc[0] < 0 || nc[1] < 0 || nc[2] < 0 || nc[0] >= S.cn[0] || nc[1] >= S.cn[1] || nc[2] >= S.cn[2]) {
+        set_err(B, SDMD_ELINK, t); return;
+    }
+    int newc = cell_lin(S, nc[0], nc[1], nc[2]);
+    int32_t *L = S.cell_list;
+    int at = oldc + N, guard = 0;
+    if (L[at] == 0) { set_err(B, SDMD_ELINK, t); return; }
+    while (L[at] != t) {
+        at = L[at];
+        if (at == 0 || ++guard > N) { set_err(B, SDMD_ELINK, t); return; }
+    }
+    L[at] = L[t];
+    L[t] = L[newc + N];
+    L[newc + N] = t;
+}
+
+// WallEvent, smooth walls (src/Events.c:423-499)
+__device__ void wall_event(const DSys &S, int t, Blk &B) {
+    double p[3] = {S.x[t], S.y[t], S.z[t]}, v[3] = {S.vx[t], S.vy[t], S.vz[t]};
+    if (S.wall == SDMD_WALL_PARALLEL) { p[0] = p[2] = 0; v[0] = v[2] = 0; }
+    else if (S.wall == SDMD_WALL_CYLINDER) { p[0] = 0; v[0] = 0; }
+    double r[3] = {p[0] - S.wall_pos[0], p[1] - S.wall_pos[1], p[2] - S.wall_pos[2]};
+    double w[3] = {v[0] - S.wall_vel[0], v[1] - S.wall_vel[1], v[2] - S.wall_vel[2]};
+    double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    double b = r[0] * w[0] + r[1] * w[1] + r[2] * w[2];
+    double mu = S.mass[t], pot = S.ev_potential[t];
+    int sv;
+    switch (S.ev_sub[t]) {
+        case SDMD_SUB_WELL_BOUNCE: sv = -1; pot = 0; break;
+        case SDMD_SUB_TBD_CAPTURE: if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = 1; } else sv = -1; break;
+        case SDMD_SUB_TBD_ESCAPE: if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = -1; } else sv = 1; break;
+        default: set_err(B, SDMD_EEVENTTYPE, t); return;
+    }
+    double phi = (-1 * b + sv * sqrt(b * b - 2 * d2 * pot / S.mass[t])) / d2;
+    if (isnan(phi)) { set_err(B, SDMD_ENAN, t); return; }
+    S.vx[t] = S.vx[t] + phi * r[0]; S.vy[t] = S.vy[t] + phi * r[1]; S.vz[t] = S.vz[t] + phi * r[2];
+}
+
+// DoEvent (src/Events.c:25-114)
+__device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, sdmd_rng &rng) {
+    int bad = 0;
+    switch (S.ev_type[t]) {
+        case SDMD_EV_COLLISION: interaction_event(S, t, p, 0, 0, B, &bad); C.c.collision++; break;
+        case SDMD_EV_BOND: interaction_event(S, t, p, 0, 0, B, &bad); C.c.bond++; break;
+        case SDMD_EV_HBNEIGHBOR: interaction_event(S, t, p, 0, 0, B, &bad); C.c.hbneighbor++; break;
+        case SDMD_EV_HB: {
+            int ni = S.hb_neighbor[t], nj = S.hb_neighbor[p];
+            interaction_event(S, t, p, ni, nj, B, &bad);
+            if (!B.err) hb_event(S, C, t, p, ni, nj, B);
+            C.c.hb++;
+        } break;
+        case SDMD_EV_THERMOSTAT: thermostat_event(S, t, rng, B); C.c.thermostat++; break;
+        case SDMD_EV_PCC: pcc_event(S, t, B); C.c.pcc++; break;
+        case SDMD_EV_WALL: wall_event(S, t, B); C.c.wall++; break;
+        default: set_err(B, SDMD_EEVENTTYPE, t); break;
+    }
+    if (bad) set_err(B, SDMD_EHBMAP, t);
+}
+
+// ---- CBT (src/CBT.c) -----------------------------------------------------------
+__device__ void cbt_update(const DSys &S, int a) {   // UpdateCBTRun, src/CBT.c:56-83
+    int32_t *node = S.cbt_node;
+    const int32_t *leaf = S.cbt_leaf;
+    const double *tm = S.ev_time;
+    int f;
+    for (f = leaf[a] / 2; f > 0; f /= 2) {
+        if (node[f] != a) break;
+        int l = node[2 * f], r = node[2 * f + 1];
+        node[f] = tm[l] < tm[r] ? l : r;
+    }
+    for (; f > 0; f /= 2) {
+        int old = node[f], l = node[2 * f], r = node[2 * f + 1];
+        node[f] = tm[l] < tm[r] ? l : r;
+        if (node[f] == old) return;
+    }
+}
+__device__ void cbt_build(const DSys &S) {            // CreateCBT, src/CBT.c:16-30
+    int32_t *node = S.cbt_node, *leaf = S.cbt_leaf;
+    int count = 0;
+    for (int a = 1; a <= S.n; a++) {
+        if (count == 0) { node[1] = a; count = 1; continue; }
+        int i = node[count];
+        node[2 * count] = i; node[2 * count + 1] = a;
+        leaf[i] = 2 * count; leaf[a] = 2 * count + 1;
+        count++;
+        cbt_update(S, i);
+    }
+}
+
+// ---- kernels ---------------------------------------------------------------------
+__device__ inline void carve(Shm &M, int nbcap) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    int cap = nbcap > 64 ? nbcap : 64;
+    double *d = reinterpret_cast<double *>(smem);
+    M.L.t = d; M.L.tdup = d + cap; M.L.pot = d + 2 * cap;
+    int32_t *ip = reinterpret_cast<int32_t *>(d + 3 * cap);
+    M.L.j = ip; M.L.info = ip + cap; M.nbj = ip + 2 * cap; M.cnt = ip + 2 * cap + nbcap;
+}
+
+size_t fp64_smem_bytes(int nbcap) {
+    int cap = nbcap > 64 ? nbcap : 64;
+    return (size_t)cap * 3 * sizeof(double) + (size_t)(2 * cap + nbcap + 32) * sizeof(int32_t);
+}
+
+// Full-rebuild sweep: ResetTarget + Predict over 1..N (src/SGThread.c:47-52), then
+// CreateCBT.  With full == 0 only the tree is built (continue mode).
+__global__ void sweep_kernel_fp64(const DSys *systems, int full) {
+    __shared__ DSys S;
+    if (threadIdx.x == 0) S = systems[blockIdx.x];
+    __shared__ Blk B;
+    __shared__ sdmd_rng rng;
+    if (threadIdx.x == 0) { B.err = 0; B.warn = 0; rng = S.sc->rng; }
+    __syncthreads();
+    Shm M; carve(M, S.nbcap);
+    if (full) {
+        for (int i = 1 + threadIdx.x; i <= S.n; i += blockDim.x) {
+            S.ev_type[i] = SDMD_EV_INVALID; S.ev_time[i] = INFINIT; S.ev_partner[i] = INVALID;
+        }
+        __syncthreads();
+        for (int i = 1; i <= S.n && B.err == 0; i++) predict_atom(S, i, M, B, rng);
+    }
+    if (threadIdx.x == 0) {
+        if (B.err == 0) cbt_build(S);
+        S.sc->rng = rng;
+        S.sc->c.warnings += B.warn;
+        S.sc->cbt_built = 1;
+        if (B.err) { S.sc->err = B.err; S.sc->err_atom = B.err_atom; S.sc->err_event = S.sc->c.frame; }
+    }
+}
+
+// The event loop (src/SGThread.c:75-151)
+__global__ void loop_kernel_fp64(const DSys *systems, int64_t max_events, double t_end_override) {
+    __shared__ DSys S;
+    if (threadIdx.x == 0) S = systems[blockIdx.x];
+    const int tid = threadIdx.x, T = blockDim.x;
+    __shared__ Blk B;
+    __shared__ DScal C;
+    __shared__ int32_t sh_t, sh_p, sh_exec, sh_go;
+    __shared__ double sh_dt;
+    __shared__ int32_t rec_partner, rec_type, rec_sub;
+    if (tid == 0) {
+        B.err = 0; B.warn = 0; C = *S.sc;
+        if (!C.cbt_built && !C.err) { C.err = SDMD_EINVAL; C.err_atom = 0; *S.sc = C; }   // prepare() first
+    }
+    __syncthreads();
+    if (C.err) return;
+    Shm M; carve(M, S.nbcap);
+    const double t_end = t_end_override > 0 ? t_end_override : S.t_end;
+    const int64_t stop_at = C.c.frame + max_events;
+    // denied pops do not advance `frame`; bound the pops so that no input can spin forever
+    const int64_t pop_limit = C.pops + 64 * max_events + 1000000;
+    for (;;) {
+        if (tid == 0) {
+            if (C.pops >= pop_limit) set_err(B, SDMD_ETIMEOUT, 0);
+            int go = (C.time <= t_end) && (C.c.frame < stop_at) && B.err == 0;
+            sh_go = go;
+            if (go) {
+                int t = S.cbt_node[1];
+                sh_t = t; sh_dt = S.ev_time[t];
+                rec_partner = S.ev_partner[t]; rec_type = S.ev_type[t]; rec_sub = S.ev_sub[t];
+                sh_p = rec_partner > 0 ? rec_partner : 0;
+            }
+        }
+        __syncthreads();
+        if (!sh_go) break;
+        const double dt = sh_dt;
+        for (int i = 1 + tid; i <= S.n; i += T) {      // UpdateData + TimeForward
+            S.x[i] += S.vx[i] * dt;
+            S.y[i] += S.vy[i] * dt;
+            S.z[i] += S.vz[i] * dt;
+            S.ev_time[i] -= dt;
+        }
+        __syncthreads();
+        const int t = sh_t, p = sh_p;
+        if (tid == 0) {
+            C.time += dt;
+            int hazard = p > 0 && S.ev_pcounter[t] < S.ev_counter[p];   // HazardCheck
+            sh_exec = !hazard;
+            if (!hazard) {
+                C.c.frame++;
+                do_event(S, C, t, p, B, C.rng);
+                S.ev_counter[t]++;
+                if (p) S.ev_counter[p]++;
+            } else {
+                C.c.recal++;
+            }
+            // ResetTarget for the renew list
+            S.ev_type[t] = SDMD_EV_INVALID; S.ev_time[t] = INFINIT; S.ev_partner[t] = INVALID;
+            if (!hazard && p) { S.ev_type[p] = SDMD_EV_INVALID; S.ev_time[p] = INFINIT; S.ev_partner[p] = INVALID; }
+        }
+        __syncthreads();
+        if (B.err) break;
+        predict_atom(S, t, M, B, C.rng);
+        if (sh_exec && p && B.err == 0) predict_atom(S, p, M, B, C.rng);
+        if (tid == 0) {
+            cbt_update(S, t);
+            if (sh_exec && p) cbt_update(S, p);
+            if (S.trace_cap > 0) {
+                sdmd_trace_rec &r = S.trace[C.pops % S.trace_cap];
+                r.target = t; r.partner = rec_partner; r.type = rec_type; r.sub = rec_sub;
+                r.executed = sh_exec; r.hb_itype_after = S.hb_itype[t];
+                r.t_new_partner = S.ev_partner[t]; r.t_new_type = S.ev_type[t];
+                r.p_new_partner = p ? S.ev_partner[p] : 0; r.p_new_type = p ? S.ev_type[p] : 0;
+                r.system = blockIdx.x; r.pad = 0;
+                r.dt = dt; r.time_now = C.time;
+                r.vt[0] = S.vx[t]; r.vt[1] = S.vy[t]; r.vt[2] = S.vz[t];
+                r.vp[0] = p ? S.vx[p] : 0; r.vp[1] = p ? S.vy[p] : 0; r.vp[2] = p ? S.vz[p] : 0;
+                r.t_new_time = S.ev_time[t]; r.p_new_time = p ? S.ev_time[p] : 0;
+            }
+            C.pops++;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        C.c.warnings += B.warn;
+        if (B.err) { C.err = B.err; C.err_atom = B.err_atom; C.err_event = C.c.frame; }
+        *S.sc = C;
+    }
+}
+
+}  // namespace sdmd

@@ -1,0 +1,142 @@
+"""Python front end of the GB300 event-loop engine (ctypes over libsdmd_gpu.so).
+
+The C ABI (include/sdmd_gpu.h) is the product boundary; this module is the
+thin host-side mirror used by the tests and the benchmark.  There is no CPU
+fallback: if the CUDA library is missing or no device is present, every call
+raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .system import TRACE_DTYPE, sdmd_error_info, sdmd_opts, sdmd_rng, sdmd_system, sdmd_trace_rec
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GPU_LIB = os.path.join(HERE, "libsdmd_gpu.so")
+
+ADVANCE_EAGER, ADVANCE_LAZY = 0, 1
+SCREEN_FP64, SCREEN_FP32 = 0, 1
+
+ABI_FUNCS = ["sdmd_gpu_abi_version", "sdmd_gpu_device_count", "sdmd_gpu_strerror", "sdmd_gpu_create",
+             "sdmd_gpu_destroy", "sdmd_gpu_prepare", "sdmd_gpu_run", "sdmd_gpu_download", "sdmd_gpu_trace",
+             "sdmd_gpu_last_ms", "sdmd_gpu_last_error", "sdmd_rng_seed", "sdmd_rng_next", "sdmd_rng_skip"]
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, where, info=None):
+        self.code = code
+        msg = f"{where}: {strerror(code)} ({code})"
+        if info is not None and info.code:
+            msg += f" [system {info.system}, atom {info.atom}, event {info.event}]"
+        super().__init__(msg)
+
+
+def lib():
+    """Load libsdmd_gpu.so (built by __graft_entry__.build()).  Raises if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(GPU_LIB):
+            raise RuntimeError(f"{GPU_LIB} is missing: run __graft_entry__.build() (no CPU fallback exists)")
+        L = C.CDLL(GPU_LIB)
+        P = C.POINTER
+        L.sdmd_gpu_abi_version.restype = C.c_int
+        L.sdmd_gpu_device_count.argtypes = [P(C.c_int32)]
+        L.sdmd_gpu_strerror.argtypes = [C.c_int]
+        L.sdmd_gpu_strerror.restype = C.c_char_p
+        L.sdmd_gpu_create.argtypes = [P(sdmd_system), C.c_int32, P(sdmd_opts), P(C.c_void_p)]
+        L.sdmd_gpu_destroy.argtypes = [C.c_void_p]
+        L.sdmd_gpu_destroy.restype = None
+        L.sdmd_gpu_prepare.argtypes = [C.c_void_p, C.c_int32]
+        L.sdmd_gpu_run.argtypes = [C.c_void_p, C.c_int64, C.c_double]
+        L.sdmd_gpu_download.argtypes = [C.c_void_p, P(sdmd_system), C.c_int32]
+        L.sdmd_gpu_trace.argtypes = [C.c_void_p, C.c_int32, P(sdmd_trace_rec), C.c_int32, P(C.c_int32)]
+        L.sdmd_gpu_last_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+        L.sdmd_gpu_last_error.argtypes = [C.c_void_p, P(sdmd_error_info)]
+        L.sdmd_rng_seed.argtypes = [P(sdmd_rng), C.c_uint32]
+        L.sdmd_rng_seed.restype = None
+        L.sdmd_rng_next.argtypes = [P(sdmd_rng)]
+        L.sdmd_rng_next.restype = C.c_int32
+        L.sdmd_rng_skip.argtypes = [P(sdmd_rng), C.c_int64]
+        L.sdmd_rng_skip.restype = None
+        _lib = L
+    return _lib
+
+
+def strerror(code):
+    try:
+        return lib().sdmd_gpu_strerror(int(code)).decode()
+    except Exception:
+        return "error"
+
+
+def device_count():
+    n = C.c_int32(0)
+    lib().sdmd_gpu_device_count(C.byref(n))
+    return n.value
+
+
+class Engine:
+    """A handle over a batch of systems (sdmd_gb300.system.System objects)."""
+
+    def __init__(self, systems, advance=ADVANCE_EAGER, screen=SCREEN_FP64, threads=0, trace=0, device=0):
+        self.systems = list(systems)
+        self.structs = (sdmd_system * len(self.systems))(*[s.struct() for s in self.systems])
+        o = sdmd_opts()
+        o.advance, o.screen, o.threads_per_system, o.device, o.trace_capacity = advance, screen, threads, device, trace
+        self.opts = o
+        h = C.c_void_p()
+        rc = lib().sdmd_gpu_create(self.structs, len(self.systems), C.byref(o), C.byref(h))
+        if rc:
+            raise EngineError(rc, "sdmd_gpu_create")
+        self.h = h
+
+    def _check(self, rc, where):
+        if rc:
+            info = sdmd_error_info()
+            lib().sdmd_gpu_last_error(self.h, C.byref(info))
+            raise EngineError(rc, where, info)
+
+    def prepare(self, full=True):
+        self._check(lib().sdmd_gpu_prepare(self.h, 1 if full else 0), "sdmd_gpu_prepare")
+
+    def run(self, max_events, t_end=0.0):
+        self._check(lib().sdmd_gpu_run(self.h, int(max_events), float(t_end)), "sdmd_gpu_run")
+
+    def download(self):
+        """Copy device state back into the System objects' arrays and scalars."""
+        self._check(lib().sdmd_gpu_download(self.h, self.structs, len(self.systems)), "sdmd_gpu_download")
+        for s, st in zip(self.systems, self.structs):
+            s.pull_scalars(st)
+
+    def trace(self, s=0, cap=None):
+        cap = cap if cap is not None else max(self.opts.trace_capacity, 1)
+        out = np.zeros(cap, TRACE_DTYPE)
+        n = C.c_int32(0)
+        self._check(lib().sdmd_gpu_trace(self.h, s, out.ctypes.data_as(C.POINTER(sdmd_trace_rec)), cap,
+                                         C.byref(n)), "sdmd_gpu_trace")
+        return out[:n.value]
+
+    def last_ms(self):
+        a, b = C.c_double(0), C.c_double(0)
+        lib().sdmd_gpu_last_ms(self.h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().sdmd_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

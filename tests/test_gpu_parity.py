@@ -1,0 +1,142 @@
+"""CUDA engine vs the reference's golden fixtures and the CPU oracle (GPU).
+
+The exact FP64 path must reproduce the reference bit for bit: the full-rebuild
+sweep (src/SGThread.c:47-52), the event tree (src/CBT.c), every popped event of
+the loop (src/SGThread.c:75-151) and the state at every checkpoint.  All calls go
+through the C ABI (libsdmd_gpu.so).
+"""
+import numpy as np
+import pytest
+
+from sdmd_gb300.system import fixture_dynamic, from_fixture
+
+pytestmark = pytest.mark.gpu
+
+DYN = ["x", "y", "z", "vx", "vy", "vz", "cx", "cy", "cz", "type", "hb_bond", "hb_itype", "nb_partner", "nb_status",
+       "nb_pnum", "ev_time", "ev_partner", "ev_counter", "ev_pcounter", "ev_potential", "ev_type", "ev_sub",
+       "cell_list"]
+SWEEP = ["ev_time", "ev_partner", "ev_type", "ev_sub", "ev_potential", "ev_pcounter", "nb_pnum", "hb_itype"]
+
+
+@pytest.fixture(scope="module")
+def engine_mod():
+    import __graft_entry__ as G
+    G.build()
+    from sdmd_gb300 import engine
+    if engine.device_count() < 1:
+        pytest.fail("no CUDA device visible: the GPU tests need one")
+    return engine
+
+
+def assert_state_equal(a, ref, keys=DYN):
+    for k in keys:
+        x, y = a[k], ref[k]
+        if not np.array_equal(x, y):
+            idx = np.nonzero(x != y)[0][:5]
+            raise AssertionError(f"{k} differs at {idx}: {x[idx]} vs {y[idx]}")
+
+
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long"])
+def test_sweep_matches_reference(golden, engine_mod, case):
+    d = golden(case)
+    s = from_fixture(d, "pre")
+    with engine_mod.Engine([s]) as eng:
+        eng.prepare(full=True)
+        eng.download()
+    assert_state_equal(s.a, fixture_dynamic(d, "sweep"), SWEEP)
+    assert s.counters["warnings"] == int(d["sweep/warningsum"][0])
+
+
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt"])
+def test_loop_matches_reference_event_for_event(golden, engine_mod, case):
+    d = golden(case)
+    ids, dts = d["trace/ids"], d["trace/dt"]
+    s = from_fixture(d, "pre")
+    with engine_mod.Engine([s], trace=len(ids) + 16) as eng:
+        eng.prepare(full=True)
+        eng.run(int(d["meta/n_events"][0]))
+        eng.download()
+        tr = eng.trace(0)
+    assert len(tr) == len(ids)
+    mine = np.stack([tr["target"], tr["partner"], tr["type"], tr["sub"], tr["executed"]], 1)
+    bad = np.nonzero((mine != ids).any(1) | (tr["dt"] != dts))[0]
+    assert len(bad) == 0, f"first divergence at pop {bad[0]}: {mine[bad[0]]} {tr['dt'][bad[0]]} vs {ids[bad[0]]} {dts[bad[0]]}"
+    full = d["trace/full_d"]
+    k = len(full)
+    assert np.array_equal(tr["time_now"][:k], full[:, 1])
+    assert np.array_equal(tr["vt"][:k], full[:, 2:5])
+    ref = fixture_dynamic(d, "final")
+    assert_state_equal(s.a, ref)
+    assert s.counters == ref["_counters"]
+    assert s.time == ref["_time"]
+
+
+def test_long_run_with_hb_events(golden, engine_mod):
+    """1.5e5 events covering HB formation/breaking and HB-neighbour events, in
+    chunks (the device state persists between run calls)."""
+    d = golden("ala10_nvt_long")
+    s = from_fixture(d, "pre")
+    with engine_mod.Engine([s]) as eng:
+        eng.prepare(full=True)
+        done = 0
+        for c in [int(v) for v in d["meta/ckpts"]] + [int(d["meta/n_events"][0])]:
+            eng.run(c - done)
+            done = c
+            eng.download()
+            ref = fixture_dynamic(d, f"ckpt{c}" if f"ckpt{c}/x" in d.files else "final")
+            assert_state_equal(s.a, ref)
+            assert s.counters == ref["_counters"], c
+    assert s.counters["hb"] > 0 and s.counters["hbneighbor"] > 0
+
+
+def test_batch_of_systems_matches_oracle(golden, engine_mod):
+    """Several independent systems in one launch (one CTA each): NVE, NVT and NVT
+    with other RNG streams; each must equal its own oracle run."""
+    from oracle import oracle as O
+    d_nvt, d_nve = golden("ala10_nvt"), golden("ala10_nve")
+    systems = [from_fixture(d_nve, "pre"), from_fixture(d_nvt, "pre")]
+    for seed in (11, 12, 13):
+        s = from_fixture(d_nvt, "pre")
+        from tests.golden.make_golden import rng_state_after
+        s.rng = rng_state_after(seed, 0)
+        systems.append(s)
+    refs = [s.copy() for s in systems]
+    with engine_mod.Engine(systems, threads=64) as eng:
+        eng.prepare(full=True)
+        eng.run(3000)
+        eng.download()
+    for s, r in zip(systems, refs):
+        O.predict_all(r)
+        loop = O.Loop(r)
+        rc, _, _ = loop.run(3000)
+        assert rc == 0
+        assert_state_equal(s.a, r.a)
+        assert s.counters == r.counters and s.time == r.time
+
+
+@pytest.mark.parametrize("threads", [32, 96, 256])
+def test_block_size_does_not_change_results(golden, engine_mod, threads):
+    d = golden("ala10_nvt")
+    s = from_fixture(d, "pre")
+    with engine_mod.Engine([s], threads=threads) as eng:
+        eng.prepare(full=True)
+        eng.run(2000)
+        eng.download()
+    ref = fixture_dynamic(d, "ckpt1000")
+    s2 = from_fixture(d, "pre")
+    with engine_mod.Engine([s2], threads=threads) as eng:
+        eng.prepare(full=True)
+        eng.run(1000)
+        eng.download()
+    assert_state_equal(s2.a, ref)
+
+
+def test_degenerate_rng_state_is_rejected_on_the_host(golden, engine_mod):
+    """An all-zero RNG state would make the rejection sampler loop; the ABI
+    refuses it before anything reaches the device."""
+    d = golden("ala10_nvt")
+    s = from_fixture(d, "pre")
+    s.rng[:] = 0
+    with pytest.raises(engine_mod.EngineError) as e:
+        engine_mod.Engine([s])
+    assert e.value.code == -1
