@@ -1,0 +1,79 @@
+/*
+ * sdmd_host.h -- host-side C library: builds an engine system (sdmd_system,
+ * include/sdmd_gpu.h) from the reference sDMD's own inputs.
+ *
+ * It reads the same files with the same semantics as the reference's "new run"
+ * path: parameter.txt by position (ReadParameter, src/Initialization.c:512-730),
+ * a .gro/.pdb coordinate file filtered through the force-field library
+ * (ModifyCoordinateFile/ReadGROFile/ReadPDBFile, src/Initialization.c:733-989),
+ * the Library_<Force_Field> model files (ReadModel/ScanAA, :1076-1339;
+ * CreatePotentialMatrix, :1468-1544; ReadHB/HBNeighborAssign, :1572-1847;
+ * ReadWall, :1894-2053), Maxwell-Boltzmann velocities from the seeded rand()
+ * stream (GenerateVelocity, :1850-1881), and Prepare()'s set-up up to the
+ * full-rebuild sweep: SDEnergyMin, PBC and LinkList (src/SGThread.c:21-46).
+ */
+#ifndef SDMD_HOST_H
+#define SDMD_HOST_H
+
+#include "sdmd_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sdmd_params {
+    char   continue_mode[20];      /* "new" or "continue" */
+    double time;                   /* Time: the loop runs while currenttime <= Time */
+    char   temperature_str[20];    /* "no" keeps the previous temperature */
+    double temperature;            /* reduced (kcal/mol) */
+    double dump_rate;
+    double cutoff;                 /* A */
+    char   force_field[20];        /* "Ding" */
+    char   thermostat[20];         /* "Andersen" or "no" */
+    double thermo_freq;
+    char   cg[16];                 /* "no" */
+    char   wall_exist[20];         /* "no" or "smooth" */
+    char   wall_type[20];          /* "no", "parallel", "cylinder", "sphere" */
+    char   wall_dyn[16];           /* "no" */
+    char   flow[32], obstruct[32], tunnel[32], sphobst[32];   /* "no" */
+} sdmd_params;
+
+typedef struct sdmd_host_system sdmd_host_system;   /* owns every array of an sdmd_system */
+
+/* Parse parameter.txt (positional, 16 lines).  Returns SDMD_OK or SDMD_EINVAL. */
+int sdmd_read_parameters(const char *path, sdmd_params *out);
+
+/* Build a system from <datadir>/<coord_file> and <datadir>/Library_<ff>/.
+ * box: used only for .pdb files (the reference's -box flag), else NULL.
+ * seed: srand() seed; the reference uses time(NULL), or 1575263273 when built
+ * with -DDEBUG_RANDOM.  energy_min_steps: SDEnergyMin's step limit (20000 in
+ * Prepare()); 0 skips it.  errbuf (may be NULL) receives a message on failure. */
+int sdmd_build_system(const char *datadir, const char *coord_file, const sdmd_params *p, const double *box,
+                      uint32_t seed, int energy_min_steps, sdmd_host_system **out, char *errbuf, int errlen);
+
+/* Same, from in-memory .gro text (no file I/O for the coordinates). */
+int sdmd_build_system_gro_text(const char *datadir, const char *gro_text, const sdmd_params *p, uint32_t seed,
+                               int energy_min_steps, sdmd_host_system **out, char *errbuf, int errlen);
+
+/* Synthetic workloads: n_chains peptides (each a string of 3-letter residue
+ * codes separated by spaces), relaxed against the model's distance bounds,
+ * rotated uniformly at random and placed without overlap in the box (inside a
+ * cylinder of radius box[1]/2 about the x axis, `margin` A from its surface,
+ * when wall == SDMD_WALL_CYLINDER).  Writes malloc'd .gro text to *gro_out
+ * (free with sdmd_free_text). */
+int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const char *const *sequences,
+                      const double box[3], int wall, double margin, uint64_t seed, char **gro_out, char *errbuf,
+                      int errlen);
+void sdmd_free_text(char *p);
+
+sdmd_system *sdmd_host_view(sdmd_host_system *h);
+void sdmd_host_free(sdmd_host_system *h);
+
+/* Atom names (8 bytes each, entry i*8) and residue names, for output writers. */
+const char *sdmd_host_atom_names(const sdmd_host_system *h);
+const char *sdmd_host_residue_names(const sdmd_host_system *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -86,7 +86,7 @@ def build_host(force=False):
     if not force and _newer(HOST_LIB, deps):
         return HOST_LIB
     tmp = HOST_LIB + ".tmp"
-    subprocess.check_call(["gcc", "-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared", "-Wall",
+    subprocess.check_call(["gcc", "-O2", "-std=gnu99", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-pthread",
                            "-I" + INCLUDE, "-I" + HOST, "-o", tmp, *srcs, "-lm"])
     os.replace(tmp, HOST_LIB)
     return HOST_LIB

@@ -190,9 +190,29 @@ def cases():
     return out
 
 
+def bundle_force_field():
+    """Copy the reference's force-field input tables (Library_Ding, MIT licence,
+    input/Library_Ding/ of alexzheng42/sDMD) next to the fixtures: the tests and
+    the benchmark build systems from them on machines without the reference."""
+    src = os.path.join(REF, "input", "Library_Ding")
+    dst = os.path.join(HERE, "Library_Ding")
+    if os.path.isdir(dst):
+        shutil.rmtree(dst)
+    shutil.copytree(src, dst)
+    for root, dirs, files in os.walk(dst):
+        for f in files:
+            os.chmod(os.path.join(root, f), 0o644)
+    with open(os.path.join(dst, "PROVENANCE.txt"), "w") as f:
+        f.write("Force-field input tables of sDMD (alexzheng42/sDMD, input/Library_Ding), MIT licence,\n"
+                "Copyright (c) 2018 Size Zheng.  Copied unchanged by tests/golden/make_golden.py as input data.\n")
+
+
 def main(argv):
     if not os.path.isdir(REF):
         sys.exit("the reference sources are not present; golden fixtures can only be regenerated where they are")
+    bundle_force_field()
+    if argv == ["--force-field-only"]:
+        return
     build_harness()
     all_cases = cases()
     names = argv or list(all_cases)
