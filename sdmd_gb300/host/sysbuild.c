@@ -1576,16 +1576,28 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
                     if (sqrt(ry * ry + rz * rz) > box[1] / 2 - margin) { ok = 0; break; }
                     if (q[0] < 0 || q[0] >= box[0]) { ok = 0; break; }
                 } else {
-                    for (int d = 0; d < 3; d++) if (q[d] < 0 || q[d] >= box[d]) ok = 0;
+                    /* periodic box: the build wraps every atom once (PBC "full"), so stay
+                       within one box length of the primary cell */
+                    for (int d = 0; d < 3; d++) if (q[d] < -box[d] || q[d] >= 2 * box[d]) ok = 0;
                 }
                 if (!ok) break;
                 int gc[3];
-                for (int d = 0; d < 3; d++) { gc[d] = (int)(q[d] / G); if (gc[d] >= gn[d]) gc[d] = gn[d] - 1; if (gc[d] < 0) gc[d] = 0; }
+                for (int d = 0; d < 3; d++) {
+                    double w = fmod(q[d], box[d]); if (w < 0) w += box[d];
+                    gc[d] = (int)(w / G); if (gc[d] >= gn[d]) gc[d] = gn[d] - 1; if (gc[d] < 0) gc[d] = 0;
+                }
                 for (int dz = -1; dz <= 1 && ok; dz++) for (int dy = -1; dy <= 1 && ok; dy++) for (int dx = -1; dx <= 1 && ok; dx++) {
                     int x = gc[0] + dx, y = gc[1] + dy, z = gc[2] + dz;
                     if (x < 0 || y < 0 || z < 0 || x >= gn[0] || y >= gn[1] || z >= gn[2]) continue;
-                    for (int a = head[((long)z * gn[1] + y) * gn[0] + x]; a >= 0; a = next[a])
-                        if (dist3(q, all + 3 * a) < 4.0) { ok = 0; break; }
+                    for (int a = head[((long)z * gn[1] + y) * gn[0] + x]; a >= 0; a = next[a]) {
+                        double dd = 0;
+                        for (int d = 0; d < 3; d++) {   /* minimum image */
+                            double v = q[d] - all[3 * a + d];
+                            v -= box[d] * floor(v / box[d] + 0.5);
+                            dd += v * v;
+                        }
+                        if (dd < 16.0) { ok = 0; break; }
+                    }
                 }
             }
         }
@@ -1608,7 +1620,10 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
             rid[a] = ri[i];   /* residue numbers restart at 1 in every chain */
             const double *q = all + 3 * a;
             int gc[3];
-            for (int d = 0; d < 3; d++) { gc[d] = (int)(q[d] / G); if (gc[d] >= gn[d]) gc[d] = gn[d] - 1; if (gc[d] < 0) gc[d] = 0; }
+            for (int d = 0; d < 3; d++) {
+                double w = fmod(q[d], box[d]); if (w < 0) w += box[d];
+                gc[d] = (int)(w / G); if (gc[d] >= gn[d]) gc[d] = gn[d] - 1; if (gc[d] < 0) gc[d] = 0;
+            }
             long cell = ((long)gc[2] * gn[1] + gc[1]) * gn[0] + gc[0];
             next[a] = head[cell]; head[cell] = a;
         }

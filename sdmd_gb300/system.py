@@ -99,6 +99,32 @@ class sdmd_error_info(C.Structure):
 WALL = {"no": 0, "parallel": 1, "cylinder": 2, "sphere": 3}
 
 
+def glibc_rng_state(seed, skip=0):
+    """The rand() stream state after srand(seed) and `skip` draws, as the
+    33-entry sdmd_rng layout [tab[0..30], front, rear].  Lehmer-seeded additive
+    feedback generator of degree 31 and separation 3 (the first 310 outputs are
+    discarded at seeding)."""
+    r = [0] * 31
+    r[0] = seed if seed != 0 else 1
+    for i in range(1, 31):
+        hi, lo = divmod(r[i - 1], 127773)
+        w = 16807 * lo - 2836 * hi
+        if w < 0:
+            w += 2147483647
+        r[i] = w
+    f, b = 3, 0
+    for _ in range(310 + skip):
+        r[f] = (r[f] + r[b]) & 0xFFFFFFFF
+        f += 1
+        b += 1
+        if f >= 31:
+            f = 0
+        elif b >= 31:
+            b = 0
+    tab = np.array(r, np.uint32).view(np.int32)
+    return np.concatenate([tab, np.array([f, b], np.int32)])
+
+
 class System:
     """Arrays of one system plus its ctypes view.  Construct with `from_arrays`."""
 

@@ -1,0 +1,106 @@
+"""The benchmark configurations, built from seeded synthetic inputs.
+
+Every system goes through the same path a user's input does: .gro text (here
+generated: random-sequence peptides, relaxed and placed without overlap) plus
+parameter.txt, read by the host-side C builder with the reference's semantics
+and the force-field tables of Library_Ding.  No public dataset is involved.
+
+  C1  one ALA x 10 chain (59 atoms), extended start, 40 A cube, Andersen NVT at
+      300 K (T* = 300 * 0.0019872041 = 0.5962), Thermo_Freq 6, cutoff 9 A
+  C2  256 chains x 16 residues, residues uniform over the 20 amino acids,
+      random rigid placement at 5 mM: cube edge (256 / (0.005 N_A))^(1/3) = 440 A
+  C3  64 replicas of C1, temperatures geometric 270-500 K
+  C4  512 single chains of 5-60 residues, box edge scaled to C1's density,
+      temperatures 280-400 K
+  C5  replicas of 400 ten-residue chains in a cylinder (radius 60 A, axis x,
+      120 A periodic), NVT 310 K
+"""
+import json
+import os
+import tempfile
+
+import numpy as np
+
+from .host import AMINO_ACIDS, build_system, generate_gro, params_text
+from .system import glibc_rng_state
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DATA = os.path.join(REPO, "tests", "golden")          # holds Library_Ding (force-field input tables)
+BOLTZMANN = 0.0019872041                               # kcal/mol/K (src/REMDExec.c:19)
+
+
+CACHE = os.environ.get("SDMD_WORKLOAD_CACHE", os.path.join(tempfile.gettempdir(), "sdmd_workloads"))
+
+
+def cached(key, make):
+    """Build a System once per machine session (keyed by the workload parameters
+    and the host library's build time) and reload it from an .npz afterwards."""
+    from .host import HOST_LIB
+    from .system import System
+    os.makedirs(CACHE, exist_ok=True)
+    stamp = int(os.path.getmtime(HOST_LIB)) if os.path.exists(HOST_LIB) else 0
+    path = os.path.join(CACHE, f"{key}_{stamp}.npz")
+    if os.path.exists(path):
+        d = np.load(path, allow_pickle=False)
+        s = System()
+        for k in d.files:
+            if k.startswith("a/"):
+                s.a[k[2:]] = d[k].copy()
+        s.scal = json.loads(str(d["scal"]))
+        s.counters = json.loads(str(d["counters"]))
+        s.rng = d["rng"].copy()
+        s.time = float(d["time"])
+        return s
+    s = make()
+    tmp = path + f".{os.getpid()}.tmp.npz"
+    np.savez(tmp, scal=json.dumps(s.scal), counters=json.dumps(s.counters), rng=s.rng, time=s.time,
+             **{f"a/{k}": v for k, v in s.a.items()})
+    os.replace(tmp, path)
+    return s
+
+
+def _datadir(param_kw):
+    d = tempfile.mkdtemp(prefix="sdmd_wl_")
+    os.symlink(os.path.join(DATA, "Library_Ding"), os.path.join(d, "Library_Ding"))
+    with open(os.path.join(d, "parameter.txt"), "w") as f:
+        f.write(params_text(**param_kw))
+    return d
+
+
+def random_sequences(n, length, seed, lo=None, hi=None):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        L = length if lo is None else int(rng.integers(lo, hi + 1))
+        out.append([AMINO_ACIDS[k] for k in rng.integers(0, 20, L)])
+    return out
+
+
+def c1(seed=1, temperature_k=300.0, thermostat="Andersen", box=40.0, rng_seed=1575263273):
+    d = _datadir(dict(temp=round(temperature_k * BOLTZMANN, 4), thermostat=thermostat, time=1e9))
+    gro = generate_gro(d, [["ALA"] * 10], (box, box, box), seed=seed)
+    return build_system(d, gro_text=gro, seed=rng_seed)
+
+
+def c2(n_chains=256, length=16, seed=1, temperature_k=300.0, thermostat="Andersen", conc_mM=5.0,
+       rng_seed=1575263273):
+    edge = (n_chains / (conc_mM * 1e-3 * 6.02214076e23) * 1e27) ** (1.0 / 3.0)   # A
+
+    def make():
+        d = _datadir(dict(temp=round(temperature_k * BOLTZMANN, 4), thermostat=thermostat, time=1e9))
+        gro = generate_gro(d, random_sequences(n_chains, length, seed), (edge, edge, edge), seed=seed)
+        return build_system(d, gro_text=gro, seed=rng_seed)
+
+    return cached(f"c2_{n_chains}_{length}_{seed}_{temperature_k}_{thermostat}_{conc_mM}_{rng_seed}", make)
+
+
+def c3(n_replicas=64, t_lo=270.0, t_hi=500.0, seed=1):
+    base = c1(seed=seed)
+    out = []
+    for k in range(n_replicas):
+        s = base.copy()
+        t = t_lo * (t_hi / t_lo) ** (k / max(n_replicas - 1, 1))
+        s.scal["temperature"] = t * BOLTZMANN
+        s.rng = glibc_rng_state(1000 + k)
+        out.append(s)
+    return out
