@@ -194,7 +194,9 @@ def run_ours(args, D):
     E = args.events_per_step
     host_copy = [s.copy() for s in systems]
 
-    eng = Engine(systems, threads=args.threads, device=D.local)
+    from sdmd_gb300.engine import ADVANCE_EAGER, ADVANCE_LAZY
+    adv = ADVANCE_LAZY if args.advance == "lazy" else ADVANCE_EAGER
+    eng = Engine(systems, threads=args.threads, device=D.local, advance=adv)
     eng.prepare(full=True)
     sweep_ms = eng.last_ms()[0]
     eng.download()
@@ -239,7 +241,7 @@ def run_ours(args, D):
     for k in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        with Engine(work, threads=args.threads, device=D.local) as e2:
+        with Engine(work, threads=args.threads, device=D.local, advance=adv) as e2:
             e2.prepare(full=False)
             e2.run(E)
             e2.download()
@@ -251,7 +253,9 @@ def run_ours(args, D):
     P = neighbourhood_mean(after_sweep[0])
     logn = math.ceil(math.log2(max(after_sweep[0].n, 2)))
     pops_per_event = 1.0 + after_sweep[0].counters.get("recal", 0) / max(after_sweep[0].counters.get("frame", 1), 1)
-    per_event = 2 * P * 56 + 2 * 104 + 2 * logn * 12 + pops_per_event * after_sweep[0].n * 56   # eager advance
+    per_event = 2 * P * 56 + 2 * 104 + 2 * logn * 12
+    if args.advance == "eager":
+        per_event += pops_per_event * after_sweep[0].n * 56   # every pop moves every atom and event time
     bytes_per_launch = per_event * (events / max(args.steps, 1))
     launch_s = t_dev / max(args.steps, 1)
     peak, peak_kind = peaks()
@@ -274,7 +278,7 @@ def run_ours(args, D):
 
     if D.rank == 0:
         cfg.update({"n_atoms": natoms, "n_systems": len(systems) * D.world, "events_per_step": E,
-                    "l2": "flushed between steps (256 MiB write)", "advance": "eager", "screen": "fp64",
+                    "l2": "flushed between steps (256 MiB write)", "advance": args.advance, "screen": "fp64",
                     "threads_per_system": args.threads or 128, "replicas": "independent per rank" if D.world > 1 else None})
         line = {"metric": METRIC, "value": round(value, 3), "unit": "events/s", "n_gpus": D.world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_max * 1e3 / args.steps, 3),
@@ -352,6 +356,7 @@ def main():
     ap.add_argument("--workload", default="c2")
     ap.add_argument("--events-per-step", type=int, default=20000)
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--advance", choices=["eager", "lazy"], default="lazy")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

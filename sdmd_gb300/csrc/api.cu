@@ -31,7 +31,9 @@ struct sdmd_gpu {
     unsigned char *arena = nullptr;
     size_t arena_bytes = 0;
     int threads = 128;
-    size_t smem = 0;
+    size_t smem = 0, smem_loop = 0;
+    int staged = 0;
+    std::vector<int32_t> smp_cap_of;
     double prep_ms = 0, run_ms = 0;
     sdmd_error_info err{};
 };
@@ -214,6 +216,13 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
         d.sc = cv.take<DScal>(1);
         d.trace = cv.take<sdmd_trace_rec>(trace_cap > 0 ? trace_cap : 1);
         d.trace_cap = trace_cap;
+        d.smp_cap = s.thermostat ? h->smp_cap_of[k] : 0;
+        size_t sc_ = d.smp_cap > 0 ? (size_t)d.smp_cap : 1;
+        d.smp = cv.take<double>(sc_);
+        d.smp_raw = cv.take<int32_t>(3 * sc_);
+        d.smp_cum = cv.take<int64_t>(sc_);
+        d.tloc = cv.take<double>(N1);
+        d.lazy = h->opts.advance == SDMD_ADVANCE_LAZY ? 1 : 0;
         if (copies) {
             auto &c = *copies;
             put(c, (double *)d.mass, s.mass, N1);
@@ -284,14 +293,19 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     sdmd_gpu *h = new sdmd_gpu();
     if (opts) h->opts = *opts;
     if (h->opts.device < 0 || h->opts.device >= ndev) { delete h; return SDMD_EINVAL; }
-    if (h->opts.advance != SDMD_ADVANCE_EAGER || h->opts.screen != SDMD_SCREEN_FP64) { delete h; return SDMD_EUNSUPPORTED; }
+    if ((h->opts.advance != SDMD_ADVANCE_EAGER && h->opts.advance != SDMD_ADVANCE_LAZY) ||
+        h->opts.screen != SDMD_SCREEN_FP64) { delete h; return SDMD_EUNSUPPORTED; }
     int r = cuda_fail(cudaSetDevice(h->opts.device));
     if (r) { delete h; return r; }
     h->n_systems = n_systems;
     h->hs.resize(n_systems);
     h->meta.resize(n_systems);
     int nbcap_max = 0;
+    h->smp_cap_of.resize(n_systems);
     for (int k = 0; k < n_systems; k++) {
+        long per = (1L << 23) / n_systems;
+        per = per < 4096 ? 4096 : per > 65536 ? 65536 : per;
+        h->smp_cap_of[k] = (int32_t)std::max<long>(per, (long)systems[k].n_atoms + 64);
         const sdmd_system &s = systems[k];
         SysMeta &m = h->meta[k];
         m.n = s.n_atoms;
@@ -311,8 +325,18 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         d.thermostat = s.thermostat; d.wall = s.wall; d.wall_type = s.wall_type;
         d.cutoff = s.cutoff; d.temperature = s.temperature; d.thermo_freq = s.thermo_freq; d.t_end = s.t_end;
         d.nbcap = m.nbcap;
+        d.n_bonds = s.n_bonds; d.n_cons = s.n_cons; d.n_con_steps = s.n_con_steps; d.n_conn = s.n_conn;
     }
     h->smem = fp64_smem_bytes(nbcap_max);
+    // stage whole systems in shared memory when they fit (small systems, batches)
+    size_t st_max = 0;
+    for (int k = 0; k < n_systems; k++) {
+        const sdmd_system &s = systems[k];
+        st_max = std::max(st_max, staged_state_bytes(s.n_atoms, h->meta[k].ncell, s.n_bonds, s.n_cons,
+                                                     s.n_con_steps, s.n_conn));
+    }
+    h->staged = (h->smem + st_max <= 200 * 1024) ? 1 : 0;
+    h->smem_loop = h->staged ? h->smem + st_max : h->smem;
     h->threads = h->opts.threads_per_system > 0 ? h->opts.threads_per_system : 128;
     if (h->threads < 32 || h->threads > 1024 || (h->threads & 31)) { delete h; return SDMD_EINVAL; }
     if (h->smem > 227 * 1024) { delete h; return SDMD_ECAPACITY; }
@@ -339,10 +363,11 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         cudaMemcpyAsync(h->hs[k].sc, &sc[k], sizeof(DScal), cudaMemcpyHostToDevice, h->stream);
     }
     cudaMemcpyAsync(h->ds, h->hs.data(), sizeof(DSys) * n_systems, cudaMemcpyHostToDevice, h->stream);
-    if (h->smem > 48 * 1024) {
+    if (h->smem > 48 * 1024)
         cudaFuncSetAttribute(sweep_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
-        cudaFuncSetAttribute(loop_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
-    }
+    if (h->smem_loop > 48 * 1024)
+        cudaFuncSetAttribute(loop_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem_loop);
+    if (h->opts.advance == SDMD_ADVANCE_LAZY) lazy_enter_kernel<<<n_systems, 128, 0, h->stream>>>(h->ds);
     if ((r = cuda_fail(cudaStreamSynchronize(h->stream)))) { sdmd_gpu_destroy(h); return r; }
     *out = h;
     return SDMD_OK;
@@ -363,11 +388,29 @@ static int collect_errors(sdmd_gpu *h) {
     return SDMD_OK;
 }
 
+static int n_blocks(int n, int t) { return (n + t - 1) / t; }
+
+// draw a fresh batch of normal samples for every system that still runs
+static void launch_samples(sdmd_gpu *h, int64_t want) {
+    samples_walk_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems, want);
+    int64_t cap = 0;
+    for (auto &m : h->hs) cap = std::max<int64_t>(cap, m.smp_cap);
+    if (cap > 0) {
+        int64_t w = std::min<int64_t>(want, cap);
+        dim3 grid((unsigned)std::max<int64_t>(1, std::min<int64_t>((w + 255) / 256, 1024)), (unsigned)h->n_systems);
+        samples_values_kernel<<<grid, 256, 0, h->stream>>>(h->ds, w);
+    }
+}
+
 extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
     if (!h) return SDMD_EINVAL;
     CK(cudaSetDevice(h->opts.device));
+    int32_t nmax = 0;
+    for (auto &m : h->meta) nmax = std::max(nmax, m.n);
     CK(cudaEventRecord(h->e0, h->stream));
+    if (full_predict) launch_samples(h, (int64_t)nmax + 8);
     sweep_kernel_fp64<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+    if (full_predict) samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->e1, h->stream));
     CK(cudaEventSynchronize(h->e1));
@@ -381,8 +424,23 @@ extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
     if (!h || max_events < 0) return SDMD_EINVAL;
     CK(cudaSetDevice(h->opts.device));
     CK(cudaEventRecord(h->e0, h->stream));
-    loop_kernel_fp64<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, max_events, t_end);
-    CK(cudaGetLastError());
+    begin_run_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems, max_events);
+    // each round: a sample batch, the loop until it runs low, then the rand() state
+    // is moved past the consumed draws; systems without a thermostat need one round
+    std::vector<DScal> sc(h->n_systems);
+    int64_t want = std::min<int64_t>(4 * max_events + 64, 1 << 16);
+    for (int round = 0; round < 1 << 20; round++) {
+        launch_samples(h, want);
+        loop_kernel_fp64<<<h->n_systems, h->threads, h->smem_loop, h->stream>>>(h->ds, t_end, h->staged);
+        samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
+        CK(cudaGetLastError());
+        for (int k = 0; k < h->n_systems; k++)
+            CK(cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        bool again = false;
+        for (auto &c : sc) if (c.paused && !c.err) again = true;
+        if (!again) break;
+    }
     CK(cudaEventRecord(h->e1, h->stream));
     CK(cudaEventSynchronize(h->e1));
     float ms = 0;
@@ -402,11 +460,30 @@ extern "C" int sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_sy
         });
         cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream);
     }
+    std::vector<std::vector<double>> tl(n_systems);
+    if (h->opts.advance == SDMD_ADVANCE_LAZY)
+        for (int k = 0; k < n_systems; k++) {
+            tl[k].resize((size_t)h->meta[k].n + 1);
+            cudaMemcpyAsync(tl[k].data(), h->hs[k].tloc, tl[k].size() * 8, cudaMemcpyDeviceToHost, h->stream);
+        }
     CK(cudaStreamSynchronize(h->stream));
     for (int k = 0; k < n_systems; k++) {
-        systems[k].time = sc[k].time;
-        systems[k].rng = sc[k].rng;
-        systems[k].counters = sc[k].c;
+        sdmd_system &s = systems[k];
+        s.time = sc[k].time;
+        s.rng = sc[k].rng;
+        s.counters = sc[k].c;
+        if (h->opts.advance == SDMD_ADVANCE_LAZY) {
+            // back to the reference's representation: positions at the current
+            // time (same expression as the device's extrapolation), relative times
+            const double T = s.time;
+            for (int i = 1; i <= s.n_atoms; i++) {
+                double dt = T - tl[k][i];
+                s.x[i] = s.x[i] + s.vx[i] * dt;
+                s.y[i] = s.y[i] + s.vy[i] * dt;
+                s.z[i] = s.z[i] + s.vz[i] * dt;
+                s.ev_time[i] = s.ev_time[i] - T;
+            }
+        }
     }
     return SDMD_OK;
 }

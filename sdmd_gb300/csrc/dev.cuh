@@ -18,13 +18,16 @@ constexpr int NT = SDMD_NTYPES;
 // per-system scalars living in device memory
 struct DScal {
     double time;
-    sdmd_rng rng;
+    sdmd_rng rng;            // rand() state after every consumed draw
     sdmd_counters c;
     int32_t err, err_atom;
     int64_t err_event;
     int64_t pops;            // total pops (trace ring position)
     int32_t cbt_built;
-    int32_t pad;
+    int32_t paused;          // 1: the loop stopped because its normal-sample batch ran low
+    sdmd_rng rng0;           // state at the start of the current sample batch
+    int64_t smp_avail, smp_used;
+    int64_t target_frame;    // the run stops once c.frame reaches it
 };
 
 // one system's device arrays (all 1-based per-atom arrays, entry 0 unused)
@@ -59,7 +62,30 @@ struct DSys {
     sdmd_trace_rec *trace;
     int32_t trace_cap;
     int32_t nbcap;           // capacity of the gathered 27-cell neighbour list
+    // precomputed standard-normal samples of the rand() stream (see samples.cu)
+    double *smp;             // sample values, consumed in order
+    int32_t *smp_raw;        // 3 rand() outputs per sample (a, b, coin)
+    int64_t *smp_cum;        // rand() calls consumed up to and including sample k
+    int32_t smp_cap;
+    int32_t n_bonds, n_cons, n_con_steps, n_conn;
+    // lazy free flight: positions are valid at tloc[i]; event times are absolute
+    double *tloc;
+    int32_t lazy, pad3;
+    double now;              // the current time while a block works on this system
 };
+
+// position component of atom j at the current time (lazy mode extrapolates)
+__device__ __forceinline__ double lzx(const DSys &S, const double *x, const double *v, int j) {
+    return S.lazy ? x[j] + v[j] * (S.now - S.tloc[j]) : x[j];
+}
+
+// Total order on doubles as a signed 64-bit key (equal keys for +0.0 and -0.0):
+// FP64 compares cost as much as FP64 arithmetic on this part, integer compares
+// do not.
+__device__ __forceinline__ long long tkey(double d) {
+    long long b = __double_as_longlong(d);
+    return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
 
 // 27-cell scan order of the reference (src/DMD.c:117-121)
 __constant__ int8_t c_nbx[27] = {0, 1, 0, 0, 0, 1, 1, 1, -1, 0, 0, 0, -1, -1, -1, 0, 0, 1, -1, 1, -1, -1, -1, 1, 1, 1, -1};
@@ -335,9 +361,9 @@ __device__ inline void pair_kin(const DSys &S, int i, int j, Kin &k) {
             else if (ci[d] == S.cn[d] - 1 && cj[d] == 0) sh[d] = S.box[d];
         }
     }
-    double rx = S.x[i] - (S.x[j] + sh[0]);
-    double ry = S.y[i] - (S.y[j] + sh[1]);
-    double rz = S.z[i] - (S.z[j] + sh[2]);
+    double rx = lzx(S, S.x, S.vx, i) - (lzx(S, S.x, S.vx, j) + sh[0]);
+    double ry = lzx(S, S.y, S.vy, i) - (lzx(S, S.y, S.vy, j) + sh[1]);
+    double rz = lzx(S, S.z, S.vz, i) - (lzx(S, S.z, S.vz, j) + sh[2]);
     double vx = S.vx[i] - S.vx[j], vy = S.vy[i] - S.vy[j], vz = S.vz[i] - S.vz[j];
     k.rx = rx; k.ry = ry; k.rz = rz;
     k.r2 = rx * rx + ry * ry + rz * rz;

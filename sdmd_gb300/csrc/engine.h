@@ -11,5 +11,13 @@ struct DScal;
 // exact FP64 path (loop_fp64.cu)
 size_t fp64_smem_bytes(int nbcap);
 __global__ void sweep_kernel_fp64(const DSys *systems, int full);
-__global__ void loop_kernel_fp64(const DSys *systems, int64_t max_events, double t_end_override);
+__global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int staged);
+size_t staged_state_bytes(int n, int ncell, int nb, int nc, int ncs, int nconn);
+__global__ void lazy_enter_kernel(const DSys *systems);
+
+// thermostat sample stream (samples.cu)
+__global__ void samples_walk_kernel(const DSys *systems, int n_systems, int64_t want);
+__global__ void samples_values_kernel(const DSys *systems, int64_t want);
+__global__ void samples_commit_kernel(const DSys *systems, int n_systems);
+__global__ void begin_run_kernel(const DSys *systems, int n_systems, int64_t max_events);
 }  // namespace sdmd

@@ -21,6 +21,8 @@ namespace sdmd {
 // slot flags
 enum : int32_t { F_DUP = 1, F_FRESH = 2 };
 
+__host__ __device__ inline size_t al16(size_t b) { return (b + 15) & ~size_t(15); }
+
 struct Slots {
     int32_t *j, *info;      // info: flags | sub << 8 | warnings << 16
     double *t, *tdup, *pot;
@@ -35,6 +37,16 @@ struct Blk {                 // block-uniform scalars in shared memory
 
 __device__ inline void set_err(Blk &B, int code, int atom) {
     if (B.err == 0) { B.err = code; B.err_atom = atom; }
+}
+
+// lazy mode: bring atom a's position to the current time before it changes
+__device__ inline void sync_atom(const DSys &S, int a) {
+    if (!S.lazy || a <= 0) return;
+    double dt = S.now - S.tloc[a];
+    S.x[a] = S.x[a] + S.vx[a] * dt;
+    S.y[a] = S.y[a] + S.vy[a] * dt;
+    S.z[a] = S.z[a] + S.vz[a] * dt;
+    S.tloc[a] = S.now;
 }
 
 // ---------------------------------------------------------------------------
@@ -175,63 +187,93 @@ __device__ void eval_hb_scan(const DSys &S, int i, int j, double cut, Slots &L, 
 }
 
 // ---- running minimum (thread 0): JobAssign + CheckDuplication ---------------
-// (src/TimePrediction.c:1140-1158, 1101-1117)
-__device__ inline bool job_assign(const DSys &S, int i, int j, double t, double pot, int sub, int type) {
-    if (t > 0 && S.ev_time[i] > t) {
-        S.ev_potential[i] = pot; S.ev_sub[i] = sub; S.ev_time[i] = t; S.ev_type[i] = type;
-        if (j) { S.ev_partner[i] = j; S.ev_pcounter[i] = S.ev_counter[j]; }
-        else S.ev_partner[i] = INVALID;
+// (src/TimePrediction.c:1140-1158, 1101-1117).  The atom's running event lives in
+// thread 0's registers during a prediction and is stored once at the end.
+struct Cur {
+    long long key;          // tkey(time)
+    double time, potential;
+    int32_t partner, type, sub;
+    int64_t pcounter;
+};
+__device__ inline void cur_load(const DSys &S, int i, Cur &c) {
+    c.time = S.ev_time[i]; c.key = tkey(c.time); c.potential = S.ev_potential[i];
+    c.partner = S.ev_partner[i]; c.type = S.ev_type[i]; c.sub = S.ev_sub[i]; c.pcounter = S.ev_pcounter[i];
+}
+__device__ inline void cur_store(const DSys &S, int i, const Cur &c) {
+    S.ev_time[i] = c.time; S.ev_potential[i] = c.potential; S.ev_partner[i] = c.partner;
+    S.ev_type[i] = c.type; S.ev_sub[i] = c.sub; S.ev_pcounter[i] = c.pcounter;
+}
+__device__ inline bool job_assign(const DSys &S, Cur &c, int j, double t, double pot, int sub, int type) {
+    if (tkey(t) <= 0) return false;
+    if (S.lazy) t = S.now + t;          // lazy mode keeps absolute event times
+    const long long kt = tkey(t);
+    if (c.key > kt) {
+        c.potential = pot; c.sub = sub; c.time = t; c.key = kt; c.type = type;
+        if (j) { c.partner = j; c.pcounter = S.ev_counter[j]; }
+        else c.partner = INVALID;
         return true;
     }
     return false;
 }
-__device__ inline bool dup_assign(const DSys &S, int i, int j, double tdup, int type) {
-    if (S.ev_time[i] > tdup) {
-        S.ev_partner[i] = j; S.ev_potential[i] = S.ev_potential[j]; S.ev_sub[i] = S.ev_sub[j];
-        S.ev_time[i] = tdup; S.ev_type[i] = type; S.ev_pcounter[i] = S.ev_counter[j];
+__device__ inline bool dup_assign(const DSys &S, Cur &c, int j, double tdup, int type) {
+    const long long kt = tkey(tdup);
+    if (c.key > kt) {
+        c.partner = j; c.potential = S.ev_potential[j]; c.sub = S.ev_sub[j];
+        c.time = tdup; c.key = kt; c.type = type; c.pcounter = S.ev_counter[j];
         return true;
     }
     return false;
 }
-__device__ void resolve(const DSys &S, int i, const Slots &L, int n, int type, Blk &B) {
+__device__ void resolve(const DSys &S, Cur &c, const Slots &L, int n, int type, Blk &B) {
     for (int k = 0; k < n; k++) {
         int info = L.info[k];
         if (info < 0) continue;
         int j = L.j[k];
-        if ((info & F_DUP) && dup_assign(S, i, j, L.tdup[k], type)) continue;
+        if ((info & F_DUP) && dup_assign(S, c, j, L.tdup[k], type)) continue;
         B.warn += (info >> 16) & 0xff;
-        if (info & F_FRESH) job_assign(S, i, j, L.t[k], L.pot[k], (info >> 8) & 0xff, type);
+        if (info & F_FRESH) job_assign(S, c, j, L.t[k], L.pot[k], (info >> 8) & 0xff, type);
     }
 }
 
 // ---- scalar predictions (thread 0) -----------------------------------------
-// PBCandCrossCellTime (src/TimePrediction.c:598-632)
-__device__ void pcc_time(const DSys &S, int i) {
+// PBCandCrossCellTime (src/TimePrediction.c:598-632): the face-crossing time of
+// one dimension (computed by three threads at once; FP64 divisions are slow)
+__device__ double pcc_face(const DSys &S, int i, int d) {
+    const double pos = d == 0 ? S.x[i] : d == 1 ? S.y[i] : S.z[i];
+    const double v = d == 0 ? S.vx[i] : d == 1 ? S.vy[i] : S.vz[i];
+    const int ci = d == 0 ? S.cx[i] : d == 1 ? S.cy[i] : S.cz[i];
+    double lo = ci * S.cs[d], hi = (ci + 1) * S.cs[d];
+    if (v > 0) return (hi - pos + ZERO) / v;
+    if (v < 0) return (lo - pos - ZERO) / v;
+    return -1.0;   // no crossing in this dimension
+}
+__device__ void pcc_time(const DSys &S, Cur &c, const double *face) {
     double best = INFINIT;
-    const double pos[3] = {S.x[i], S.y[i], S.z[i]}, v[3] = {S.vx[i], S.vy[i], S.vz[i]};
-    const int ci[3] = {S.cx[i], S.cy[i], S.cz[i]};
     for (int d = 0; d < 3; d++) {
-        double lo = ci[d] * S.cs[d], hi = (ci[d] + 1) * S.cs[d], t;
-        if (v[d] > 0) { t = (hi - pos[d] + ZERO) / v[d]; if (best > t && t > 0) best = t; }
-        else if (v[d] < 0) { t = (lo - pos[d] - ZERO) / v[d]; if (best > t && t > 0) best = t; }
+        double t = face[d];
+        if (tkey(best) > tkey(t) && tkey(t) > 0) best = t;
     }
-    job_assign(S, i, 0, best, 0, SDMD_SUB_INVALID, SDMD_EV_PCC);
+    job_assign(S, c, 0, best, 0, SDMD_SUB_INVALID, SDMD_EV_PCC);
 }
 
 // ThermostatTime (src/TimePrediction.c:582-595)
-__device__ void thermostat_time(const DSys &S, int i, sdmd_rng &rng, Blk &B) {
+__device__ inline double take_sample(const DSys &S, DScal &C, Blk &B) {
+    if (C.smp_used >= C.smp_avail) { set_err(B, SDMD_ETIMEOUT, 0); return 1.0; }   // the loop pauses before this
+    return S.smp[C.smp_used++];
+}
+
+// ThermostatTime (src/TimePrediction.c:582-595): MB(0, 1) = the sample * sqrt(1) + 0
+__device__ void thermostat_time(const DSys &S, Cur &c, DScal &C, Blk &B) {
     if (!S.thermostat) return;
-    int bad = 0;
-    double t = mb_draw(rng, 0, 1, &bad);
-    if (bad) { set_err(B, SDMD_ETIMEOUT, i); return; }
-    job_assign(S, i, 0, S.thermo_freq * (t < 0 ? -t : t), 0, SDMD_SUB_INVALID, SDMD_EV_THERMOSTAT);
+    double t = take_sample(S, C, B) * sqrt(1.0) + 0;
+    job_assign(S, c, 0, S.thermo_freq * (t < 0 ? -t : t), 0, SDMD_SUB_INVALID, SDMD_EV_THERMOSTAT);
 }
 
 // HBTime for an HB-bonded atom (src/TimePrediction.c:329-387)
-__device__ void hb_bonded(const DSys &S, int i, Blk &B, int *bad) {
+__device__ void hb_bonded(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     int j = S.hb_bond[i];
     if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
-        dup_assign(S, i, j, S.ev_time[j], SDMD_EV_HB))
+        dup_assign(S, c, j, S.ev_time[j], SDMD_EV_HB))
         return;
     Kin kk; pair_kin(S, i, j, kk);
     Lim o; int warn = 0;
@@ -245,17 +287,17 @@ __device__ void hb_bonded(const DSys &S, int i, Blk &B, int *bad) {
     }
     double t = root(kk, st, d2);
     if (t < 0) t = INFINIT;
-    job_assign(S, i, j, t, pot, sub, SDMD_EV_HB);
+    job_assign(S, c, j, t, pot, sub, SDMD_EV_HB);
 }
 
 // HBNeighborTime (src/TimePrediction.c:486-579)
-__device__ void hbnb_time(const DSys &S, int i, Blk &B, int *bad) {
+__device__ void hbnb_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     int flag = 0;
     for (int n = 1; n <= S.nb_status[i]; n++) {
         int j = S.nb_partner[4 * i + n - 1];
         if (flag == 0) S.nb_pnum[i] = n;
         if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HBNEIGHBOR && S.ev_pcounter[j] == S.ev_counter[i] &&
-            dup_assign(S, i, j, S.ev_time[j], SDMD_EV_HBNEIGHBOR)) {
+            dup_assign(S, c, j, S.ev_time[j], SDMD_EV_HBNEIGHBOR)) {
             S.nb_pnum[i] = n; flag = 1; continue;
         }
         Kin kk; pair_kin(S, i, j, kk);
@@ -276,12 +318,12 @@ __device__ void hbnb_time(const DSys &S, int i, Blk &B, int *bad) {
         }
         double t = root(kk, st, d2);
         if (t < 0) t = INFINIT;
-        if (job_assign(S, i, j, t, pot, sub, SDMD_EV_HBNEIGHBOR)) { S.nb_pnum[i] = n; flag = 1; }
+        if (job_assign(S, c, j, t, pot, sub, SDMD_EV_HBNEIGHBOR)) { S.nb_pnum[i] = n; flag = 1; }
     }
 }
 
 // WallTime, smooth walls (src/TimePrediction.c:635-737)
-__device__ void wall_time(const DSys &S, int i, Blk &B, int *bad) {
+__device__ void wall_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     double p[3] = {S.x[i], S.y[i], S.z[i]}, v[3] = {S.vx[i], S.vy[i], S.vz[i]};
     if (S.wall == SDMD_WALL_PARALLEL) { p[0] = p[2] = 0; v[0] = v[2] = 0; }
     else if (S.wall == SDMD_WALL_CYLINDER) { p[0] = 0; v[0] = 0; }
@@ -308,18 +350,21 @@ __device__ void wall_time(const DSys &S, int i, Blk &B, int *bad) {
     }
     double t = root(k, st, d2);
     if (t < 0) t = INFINIT;
-    job_assign(S, i, 0, t, pot, sub, SDMD_EV_WALL);
+    job_assign(S, c, 0, t, pot, sub, SDMD_EV_WALL);
 }
 
 // ---- Predict for one atom (ResetTarget already applied) ---------------------
 struct Shm {
     int32_t *nbj, *cnt;
     Slots L;
+    double *face;    // 3 PCC face times
 };
 
-__device__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, sdmd_rng &rng) {
+__device__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, DScal &C) {
     const int tid = threadIdx.x, T = blockDim.x;
     int bad = 0;
+    Cur c;
+    if (tid == 0) cur_load(S, i, c);
     double cut = S.cutoff * 0.90; cut *= cut;
     // BondTime
     int b0 = S.bond_off[i], nb = S.bond_off[i + 1] - b0;
@@ -330,16 +375,17 @@ __device__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, sdmd_rng &rng
     }
     for (int k = tid; k < nb; k += T) eval_bond(S, i, b0 + k, M.L, k, &bad);
     __syncthreads();
-    if (tid == 0) resolve(S, i, M.L, nb, SDMD_EV_BOND, B);
+    if (tid == 0) resolve(S, c, M.L, nb, SDMD_EV_BOND, B);
     // CollisionTime over the gathered 27-cell neighbourhood
     gather(S, i, M.nbj, M.cnt, B);
     int nn = B.nnb;
     for (int k = tid; k < nn; k += T) eval_collision(S, i, M.nbj[k], cut, M.L, k, &bad);
+    if (tid < 3) M.face[tid] = pcc_face(S, i, tid);
     __syncthreads();
     if (tid == 0) {
-        resolve(S, i, M.L, nn, SDMD_EV_COLLISION, B);
-        pcc_time(S, i);
-        thermostat_time(S, i, rng, B);
+        resolve(S, c, M.L, nn, SDMD_EV_COLLISION, B);
+        pcc_time(S, c, M.face);
+        thermostat_time(S, c, C, B);
         // HBTime prologue: one-shot HBSkip suppression (src/TimePrediction.c:309-327)
         int mode;
         if (S.hb_itype[i] == SDMD_HB_SKIP) mode = 0;
@@ -350,17 +396,18 @@ __device__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, sdmd_rng &rng
         }
         S.hb_itype[i] = SDMD_HB_NOEVENT;
         B.hbmode = mode;
-        if (mode == 1) hb_bonded(S, i, B, &bad);
+        if (mode == 1) hb_bonded(S, i, c, B, &bad);
     }
     __syncthreads();
     if (B.hbmode == 2) {
         for (int k = tid; k < nn; k += T) eval_hb_scan(S, i, M.nbj[k], cut, M.L, k, &bad);
         __syncthreads();
-        if (tid == 0) resolve(S, i, M.L, nn, SDMD_EV_HB, B);
+        if (tid == 0) resolve(S, c, M.L, nn, SDMD_EV_HB, B);
     }
     if (tid == 0) {
-        hbnb_time(S, i, B, &bad);
-        if (S.wall) wall_time(S, i, B, &bad);
+        hbnb_time(S, i, c, B, &bad);
+        if (S.wall) wall_time(S, i, c, B, &bad);
+        cur_store(S, i, c);
     }
     if (bad) set_err(B, SDMD_EHBMAP, i);
     __syncthreads();
@@ -369,7 +416,7 @@ __device__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, sdmd_rng &rng
 // ---- events (thread 0) -------------------------------------------------------
 __device__ void imaged(const DSys &S, int t, int a, double p[3]) {
     const int ct[3] = {S.cx[t], S.cy[t], S.cz[t]}, ca[3] = {S.cx[a], S.cy[a], S.cz[a]};
-    p[0] = S.x[a]; p[1] = S.y[a]; p[2] = S.z[a];
+    p[0] = lzx(S, S.x, S.vx, a); p[1] = lzx(S, S.y, S.vy, a); p[2] = lzx(S, S.z, S.vz, a);
     for (int d = 0; d < 3; d++) {
         if (ct[d] != ca[d]) {
             if (ct[d] == 0 && ca[d] == S.cn[d] - 1) p[d] -= S.box[d];
@@ -516,12 +563,11 @@ __device__ void hb_event(const DSys &S, DScal &C, int i, int j, int ni, int nj, 
 }
 
 // ThermostatEvent, Andersen (src/Events.c:396-420)
-__device__ void thermostat_event(const DSys &S, int t, sdmd_rng &rng, Blk &B) {
+__device__ void thermostat_event(const DSys &S, int t, DScal &C, Blk &B) {
     double sp[3];
     for (int d = 0; d < 3; d++) {
-        int bad = 0, tries = 0;
-        do { sp[d] = mb_draw(rng, 0, S.temperature / S.mass[t], &bad); } while (sp[d] == 0 && !bad && ++tries < 64);
-        if (bad || sp[d] == 0) { set_err(B, SDMD_ETIMEOUT, t); return; }
+        sp[d] = take_sample(S, C, B) * sqrt(S.temperature / S.mass[t]) + 0;
+        if (sp[d] == 0) { set_err(B, SDMD_ETIMEOUT, t); return; }   // a Box-Muller value is never exactly 0
     }
     S.vx[t] = sp[0]; S.vy[t] = sp[1]; S.vz[t] = sp[2];
 }
@@ -592,7 +638,7 @@ __device__ void wall_event(const DSys &S, int t, Blk &B) {
 }
 
 // DoEvent (src/Events.c:25-114)
-__device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, sdmd_rng &rng) {
+__device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B) {
     int bad = 0;
     switch (S.ev_type[t]) {
         case SDMD_EV_COLLISION: interaction_event(S, t, p, 0, 0, B, &bad); C.c.collision++; break;
@@ -604,7 +650,7 @@ __device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, sdmd_rng
             if (!B.err) hb_event(S, C, t, p, ni, nj, B);
             C.c.hb++;
         } break;
-        case SDMD_EV_THERMOSTAT: thermostat_event(S, t, rng, B); C.c.thermostat++; break;
+        case SDMD_EV_THERMOSTAT: thermostat_event(S, t, C, B); C.c.thermostat++; break;
         case SDMD_EV_PCC: pcc_event(S, t, B); C.c.pcc++; break;
         case SDMD_EV_WALL: wall_event(S, t, B); C.c.wall++; break;
         default: set_err(B, SDMD_EEVENTTYPE, t); break;
@@ -621,11 +667,11 @@ __device__ void cbt_update(const DSys &S, int a) {   // UpdateCBTRun, src/CBT.c:
     for (f = leaf[a] / 2; f > 0; f /= 2) {
         if (node[f] != a) break;
         int l = node[2 * f], r = node[2 * f + 1];
-        node[f] = tm[l] < tm[r] ? l : r;
+        node[f] = tkey(tm[l]) < tkey(tm[r]) ? l : r;
     }
     for (; f > 0; f /= 2) {
         int old = node[f], l = node[2 * f], r = node[2 * f + 1];
-        node[f] = tm[l] < tm[r] ? l : r;
+        node[f] = tkey(tm[l]) < tkey(tm[r]) ? l : r;
         if (node[f] == old) return;
     }
 }
@@ -643,19 +689,113 @@ __device__ void cbt_build(const DSys &S) {            // CreateCBT, src/CBT.c:16
 }
 
 // ---- kernels ---------------------------------------------------------------------
+__host__ __device__ inline size_t fp64_smem_bytes_dev(int nbcap) {
+    int cap = nbcap > 64 ? nbcap : 64;
+    return al16((size_t)(cap * 3 + 4) * sizeof(double) + (size_t)(2 * cap + nbcap + 32) * sizeof(int32_t));
+}
+
 __device__ inline void carve(Shm &M, int nbcap) {
     extern __shared__ __align__(16) unsigned char smem[];
     int cap = nbcap > 64 ? nbcap : 64;
     double *d = reinterpret_cast<double *>(smem);
     M.L.t = d; M.L.tdup = d + cap; M.L.pot = d + 2 * cap;
-    int32_t *ip = reinterpret_cast<int32_t *>(d + 3 * cap);
+    M.face = d + 3 * cap;
+    int32_t *ip = reinterpret_cast<int32_t *>(d + 3 * cap + 4);
     M.L.j = ip; M.L.info = ip + cap; M.nbj = ip + 2 * cap; M.cnt = ip + 2 * cap + nbcap;
 }
 
-size_t fp64_smem_bytes(int nbcap) {
-    int cap = nbcap > 64 ? nbcap : 64;
-    return (size_t)cap * 3 * sizeof(double) + (size_t)(2 * cap + nbcap + 32) * sizeof(int32_t);
+// ---- whole-system staging in shared memory ------------------------------------
+// A small system's per-atom arrays, topology, cell list and event tree are copied
+// into shared memory at kernel start; the block's DSys pointers are redirected to
+// the copies (generic addressing makes every device function work unchanged),
+// and the mutable arrays are written back at the end.  Shared-memory latency is
+// ~30 cycles against ~300-600 for L2.
+struct Stager {
+    unsigned char *p;
+    bool copy;
+    template <class T> __device__ T *take(const T *src, size_t count) {
+        size_t a = (reinterpret_cast<size_t>(p) + 15) & ~size_t(15);
+        T *dst = reinterpret_cast<T *>(a);
+        p = reinterpret_cast<unsigned char *>(dst + count);
+        if (copy && src)
+            for (size_t k = threadIdx.x; k < count; k += blockDim.x) dst[k] = src[k];
+        return dst;
+    }
+};
+
+size_t staged_state_bytes(int n, int ncell, int nb, int nc, int ncs, int nconn) {
+    size_t N1 = (size_t)n + 1, t = 0;
+    t += al16(N1 * 8) * 10;                                  // mass, x..vz, ev_time, ev_potential, tloc
+    t += al16(N1 * 4) * 17;                                  // 6 static + 11 dynamic int arrays
+    t += al16(4 * N1 * 4);                                   // nb_partner
+    t += al16(N1 * 8) * 2;                                   // ev_counter, ev_pcounter
+    t += al16((N1 + 1) * 4) * 3;                             // bond/con/conn offsets
+    t += al16((size_t)nb * 4) + 2 * al16((size_t)nb * 8);
+    t += 3 * al16((size_t)nc * 4) + 2 * al16((size_t)nc * 8) + 3 * al16((size_t)ncs * 8);
+    t += 2 * al16((size_t)nconn * 4);
+    t += al16((N1 + (size_t)ncell) * 4);                     // cell list
+    t += al16((2 * N1 + 2) * 4) + al16((N1 + 1) * 4);        // tree
+    return t + 64;
 }
+
+// stage (copy == true) or locate (copy == false) the state after the slot buffers
+__device__ void stage_state(DSys &S, const DSys &G, unsigned char *base, bool copy) {
+    Stager st{base, copy};
+    size_t N1 = (size_t)G.n + 1;
+    DSys L = G;
+    L.mass = st.take(G.mass, N1);
+    L.x = st.take(G.x, N1); L.y = st.take(G.y, N1); L.z = st.take(G.z, N1);
+    L.vx = st.take(G.vx, N1); L.vy = st.take(G.vy, N1); L.vz = st.take(G.vz, N1);
+    L.ev_time = st.take(G.ev_time, N1); L.ev_potential = st.take(G.ev_potential, N1);
+    if (G.lazy) L.tloc = st.take(G.tloc, N1);
+    L.protein = st.take(G.protein, N1); L.aanum = st.take(G.aanum, N1); L.aatype = st.take(G.aatype, N1);
+    L.hb_neighbor = st.take(G.hb_neighbor, N1); L.hb_role = st.take(G.hb_role, N1);
+    L.name_code = st.take(G.name_code, N1);
+    L.cx = st.take(G.cx, N1); L.cy = st.take(G.cy, N1); L.cz = st.take(G.cz, N1);
+    L.type = st.take(G.type, N1); L.hb_bond = st.take(G.hb_bond, N1); L.hb_itype = st.take(G.hb_itype, N1);
+    L.nb_status = st.take(G.nb_status, N1); L.nb_pnum = st.take(G.nb_pnum, N1);
+    L.ev_partner = st.take(G.ev_partner, N1); L.ev_type = st.take(G.ev_type, N1); L.ev_sub = st.take(G.ev_sub, N1);
+    L.nb_partner = st.take(G.nb_partner, 4 * N1);
+    L.ev_counter = st.take(G.ev_counter, N1); L.ev_pcounter = st.take(G.ev_pcounter, N1);
+    L.bond_off = st.take(G.bond_off, N1 + 1); L.con_off = st.take(G.con_off, N1 + 1);
+    L.conn_off = st.take(G.conn_off, N1 + 1);
+    L.bond_j = st.take(G.bond_j, (size_t)G.n_bonds);
+    L.bond_dmin = st.take(G.bond_dmin, (size_t)G.n_bonds); L.bond_dmax = st.take(G.bond_dmax, (size_t)G.n_bonds);
+    L.con_j = st.take(G.con_j, (size_t)G.n_cons); L.con_step_off = st.take(G.con_step_off, (size_t)G.n_cons);
+    L.con_step_n = st.take(G.con_step_n, (size_t)G.n_cons);
+    L.con_dmin = st.take(G.con_dmin, (size_t)G.n_cons); L.con_dmax = st.take(G.con_dmax, (size_t)G.n_cons);
+    L.con_step_d = st.take(G.con_step_d, (size_t)G.n_con_steps);
+    L.con_step_e = st.take(G.con_step_e, (size_t)G.n_con_steps);
+    L.con_step_acc = st.take(G.con_step_acc, (size_t)G.n_con_steps);
+    L.conn_j = st.take(G.conn_j, (size_t)G.n_conn); L.conn_bits = st.take(G.conn_bits, (size_t)G.n_conn);
+    L.cell_list = st.take(G.cell_list, N1 + (size_t)G.ncell);
+    L.cbt_node = st.take(G.cbt_node, 2 * N1 + 2); L.cbt_leaf = st.take(G.cbt_leaf, N1 + 1);
+    __syncthreads();
+    if (threadIdx.x == 0) S = L;
+    __syncthreads();
+}
+
+// write the mutable staged arrays back to global memory
+__device__ void unstage_state(const DSys &S, const DSys &G) {
+    size_t N1 = (size_t)G.n + 1;
+    for (size_t k = threadIdx.x; k < N1; k += blockDim.x) {
+        G.x[k] = S.x[k]; G.y[k] = S.y[k]; G.z[k] = S.z[k];
+        G.vx[k] = S.vx[k]; G.vy[k] = S.vy[k]; G.vz[k] = S.vz[k];
+        G.ev_time[k] = S.ev_time[k]; G.ev_potential[k] = S.ev_potential[k];
+        if (G.lazy) G.tloc[k] = S.tloc[k];
+        G.cx[k] = S.cx[k]; G.cy[k] = S.cy[k]; G.cz[k] = S.cz[k];
+        G.type[k] = S.type[k]; G.hb_bond[k] = S.hb_bond[k]; G.hb_itype[k] = S.hb_itype[k];
+        G.nb_status[k] = S.nb_status[k]; G.nb_pnum[k] = S.nb_pnum[k];
+        G.ev_partner[k] = S.ev_partner[k]; G.ev_type[k] = S.ev_type[k]; G.ev_sub[k] = S.ev_sub[k];
+        G.ev_counter[k] = S.ev_counter[k]; G.ev_pcounter[k] = S.ev_pcounter[k];
+        for (int q = 0; q < 4; q++) G.nb_partner[4 * k + q] = S.nb_partner[4 * k + q];
+    }
+    for (size_t k = threadIdx.x; k < N1 + (size_t)G.ncell; k += blockDim.x) G.cell_list[k] = S.cell_list[k];
+    for (size_t k = threadIdx.x; k < 2 * N1 + 2; k += blockDim.x) G.cbt_node[k] = S.cbt_node[k];
+    for (size_t k = threadIdx.x; k < N1 + 1; k += blockDim.x) G.cbt_leaf[k] = S.cbt_leaf[k];
+}
+
+size_t fp64_smem_bytes(int nbcap) { return fp64_smem_bytes_dev(nbcap); }
 
 // Full-rebuild sweep: ResetTarget + Predict over 1..N (src/SGThread.c:47-52), then
 // CreateCBT.  With full == 0 only the tree is built (continue mode).
@@ -663,30 +803,36 @@ __global__ void sweep_kernel_fp64(const DSys *systems, int full) {
     __shared__ DSys S;
     if (threadIdx.x == 0) S = systems[blockIdx.x];
     __shared__ Blk B;
-    __shared__ sdmd_rng rng;
-    if (threadIdx.x == 0) { B.err = 0; B.warn = 0; rng = S.sc->rng; }
+    __shared__ DScal C;
+    if (threadIdx.x == 0) { B.err = 0; B.warn = 0; C = *S.sc; S.now = C.time; }
     __syncthreads();
+    if (C.err) return;
     Shm M; carve(M, S.nbcap);
     if (full) {
+        if (S.thermostat && C.smp_avail < S.n) {   // one sample per predicted atom
+            if (threadIdx.x == 0) { S.sc->err = SDMD_ECAPACITY; S.sc->err_atom = 0; }
+            return;
+        }
         for (int i = 1 + threadIdx.x; i <= S.n; i += blockDim.x) {
             S.ev_type[i] = SDMD_EV_INVALID; S.ev_time[i] = INFINIT; S.ev_partner[i] = INVALID;
         }
         __syncthreads();
-        for (int i = 1; i <= S.n && B.err == 0; i++) predict_atom(S, i, M, B, rng);
+        for (int i = 1; i <= S.n && B.err == 0; i++) predict_atom(S, i, M, B, C);
     }
     if (threadIdx.x == 0) {
         if (B.err == 0) cbt_build(S);
-        S.sc->rng = rng;
-        S.sc->c.warnings += B.warn;
-        S.sc->cbt_built = 1;
-        if (B.err) { S.sc->err = B.err; S.sc->err_atom = B.err_atom; S.sc->err_event = S.sc->c.frame; }
+        C.c.warnings += B.warn;
+        C.cbt_built = 1;
+        if (B.err) { C.err = B.err; C.err_atom = B.err_atom; C.err_event = C.c.frame; }
+        *S.sc = C;
     }
 }
 
 // The event loop (src/SGThread.c:75-151)
-__global__ void loop_kernel_fp64(const DSys *systems, int64_t max_events, double t_end_override) {
+__global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int staged) {
     __shared__ DSys S;
-    if (threadIdx.x == 0) S = systems[blockIdx.x];
+    __shared__ DSys G;   // the global-memory view (write-back target when staged)
+    if (threadIdx.x == 0) { S = systems[blockIdx.x]; G = S; }
     const int tid = threadIdx.x, T = blockDim.x;
     __shared__ Blk B;
     __shared__ DScal C;
@@ -700,18 +846,30 @@ __global__ void loop_kernel_fp64(const DSys *systems, int64_t max_events, double
     __syncthreads();
     if (C.err) return;
     Shm M; carve(M, S.nbcap);
+    if (staged) {
+        extern __shared__ __align__(16) unsigned char smem_all[];
+        stage_state(S, G, smem_all + fp64_smem_bytes_dev(S.nbcap), true);
+    }
     const double t_end = t_end_override > 0 ? t_end_override : S.t_end;
-    const int64_t stop_at = C.c.frame + max_events;
+    const int64_t stop_at = C.target_frame;
     // denied pops do not advance `frame`; bound the pops so that no input can spin forever
-    const int64_t pop_limit = C.pops + 64 * max_events + 1000000;
+    const int64_t pop_limit = C.pops + 64 * (stop_at - C.c.frame) + 1000000;
     for (;;) {
         if (tid == 0) {
             if (C.pops >= pop_limit) set_err(B, SDMD_ETIMEOUT, 0);
             int go = (C.time <= t_end) && (C.c.frame < stop_at) && B.err == 0;
+            // a pop consumes at most 5 samples (2 predictions + a thermostat event)
+            if (go && S.thermostat && C.smp_avail - C.smp_used < 5) { C.paused = 1; go = 0; }
             sh_go = go;
             if (go) {
                 int t = S.cbt_node[1];
-                sh_t = t; sh_dt = S.ev_time[t];
+                sh_t = t;
+                if (S.lazy) {   // absolute event times: the clock jumps to the event
+                    sh_dt = S.ev_time[t] - C.time;
+                    S.now = S.ev_time[t];
+                } else {
+                    sh_dt = S.ev_time[t];
+                }
                 rec_partner = S.ev_partner[t]; rec_type = S.ev_type[t]; rec_sub = S.ev_sub[t];
                 sh_p = rec_partner > 0 ? rec_partner : 0;
             }
@@ -719,21 +877,24 @@ __global__ void loop_kernel_fp64(const DSys *systems, int64_t max_events, double
         __syncthreads();
         if (!sh_go) break;
         const double dt = sh_dt;
-        for (int i = 1 + tid; i <= S.n; i += T) {      // UpdateData + TimeForward
-            S.x[i] += S.vx[i] * dt;
-            S.y[i] += S.vy[i] * dt;
-            S.z[i] += S.vz[i] * dt;
-            S.ev_time[i] -= dt;
+        if (!S.lazy) {
+            for (int i = 1 + tid; i <= S.n; i += T) {      // UpdateData + TimeForward
+                S.x[i] += S.vx[i] * dt;
+                S.y[i] += S.vy[i] * dt;
+                S.z[i] += S.vz[i] * dt;
+                S.ev_time[i] -= dt;
+            }
+            __syncthreads();
         }
-        __syncthreads();
         const int t = sh_t, p = sh_p;
         if (tid == 0) {
-            C.time += dt;
+            if (S.lazy) { C.time = S.now; sync_atom(S, t); sync_atom(S, p); }
+            else C.time += dt;
             int hazard = p > 0 && S.ev_pcounter[t] < S.ev_counter[p];   // HazardCheck
             sh_exec = !hazard;
             if (!hazard) {
                 C.c.frame++;
-                do_event(S, C, t, p, B, C.rng);
+                do_event(S, C, t, p, B);
                 S.ev_counter[t]++;
                 if (p) S.ev_counter[p]++;
             } else {
@@ -745,8 +906,8 @@ __global__ void loop_kernel_fp64(const DSys *systems, int64_t max_events, double
         }
         __syncthreads();
         if (B.err) break;
-        predict_atom(S, t, M, B, C.rng);
-        if (sh_exec && p && B.err == 0) predict_atom(S, p, M, B, C.rng);
+        predict_atom(S, t, M, B, C);
+        if (sh_exec && p && B.err == 0) predict_atom(S, p, M, B, C);
         if (tid == 0) {
             cbt_update(S, t);
             if (sh_exec && p) cbt_update(S, p);
@@ -766,11 +927,27 @@ __global__ void loop_kernel_fp64(const DSys *systems, int64_t max_events, double
         }
         __syncthreads();
     }
+    if (staged) {
+        __syncthreads();
+        unstage_state(S, G);
+    }
     if (tid == 0) {
         C.c.warnings += B.warn;
         if (B.err) { C.err = B.err; C.err_atom = B.err_atom; C.err_event = C.c.frame; }
-        *S.sc = C;
+        *G.sc = C;
     }
 }
 
+}  // namespace sdmd
+
+namespace sdmd {
+// lazy mode entry: positions are valid now, event times become absolute
+__global__ void lazy_enter_kernel(const DSys *systems) {
+    const DSys &S = systems[blockIdx.x];
+    double T = S.sc->time;
+    for (int i = 1 + threadIdx.x; i <= S.n; i += blockDim.x) {
+        S.tloc[i] = T;
+        S.ev_time[i] = S.ev_time[i] + T;
+    }
+}
 }  // namespace sdmd
