@@ -93,6 +93,14 @@ static void dump_dynamic(void) {
     sec_i("HBnumformed", HBnumformed);
     sec_i("alphaHBformed", alphaHBformed);
     sec_q("warningsum", warningsum);
+    /* the reference's own observables (src/ToolFunctions.c:626-752); CalPotenE
+       may count warnings, which are restored so the dump does not perturb state */
+    {
+        long saved = warningsum;
+        sec_d("kinE", CalKinetE());
+        sec_d("potE", CalPotenE());
+        warningsum = saved;
+    }
     /* HB / NEIGHBOR bits of the dense connection map, as a sparse (i, j, bits) list,
        so the sparse HB state can be checked against them */
     {

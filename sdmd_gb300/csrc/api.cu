@@ -335,7 +335,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         st_max = std::max(st_max, staged_state_bytes(s.n_atoms, h->meta[k].ncell, s.n_bonds, s.n_cons,
                                                      s.n_con_steps, s.n_conn));
     }
-    h->staged = (h->smem + st_max <= 200 * 1024) ? 1 : 0;
+    h->staged = (h->smem + st_max <= 192 * 1024) ? 1 : 0;
     h->smem_loop = h->staged ? h->smem + st_max : h->smem;
     h->threads = h->opts.threads_per_system > 0 ? h->opts.threads_per_system : 128;
     if (h->threads < 32 || h->threads > 1024 || (h->threads & 31)) { delete h; return SDMD_EINVAL; }
@@ -363,10 +363,14 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         cudaMemcpyAsync(h->hs[k].sc, &sc[k], sizeof(DScal), cudaMemcpyHostToDevice, h->stream);
     }
     cudaMemcpyAsync(h->ds, h->hs.data(), sizeof(DSys) * n_systems, cudaMemcpyHostToDevice, h->stream);
-    if (h->smem > 48 * 1024)
-        cudaFuncSetAttribute(sweep_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem);
-    if (h->smem_loop > 48 * 1024)
-        cudaFuncSetAttribute(loop_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)h->smem_loop);
+    // the dynamic shared-memory limit must cover dynamic + static usage: always set it
+    if ((r = cuda_fail(cudaFuncSetAttribute(sweep_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)h->smem))) ||
+        (r = cuda_fail(cudaFuncSetAttribute(loop_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)h->smem_loop)))) {
+        sdmd_gpu_destroy(h);
+        return r;
+    }
     if (h->opts.advance == SDMD_ADVANCE_LAZY) lazy_enter_kernel<<<n_systems, 128, 0, h->stream>>>(h->ds);
     if ((r = cuda_fail(cudaStreamSynchronize(h->stream)))) { sdmd_gpu_destroy(h); return r; }
     *out = h;

@@ -120,3 +120,27 @@ def test_log_close_to_libm():
     ref = np.array([math.log(float(v)) for v in s])
     ulp = np.abs(mine - ref) / np.spacing(np.abs(ref))
     assert ulp.max() <= 1.0 and np.mean(mine != ref) < 0.005
+
+
+def test_oracle_nve_energy_conserved_between_hb_events(golden):
+    """The exact restatement conserves KE + PE at every non-HB event (the same
+    check the GPU modes pass in test_gpu_lazy.py)."""
+    from tests.test_gpu_lazy import assert_conserved_between_hb_events, energy_trace
+    d = golden("ala10_nve")
+    s = from_fixture(d, "pre")
+    O.predict_all(s)
+    loop = O.Loop(s)
+    e0, hb0 = O.kinetic_energy(s) + O.potential_energy(s), s.counters["hb"] + s.counters["hbneighbor"]
+    tr = energy_trace(lambda: loop.run(1000), s, 40, O.kinetic_energy, O.potential_energy)
+    assert_conserved_between_hb_events(tr, e0, hb0)
+
+
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt_long"])
+def test_energy_functions_match_reference(golden, case):
+    """oracle_kinetic_energy / oracle_potential_energy equal the reference's own
+    CalKinetE / CalPotenE (dumped by the harness) at every checkpoint."""
+    d = golden(case)
+    for st in ["pre"] + [f"ckpt{c}" for c in d["meta/ckpts"]] + ["final"]:
+        s = from_fixture(d, "pre", dynamic_stage=None if st == "pre" else st)
+        assert O.kinetic_energy(s) == d[f"{st}/kinE"][0]
+        assert O.potential_energy(s) == d[f"{st}/potE"][0]
