@@ -130,8 +130,10 @@ def test_oracle_nve_energy_conserved_between_hb_events(golden):
     s = from_fixture(d, "pre")
     O.predict_all(s)
     loop = O.Loop(s)
-    e0, hb0 = O.kinetic_energy(s) + O.potential_energy(s), s.counters["hb"] + s.counters["hbneighbor"]
-    tr = energy_trace(lambda: loop.run(1000), s, 40, O.kinetic_energy, O.potential_energy)
+    from tests.energy import total_energy
+    e0 = total_energy(s, O.kinetic_energy, O.potential_energy)
+    hb0 = s.counters["hb"] + s.counters["hbneighbor"]
+    tr = energy_trace(lambda: loop.run(250), s, 120, O.kinetic_energy, O.potential_energy)
     assert_conserved_between_hb_events(tr, e0, hb0)
 
 
