@@ -28,11 +28,15 @@ def constraint_energy(s):
             sh = np.where((ci != cj) & (ci == 0) & (cj == cn - 1), -box,
                           np.where((ci != cj) & (ci == cn - 1) & (cj == 0), box, 0.0))
             r = np.array([a["x"][i], a["y"][i], a["z"][i]]) - (np.array([a["x"][j], a["y"][j], a["z"][j]]) + sh)
+            v = np.array([a["vx"][i] - a["vx"][j], a["vy"][i] - a["vy"][j], a["vz"][i] - a["vz"][j]])
             r2 = float(r @ r)
+            # a pair on a step boundary belongs to the shell it moves into: the
+            # reference's FindPair tolerance is +ZERO approaching, -ZERO leaving
+            tol = 1e-8 if float(r @ v) < 0 else -1e-8
             o, n = int(a["con_step_off"][q]), int(a["con_step_n"][q])
             d, e = a["con_step_d"][o:o + n], a["con_step_e"][o:o + n]
             for k in range(n):
-                if r2 < d[k]:
+                if r2 < d[k] + tol:
                     tot += float(np.sum(e[k:]))
                     break
     return tot
