@@ -217,6 +217,34 @@ int  sdmd_gpu_last_ms(sdmd_gpu *h, double *prepare_ms, double *run_ms);
 
 int  sdmd_gpu_last_error(sdmd_gpu *h, sdmd_error_info *info);
 
+/* ---- allocation-free re-sweep ------------------------------------------------
+ * No counterpart in the reference (its Prepare() allocates nothing on a GPU).
+ *
+ * Same contract and bit-identical results as sdmd_gpu_prepare, but the call
+ * allocates nothing: no cudaMalloc/cudaFree, no host heap.  The scratch it needs
+ * (the descriptor table its launches read, the thermostat sample buffers and an
+ * error record) lives in one static device array of SDMD_NOALLOC_SCRATCH_BYTES
+ * compiled into the library.  It is meant for callers that must not allocate
+ * between create and destroy -- a replica-exchange or annealing driver that
+ * re-sweeps after every temperature change while another framework's caching
+ * allocator holds the rest of device memory, or a host loop that must not take
+ * the allocator's locks or its implicit device synchronisation.
+ *
+ * Limits and rules:
+ *   - the batch must fit: 256-aligned n_systems descriptors plus, with
+ *     full_predict and per system with a thermostat, about 28 bytes per atom.
+ *     Larger batches return SDMD_ECAPACITY with a message on stderr and change
+ *     nothing; use sdmd_gpu_prepare for them.
+ *   - the first call on a device looks up the array's address
+ *     (cudaGetSymbolAddress) with the handle's device current; make that first
+ *     call before any stream capture that could contain it.
+ *   - the array is shared by every handle on a device and keeps its contents
+ *     between calls.  Nothing in it must start at zero (each call writes what it
+ *     reads), but calls that overlap in time race: serialise them per device.
+ */
+#define SDMD_NOALLOC_SCRATCH_BYTES (4u << 20)
+int  sdmd_gpu_prepare_noalloc(sdmd_gpu *h, int32_t full_predict);
+
 /* glibc-compatible rand() stream helpers (host side). */
 void sdmd_rng_seed(sdmd_rng *r, uint32_t seed);
 int32_t sdmd_rng_next(sdmd_rng *r);

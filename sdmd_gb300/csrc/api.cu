@@ -548,3 +548,113 @@ extern "C" int32_t sdmd_rng_next(sdmd_rng *r) {
 extern "C" void sdmd_rng_skip(sdmd_rng *r, int64_t n) {
     for (int64_t k = 0; k < n; k++) sdmd_rng_next(r);
 }
+
+// ---- allocation-free full-rebuild sweep -------------------------------------------
+// sdmd_gpu_prepare_noalloc runs the same kernels as sdmd_gpu_prepare, but the
+// scratch they need -- the descriptor table the launches read and each system's
+// thermostat sample buffers -- lives in one file-scope device array instead of the
+// handle's arena, and the host side uses no heap.  Layout of the array:
+//   [descriptor table: n_systems DSys, 256-aligned]
+//   [first-error record, 256-aligned]
+//   per system with a thermostat: [smp: cap doubles][smp_raw: 3 cap int32][smp_cum: cap int64],
+//   each 256-aligned, cap = atoms + 8 (one sample per predicted atom plus slack).
+// Every element a call reads is written earlier in the same call, so nothing in
+// the array needs to start at zero and stale contents of an earlier call are harmless.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[SDMD_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+unsigned char *g_noalloc_addr[kNoallocMaxDevices];   // resolved once per device
+
+__host__ __device__ inline size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+__host__ __device__ inline int64_t noalloc_cap(int32_t n, int32_t thermostat) { return thermostat ? (int64_t)n + 8 : 0; }
+__host__ __device__ inline size_t noalloc_sys_bytes(int64_t cap) {
+    return cap ? al256((size_t)cap * 8) + al256((size_t)cap * 12) + al256((size_t)cap * 8) : 0;
+}
+__host__ __device__ inline size_t noalloc_head_bytes(int n_systems) {
+    return al256(sizeof(DSys) * (size_t)n_systems) + al256(sizeof(sdmd_error_info));
+}
+
+// copy the handle's descriptors into the table, pointing the sample buffers into the array
+__global__ void noalloc_table_kernel(const DSys *src, int n_systems, unsigned char *base) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    DSys *table = reinterpret_cast<DSys *>(base);
+    size_t off = noalloc_head_bytes(n_systems);
+    for (int k = 0; k < n_systems; k++) {
+        DSys s = src[k];
+        int64_t cap = noalloc_cap(s.n, s.thermostat);
+        s.smp_cap = (int32_t)cap;
+        if (cap) {
+            s.smp = reinterpret_cast<double *>(base + off);
+            s.smp_raw = reinterpret_cast<int32_t *>(base + off + al256((size_t)cap * 8));
+            s.smp_cum = reinterpret_cast<int64_t *>(base + off + al256((size_t)cap * 8) + al256((size_t)cap * 12));
+        }
+        off += noalloc_sys_bytes(cap);
+        table[k] = s;
+    }
+}
+
+// the first system with a latched error, or code 0
+__global__ void noalloc_first_error_kernel(const DSys *table, int n_systems, sdmd_error_info *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    sdmd_error_info e{0, 0, 0, 0};
+    for (int k = 0; k < n_systems; k++) {
+        const DScal &c = *table[k].sc;
+        if (c.err) { e.code = c.err; e.system = k; e.atom = c.err_atom; e.event = c.err_event; break; }
+    }
+    *out = e;
+}
+}  // namespace
+
+extern "C" int sdmd_gpu_prepare_noalloc(sdmd_gpu *h, int32_t full_predict) {
+    if (!h) return SDMD_EINVAL;
+    const int dev = h->opts.device;
+    if (dev < 0 || dev >= kNoallocMaxDevices) return SDMD_EINVAL;
+    CK(cudaSetDevice(dev));
+    size_t need = noalloc_head_bytes(h->n_systems);
+    int32_t nmax = 0;
+    for (int k = 0; k < h->n_systems; k++) {
+        nmax = std::max(nmax, h->meta[k].n);
+        if (full_predict) need += noalloc_sys_bytes(noalloc_cap(h->meta[k].n, h->hs[k].thermostat));
+    }
+    if (need > (size_t)SDMD_NOALLOC_SCRATCH_BYTES) {
+        fprintf(stderr,
+                "sdmd_gpu_prepare_noalloc: this batch needs %zu bytes of static scratch, the limit is %zu "
+                "(SDMD_NOALLOC_SCRATCH_BYTES); use sdmd_gpu_prepare\n",
+                need, (size_t)SDMD_NOALLOC_SCRATCH_BYTES);
+        return SDMD_ECAPACITY;
+    }
+    if (!g_noalloc_addr[dev]) {   // first call on this device
+        void *p = nullptr;
+        CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    unsigned char *base = g_noalloc_addr[dev];
+    DSys *table = reinterpret_cast<DSys *>(base);
+    sdmd_error_info *first = reinterpret_cast<sdmd_error_info *>(base + al256(sizeof(DSys) * (size_t)h->n_systems));
+
+    CK(cudaEventRecord(h->e0, h->stream));
+    noalloc_table_kernel<<<1, 1, 0, h->stream>>>(h->ds, h->n_systems, base);
+    if (full_predict) {
+        const int64_t want = (int64_t)nmax + 8;
+        samples_walk_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(table, h->n_systems, want);
+        dim3 grid((unsigned)std::max<int64_t>(1, std::min<int64_t>((want + 255) / 256, 1024)), (unsigned)h->n_systems);
+        samples_values_kernel<<<grid, 256, 0, h->stream>>>(table, want);
+    }
+    sweep_kernel_fp64<<<h->n_systems, h->threads, h->smem, h->stream>>>(table, full_predict ? 1 : 0);
+    if (full_predict) samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(table, h->n_systems);
+    noalloc_first_error_kernel<<<1, 1, 0, h->stream>>>(table, h->n_systems, first);
+    CK(cudaGetLastError());
+    sdmd_error_info e;
+    CK(cudaMemcpyAsync(&e, first, sizeof(e), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaEventRecord(h->e1, h->stream));
+    CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->prep_ms = ms;
+    if (e.code) {
+        h->err = e;
+        return e.code;
+    }
+    return SDMD_OK;
+}

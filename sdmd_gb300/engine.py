@@ -20,7 +20,8 @@ SCREEN_FP64, SCREEN_FP32 = 0, 1
 
 ABI_FUNCS = ["sdmd_gpu_abi_version", "sdmd_gpu_device_count", "sdmd_gpu_strerror", "sdmd_gpu_create",
              "sdmd_gpu_destroy", "sdmd_gpu_prepare", "sdmd_gpu_run", "sdmd_gpu_download", "sdmd_gpu_trace",
-             "sdmd_gpu_last_ms", "sdmd_gpu_last_error", "sdmd_rng_seed", "sdmd_rng_next", "sdmd_rng_skip"]
+             "sdmd_gpu_last_ms", "sdmd_gpu_last_error", "sdmd_rng_seed", "sdmd_rng_next", "sdmd_rng_skip",
+             "sdmd_gpu_prepare_noalloc"]
 
 _lib = None
 
@@ -50,6 +51,7 @@ def lib():
         L.sdmd_gpu_destroy.argtypes = [C.c_void_p]
         L.sdmd_gpu_destroy.restype = None
         L.sdmd_gpu_prepare.argtypes = [C.c_void_p, C.c_int32]
+        L.sdmd_gpu_prepare_noalloc.argtypes = [C.c_void_p, C.c_int32]
         L.sdmd_gpu_run.argtypes = [C.c_void_p, C.c_int64, C.c_double]
         L.sdmd_gpu_download.argtypes = [C.c_void_p, P(sdmd_system), C.c_int32]
         L.sdmd_gpu_trace.argtypes = [C.c_void_p, C.c_int32, P(sdmd_trace_rec), C.c_int32, P(C.c_int32)]
@@ -101,6 +103,10 @@ class Engine:
 
     def prepare(self, full=True):
         self._check(lib().sdmd_gpu_prepare(self.h, 1 if full else 0), "sdmd_gpu_prepare")
+
+    def prepare_noalloc(self, full=True):
+        """sdmd_gpu_prepare_noalloc: the same sweep with its scratch in the library's static array."""
+        self._check(lib().sdmd_gpu_prepare_noalloc(self.h, 1 if full else 0), "sdmd_gpu_prepare_noalloc")
 
     def run(self, max_events, t_end=0.0):
         self._check(lib().sdmd_gpu_run(self.h, int(max_events), float(t_end)), "sdmd_gpu_run")
