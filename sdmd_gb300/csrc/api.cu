@@ -5,6 +5,7 @@
 // pop trace.  Launches go to the handle's own stream and are timed with CUDA
 // events on that stream.  Nothing here falls back to the CPU: without a usable
 // device every entry point returns SDMD_ENODEV / SDMD_ECUDA.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -34,6 +35,8 @@ struct sdmd_gpu {
     size_t smem = 0, smem_loop = 0;
     int staged = 0;
     std::vector<int32_t> smp_cap_of;
+    void (*sweep_k)(const DSys *, int) = nullptr;            // plain FP64 or FP32-screened kernels
+    void (*loop_k)(const DSys *, double, int) = nullptr;
     double prep_ms = 0, run_ms = 0;
     sdmd_error_info err{};
 };
@@ -161,6 +164,48 @@ static int max_neighbourhood(const sdmd_system &s) {
     return best;
 }
 
+// ---- FP32 brackets for the screen ------------------------------------------------
+// [lo, hi]: the nearest floats below and above the double v (equal when v is a float)
+static void f32_bracket(double v, float *out) {
+    float f = (float)v;
+    out[0] = ((double)f > v) ? nextafterf(f, -INFINITY) : f;
+    out[1] = ((double)f < v) ? nextafterf(f, INFINITY) : f;
+}
+
+struct Screen32 {
+    std::vector<float> pair_thr, pair_step, con_thr, con_step, bond;
+};
+
+// brackets of every FP64 threshold the prediction compares against, computed with
+// the same FP64 operations as the device (d + ZERO, d - ZERO, dmin - ZERO, dmax + ZERO)
+static void build_screen32(const sdmd_system &s, Screen32 &o) {
+    const size_t NT3 = (size_t)SDMD_NTABLES * SDMD_NTYPES * SDMD_NTYPES;
+    auto entry = [](double dmin, double dmax, float *e) {
+        f32_bracket(dmin - SDMD_ZERO, e + 0);
+        f32_bracket(dmax + SDMD_ZERO, e + 2);
+        f32_bracket(dmin, e + 4);
+        f32_bracket(dmax, e + 6);
+    };
+    auto step = [](double d, float *e) {
+        f32_bracket(d + SDMD_ZERO, e + 0);
+        f32_bracket(d - SDMD_ZERO, e + 2);
+        f32_bracket(d, e + 4);
+    };
+    o.pair_thr.assign(NT3 * 8, 0.f);
+    for (size_t k = 0; k < NT3; k++) entry(s.pair_dmin[k], s.pair_dmax[k], &o.pair_thr[8 * k]);
+    o.pair_step.assign(((size_t)s.n_pair_steps + 1) * 6, 0.f);
+    for (int k = 0; k < s.n_pair_steps; k++) step(s.pair_step_d[k], &o.pair_step[6 * (size_t)k]);
+    o.con_thr.assign(((size_t)s.n_cons + 1) * 8, 0.f);
+    for (int k = 0; k < s.n_cons; k++) entry(s.con_dmin[k], s.con_dmax[k], &o.con_thr[8 * (size_t)k]);
+    o.con_step.assign(((size_t)s.n_con_steps + 1) * 6, 0.f);
+    for (int k = 0; k < s.n_con_steps; k++) step(s.con_step_d[k], &o.con_step[6 * (size_t)k]);
+    o.bond.assign(((size_t)s.n_bonds + 1) * 4, 0.f);
+    for (int k = 0; k < s.n_bonds; k++) {
+        f32_bracket(s.bond_dmin[k], &o.bond[4 * (size_t)k]);
+        f32_bracket(s.bond_dmax[k], &o.bond[4 * (size_t)k + 2]);
+    }
+}
+
 // ---- arena carving --------------------------------------------------------------
 struct Carver {
     unsigned char *base;
@@ -179,7 +224,8 @@ template <class T> static void put(std::vector<std::pair<void *, std::pair<const
 }
 
 static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
-                     std::vector<std::pair<void *, std::pair<const void *, size_t>>> *copies) {
+                     std::vector<std::pair<void *, std::pair<const void *, size_t>>> *copies,
+                     const std::vector<Screen32> *s32 = nullptr) {
     Carver cv{base, 0};
     const int trace_cap = h->opts.trace_capacity > 0 ? h->opts.trace_capacity : 0;
     for (int k = 0; k < h->n_systems; k++) {
@@ -223,6 +269,19 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
         d.smp_cum = cv.take<int64_t>(sc_);
         d.tloc = cv.take<double>(N1);
         d.lazy = h->opts.advance == SDMD_ADVANCE_LAZY ? 1 : 0;
+        d.pair_thr32 = cv.take<float>(NT3 * 8);
+        d.pair_step32 = cv.take<float>(((size_t)m.n_pair_steps + 1) * 6);
+        d.con_thr32 = cv.take<float>(((size_t)m.n_cons + 1) * 8);
+        d.con_step32 = cv.take<float>(((size_t)m.n_con_steps + 1) * 6);
+        d.bond32 = cv.take<float>(((size_t)m.n_bonds + 1) * 4);
+        if (copies && s32) {
+            const Screen32 &q = (*s32)[k];
+            put(*copies, (float *)d.pair_thr32, q.pair_thr.data(), q.pair_thr.size());
+            put(*copies, (float *)d.pair_step32, q.pair_step.data(), q.pair_step.size());
+            put(*copies, (float *)d.con_thr32, q.con_thr.data(), q.con_thr.size());
+            put(*copies, (float *)d.con_step32, q.con_step.data(), q.con_step.size());
+            put(*copies, (float *)d.bond32, q.bond.data(), q.bond.size());
+        }
         if (copies) {
             auto &c = *copies;
             put(c, (double *)d.mass, s.mass, N1);
@@ -294,7 +353,10 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     if (opts) h->opts = *opts;
     if (h->opts.device < 0 || h->opts.device >= ndev) { delete h; return SDMD_EINVAL; }
     if ((h->opts.advance != SDMD_ADVANCE_EAGER && h->opts.advance != SDMD_ADVANCE_LAZY) ||
-        h->opts.screen != SDMD_SCREEN_FP64) { delete h; return SDMD_EUNSUPPORTED; }
+        (h->opts.screen != SDMD_SCREEN_FP64 && h->opts.screen != SDMD_SCREEN_FP32)) {
+        delete h;
+        return SDMD_EUNSUPPORTED;
+    }
     int r = cuda_fail(cudaSetDevice(h->opts.device));
     if (r) { delete h; return r; }
     h->n_systems = n_systems;
@@ -326,8 +388,17 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         d.cutoff = s.cutoff; d.temperature = s.temperature; d.thermo_freq = s.thermo_freq; d.t_end = s.t_end;
         d.nbcap = m.nbcap;
         d.n_bonds = s.n_bonds; d.n_cons = s.n_cons; d.n_con_steps = s.n_con_steps; d.n_conn = s.n_conn;
+        d.screen = h->opts.screen;
+        double cut = s.cutoff * 0.90;   // the prediction's scan radius, as the device computes it
+        cut *= cut;
+        f32_bracket(cut, d.cut32);
+        f32_bracket(SDMD_ZERO, d.zero32);
+        for (int q = 0; q < 3; q++) f32_bracket(s.box[q], d.box32 + 2 * q);
     }
-    h->smem = fp64_smem_bytes(nbcap_max);
+    const bool scr = h->opts.screen == SDMD_SCREEN_FP32;
+    h->smem = scr ? screen_smem_bytes(nbcap_max) : fp64_smem_bytes(nbcap_max);
+    h->sweep_k = scr ? sweep_kernel_screen : sweep_kernel_fp64;
+    h->loop_k = scr ? loop_kernel_screen : loop_kernel_fp64;
     // stage whole systems in shared memory when they fit (small systems, batches)
     size_t st_max = 0;
     for (int k = 0; k < n_systems; k++) {
@@ -350,7 +421,9 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     }
     cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
     std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
-    layout(h, systems, h->arena, &copies);
+    std::vector<Screen32> s32(n_systems);
+    for (int k = 0; k < n_systems; k++) build_screen32(systems[k], s32[k]);
+    layout(h, systems, h->arena, &copies, &s32);
     for (auto &c : copies) cudaMemcpyAsync(c.first, c.second.first, c.second.second, cudaMemcpyHostToDevice, h->stream);
     std::vector<DScal> sc(n_systems);
     for (int k = 0; k < n_systems; k++) {
@@ -364,9 +437,9 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     }
     cudaMemcpyAsync(h->ds, h->hs.data(), sizeof(DSys) * n_systems, cudaMemcpyHostToDevice, h->stream);
     // the dynamic shared-memory limit must cover dynamic + static usage: always set it
-    if ((r = cuda_fail(cudaFuncSetAttribute(sweep_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if ((r = cuda_fail(cudaFuncSetAttribute(h->sweep_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)h->smem))) ||
-        (r = cuda_fail(cudaFuncSetAttribute(loop_kernel_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (r = cuda_fail(cudaFuncSetAttribute(h->loop_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)h->smem_loop)))) {
         sdmd_gpu_destroy(h);
         return r;
@@ -413,7 +486,7 @@ extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
     for (auto &m : h->meta) nmax = std::max(nmax, m.n);
     CK(cudaEventRecord(h->e0, h->stream));
     if (full_predict) launch_samples(h, (int64_t)nmax + 8);
-    sweep_kernel_fp64<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+    h->sweep_k<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
     if (full_predict) samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->e1, h->stream));
@@ -435,7 +508,7 @@ extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
     int64_t want = std::min<int64_t>(4 * max_events + 64, 1 << 16);
     for (int round = 0; round < 1 << 20; round++) {
         launch_samples(h, want);
-        loop_kernel_fp64<<<h->n_systems, h->threads, h->smem_loop, h->stream>>>(h->ds, t_end, h->staged);
+        h->loop_k<<<h->n_systems, h->threads, h->smem_loop, h->stream>>>(h->ds, t_end, h->staged);
         samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
         CK(cudaGetLastError());
         for (int k = 0; k < h->n_systems; k++)
@@ -641,7 +714,7 @@ extern "C" int sdmd_gpu_prepare_noalloc(sdmd_gpu *h, int32_t full_predict) {
         dim3 grid((unsigned)std::max<int64_t>(1, std::min<int64_t>((want + 255) / 256, 1024)), (unsigned)h->n_systems);
         samples_values_kernel<<<grid, 256, 0, h->stream>>>(table, want);
     }
-    sweep_kernel_fp64<<<h->n_systems, h->threads, h->smem, h->stream>>>(table, full_predict ? 1 : 0);
+    h->sweep_k<<<h->n_systems, h->threads, h->smem, h->stream>>>(table, full_predict ? 1 : 0);
     if (full_predict) samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(table, h->n_systems);
     noalloc_first_error_kernel<<<1, 1, 0, h->stream>>>(table, h->n_systems, first);
     CK(cudaGetLastError());

@@ -72,6 +72,14 @@ struct DSys {
     double *tloc;
     int32_t lazy, pad3;
     double now;              // the current time while a block works on this system
+    // FP32 screen: float brackets [lo, hi] around FP64 thresholds and limits
+    // (built on the host, see api.cu).  Per pair-table entry 8 floats:
+    // fl(dmin - ZERO), fl(dmax + ZERO), dmin, dmax; per pooled step 6 floats:
+    // fl(d + ZERO), fl(d - ZERO), d; constraints as pair entries / steps; per bond
+    // 4 floats: dmin, dmax.
+    const float *pair_thr32, *pair_step32, *con_thr32, *con_step32, *bond32;
+    float cut32[2], zero32[2], box32[6];
+    int32_t screen, pad4;
 };
 
 // position component of atom j at the current time (lazy mode extrapolates)

@@ -15,6 +15,11 @@ __global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int
 size_t staged_state_bytes(int n, int ncell, int nb, int nc, int ncs, int nconn);
 __global__ void lazy_enter_kernel(const DSys *systems);
 
+// FP32-screened prediction, identical results (loop_fp64.cu + screen.cuh)
+size_t screen_smem_bytes(int nbcap);
+__global__ void sweep_kernel_screen(const DSys *systems, int full);
+__global__ void loop_kernel_screen(const DSys *systems, double t_end_override, int staged);
+
 // thermostat sample stream (samples.cu)
 __global__ void samples_walk_kernel(const DSys *systems, int n_systems, int64_t want);
 __global__ void samples_values_kernel(const DSys *systems, int64_t want);

@@ -704,6 +704,10 @@ __device__ inline void carve(Shm &M, int nbcap) {
     M.L.j = ip; M.L.info = ip + cap; M.nbj = ip + 2 * cap; M.cnt = ip + 2 * cap + nbcap;
 }
 
+}  // namespace sdmd
+#include "screen.cuh"
+namespace sdmd {
+
 // ---- whole-system staging in shared memory ------------------------------------
 // A small system's per-atom arrays, topology, cell list and event tree are copied
 // into shared memory at kernel start; the block's DSys pointers are redirected to
@@ -798,16 +802,17 @@ __device__ void unstage_state(const DSys &S, const DSys &G) {
 size_t fp64_smem_bytes(int nbcap) { return fp64_smem_bytes_dev(nbcap); }
 
 // Full-rebuild sweep: ResetTarget + Predict over 1..N (src/SGThread.c:47-52), then
-// CreateCBT.  With full == 0 only the tree is built (continue mode).
-__global__ void sweep_kernel_fp64(const DSys *systems, int full) {
-    __shared__ DSys S;
+// CreateCBT.  With full == 0 only the tree is built (continue mode).  SCR selects
+// the FP32-screened prediction (identical results).
+template <bool SCR>
+__device__ __forceinline__ void sweep_body(const DSys *systems, int full, DSys &S, Blk &B, DScal &C, PairScal &PS) {
     if (threadIdx.x == 0) S = systems[blockIdx.x];
-    __shared__ Blk B;
-    __shared__ DScal C;
     if (threadIdx.x == 0) { B.err = 0; B.warn = 0; C = *S.sc; S.now = C.time; }
     __syncthreads();
     if (C.err) return;
-    Shm M; carve(M, S.nbcap);
+    Shm M;
+    ShmS MS;
+    if constexpr (SCR) carve_screen(MS, S.nbcap); else carve(M, S.nbcap);
     if (full) {
         if (S.thermostat && C.smp_avail < S.n) {   // one sample per predicted atom
             if (threadIdx.x == 0) { S.sc->err = SDMD_ECAPACITY; S.sc->err_atom = 0; }
@@ -817,7 +822,10 @@ __global__ void sweep_kernel_fp64(const DSys *systems, int full) {
             S.ev_type[i] = SDMD_EV_INVALID; S.ev_time[i] = INFINIT; S.ev_partner[i] = INVALID;
         }
         __syncthreads();
-        for (int i = 1; i <= S.n && B.err == 0; i++) predict_atom(S, i, M, B, C);
+        for (int i = 1; i <= S.n && B.err == 0; i++) {
+            if constexpr (SCR) predict_two(S, i, 0, MS, PS, B, C);
+            else predict_atom(S, i, M, B, C);
+        }
     }
     if (threadIdx.x == 0) {
         if (B.err == 0) cbt_build(S);
@@ -828,14 +836,27 @@ __global__ void sweep_kernel_fp64(const DSys *systems, int full) {
     }
 }
 
-// The event loop (src/SGThread.c:75-151)
-__global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int staged) {
+__global__ void sweep_kernel_fp64(const DSys *systems, int full) {
     __shared__ DSys S;
-    __shared__ DSys G;   // the global-memory view (write-back target when staged)
-    if (threadIdx.x == 0) { S = systems[blockIdx.x]; G = S; }
-    const int tid = threadIdx.x, T = blockDim.x;
     __shared__ Blk B;
     __shared__ DScal C;
+    __shared__ PairScal PS;
+    sweep_body<false>(systems, full, S, B, C, PS);
+}
+__global__ void sweep_kernel_screen(const DSys *systems, int full) {
+    __shared__ DSys S;
+    __shared__ Blk B;
+    __shared__ DScal C;
+    __shared__ PairScal PS;
+    sweep_body<true>(systems, full, S, B, C, PS);
+}
+
+// The event loop (src/SGThread.c:75-151)
+template <bool SCR>
+__device__ __forceinline__ void loop_body(const DSys *systems, double t_end_override, int staged, DSys &S, DSys &G,
+                                          Blk &B, DScal &C, PairScal &PS) {
+    if (threadIdx.x == 0) { S = systems[blockIdx.x]; G = S; }
+    const int tid = threadIdx.x, T = blockDim.x;
     __shared__ int32_t sh_t, sh_p, sh_exec, sh_go;
     __shared__ double sh_dt;
     __shared__ int32_t rec_partner, rec_type, rec_sub;
@@ -845,10 +866,12 @@ __global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int
     }
     __syncthreads();
     if (C.err) return;
-    Shm M; carve(M, S.nbcap);
+    Shm M;
+    ShmS MS;
+    if constexpr (SCR) carve_screen(MS, S.nbcap); else carve(M, S.nbcap);
     if (staged) {
         extern __shared__ __align__(16) unsigned char smem_all[];
-        stage_state(S, G, smem_all + fp64_smem_bytes_dev(S.nbcap), true);
+        stage_state(S, G, smem_all + (SCR ? screen_smem_bytes_dev(S.nbcap) : fp64_smem_bytes_dev(S.nbcap)), true);
     }
     const double t_end = t_end_override > 0 ? t_end_override : S.t_end;
     const int64_t stop_at = C.target_frame;
@@ -906,11 +929,21 @@ __global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int
         }
         __syncthreads();
         if (B.err) break;
-        predict_atom(S, t, M, B, C);
-        if (sh_exec && p && B.err == 0) predict_atom(S, p, M, B, C);
+        if constexpr (SCR) {
+            predict_two(S, t, sh_exec ? p : 0, MS, PS, B, C);
+            if (tid < 32 && B.err == 0) {
+                cbt_update_warp(S, t);
+                if (sh_exec && p) cbt_update_warp(S, p);
+            }
+        } else {
+            predict_atom(S, t, M, B, C);
+            if (sh_exec && p && B.err == 0) predict_atom(S, p, M, B, C);
+            if (tid == 0) {
+                cbt_update(S, t);
+                if (sh_exec && p) cbt_update(S, p);
+            }
+        }
         if (tid == 0) {
-            cbt_update(S, t);
-            if (sh_exec && p) cbt_update(S, p);
             if (S.trace_cap > 0) {
                 sdmd_trace_rec &r = S.trace[C.pops % S.trace_cap];
                 r.target = t; r.partner = rec_partner; r.type = rec_type; r.sub = rec_sub;
@@ -937,6 +970,23 @@ __global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int
         *G.sc = C;
     }
 }
+
+__global__ void loop_kernel_fp64(const DSys *systems, double t_end_override, int staged) {
+    __shared__ DSys S, G;   // G: the global-memory view (write-back target when staged)
+    __shared__ Blk B;
+    __shared__ DScal C;
+    __shared__ PairScal PS;
+    loop_body<false>(systems, t_end_override, staged, S, G, B, C, PS);
+}
+__global__ void loop_kernel_screen(const DSys *systems, double t_end_override, int staged) {
+    __shared__ DSys S, G;
+    __shared__ Blk B;
+    __shared__ DScal C;
+    __shared__ PairScal PS;
+    loop_body<true>(systems, t_end_override, staged, S, G, B, C, PS);
+}
+
+size_t screen_smem_bytes(int nbcap) { return screen_smem_bytes_dev(nbcap); }
 
 }  // namespace sdmd
 

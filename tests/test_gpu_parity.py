@@ -15,6 +15,10 @@ pytestmark = pytest.mark.gpu
 DYN = ["x", "y", "z", "vx", "vy", "vz", "cx", "cy", "cz", "type", "hb_bond", "hb_itype", "nb_partner", "nb_status",
        "nb_pnum", "ev_time", "ev_partner", "ev_counter", "ev_pcounter", "ev_potential", "ev_type", "ev_sub",
        "cell_list"]
+# every exactness test runs on both prediction paths: plain FP64, and the FP32
+# screen with FP64 refine (which must give identical results)
+SCREENS = pytest.mark.parametrize("screen", [0, 1], ids=["fp64", "screen32"])
+
 SWEEP = ["ev_time", "ev_partner", "ev_type", "ev_sub", "ev_potential", "ev_pcounter", "nb_pnum", "hb_itype"]
 
 
@@ -36,23 +40,25 @@ def assert_state_equal(a, ref, keys=DYN):
             raise AssertionError(f"{k} differs at {idx}: {x[idx]} vs {y[idx]}")
 
 
+@SCREENS
 @pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long"])
-def test_sweep_matches_reference(golden, engine_mod, case):
+def test_sweep_matches_reference(golden, engine_mod, case, screen):
     d = golden(case)
     s = from_fixture(d, "pre")
-    with engine_mod.Engine([s]) as eng:
+    with engine_mod.Engine([s], screen=screen) as eng:
         eng.prepare(full=True)
         eng.download()
     assert_state_equal(s.a, fixture_dynamic(d, "sweep"), SWEEP)
     assert s.counters["warnings"] == int(d["sweep/warningsum"][0])
 
 
+@SCREENS
 @pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt"])
-def test_loop_matches_reference_event_for_event(golden, engine_mod, case):
+def test_loop_matches_reference_event_for_event(golden, engine_mod, case, screen):
     d = golden(case)
     ids, dts = d["trace/ids"], d["trace/dt"]
     s = from_fixture(d, "pre")
-    with engine_mod.Engine([s], trace=len(ids) + 16) as eng:
+    with engine_mod.Engine([s], trace=len(ids) + 16, screen=screen) as eng:
         eng.prepare(full=True)
         eng.run(int(d["meta/n_events"][0]))
         eng.download()
@@ -71,12 +77,13 @@ def test_loop_matches_reference_event_for_event(golden, engine_mod, case):
     assert s.time == ref["_time"]
 
 
-def test_long_run_with_hb_events(golden, engine_mod):
+@SCREENS
+def test_long_run_with_hb_events(golden, engine_mod, screen):
     """1.5e5 events covering HB formation/breaking and HB-neighbour events, in
     chunks (the device state persists between run calls)."""
     d = golden("ala10_nvt_long")
     s = from_fixture(d, "pre")
-    with engine_mod.Engine([s]) as eng:
+    with engine_mod.Engine([s], screen=screen) as eng:
         eng.prepare(full=True)
         done = 0
         for c in [int(v) for v in d["meta/ckpts"]] + [int(d["meta/n_events"][0])]:
@@ -89,7 +96,8 @@ def test_long_run_with_hb_events(golden, engine_mod):
     assert s.counters["hb"] > 0 and s.counters["hbneighbor"] > 0
 
 
-def test_batch_of_systems_matches_oracle(golden, engine_mod):
+@SCREENS
+def test_batch_of_systems_matches_oracle(golden, engine_mod, screen):
     """Several independent systems in one launch (one CTA each): NVE, NVT and NVT
     with other RNG streams; each must equal its own oracle run."""
     from oracle import oracle as O
@@ -101,7 +109,7 @@ def test_batch_of_systems_matches_oracle(golden, engine_mod):
         s.rng = rng_state_after(seed, 0)
         systems.append(s)
     refs = [s.copy() for s in systems]
-    with engine_mod.Engine(systems, threads=64) as eng:
+    with engine_mod.Engine(systems, threads=64, screen=screen) as eng:
         eng.prepare(full=True)
         eng.run(3000)
         eng.download()
@@ -114,17 +122,18 @@ def test_batch_of_systems_matches_oracle(golden, engine_mod):
         assert s.counters == r.counters and s.time == r.time
 
 
+@SCREENS
 @pytest.mark.parametrize("threads", [32, 96, 256])
-def test_block_size_does_not_change_results(golden, engine_mod, threads):
+def test_block_size_does_not_change_results(golden, engine_mod, threads, screen):
     d = golden("ala10_nvt")
     s = from_fixture(d, "pre")
-    with engine_mod.Engine([s], threads=threads) as eng:
+    with engine_mod.Engine([s], threads=threads, screen=screen) as eng:
         eng.prepare(full=True)
         eng.run(2000)
         eng.download()
     ref = fixture_dynamic(d, "ckpt1000")
     s2 = from_fixture(d, "pre")
-    with engine_mod.Engine([s2], threads=threads) as eng:
+    with engine_mod.Engine([s2], threads=threads, screen=screen) as eng:
         eng.prepare(full=True)
         eng.run(1000)
         eng.download()
