@@ -14,10 +14,10 @@
 //      intermediate lies inside its interval).  The screen decides each
 //      branch of CollisionTime / BondTime / HBTime / FindPair with certainty
 //      or marks the candidate "refine";
-//   2. U = the smallest upper time bound over offers that are certainly made,
-//      plus the exact PCC and thermostat times.  The running minimum of the
-//      fold can only end at or below U.  Offers whose lower bound exceeds
-//      U' = max(U, every duplicate time) can neither win nor change the
+//   2. U = the smallest upper time bound over bond and collision offers that
+//      are certainly made: the bond/collision part of the fold ends at or below
+//      U.  Offers whose lower bound exceeds U' = max(U, every duplicate time)
+//      can neither be a running-minimum record of the fold nor change the
 //      outcome of a duplicate check, so they are dropped (their warning counts
 //      are certain and still added);
 //   3. the remaining candidates (typically 1-4 per atom) are recomputed
@@ -578,7 +578,7 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         }
         M.stat[a][e] = (uint8_t)(v.st | (v.warn << 2));
         M.tlo[a][e] = v.t.lo;
-        if (v.st == SC_OFFER) atomicMin(&PS.u_key[a], f_key(v.t.hi));
+        if (v.st == SC_OFFER && e < nb + nn) atomicMin(&PS.u_key[a], f_key(v.t.hi));
         else if (v.st == SC_NONE && v.warn) atomicAdd(&PS.warn_excl[a], v.warn);
         if (v.dup) {   // CheckDuplication may adopt j's stored time: it bounds what can matter
             double d = S.ev_time[j];
@@ -587,23 +587,16 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         }
     }
     __syncthreads();
-    // 3. U: an upper bound of each atom's final event time; U' adds every duplicate time
+    // 3. U: the bond / collision segment of the fold ends at or below U (its smallest
+    // certain upper bound).  Bounding only by that segment keeps the whole fold
+    // exact, including JobAssign's partnerCounter, which a partner-less winner
+    // (PCC, thermostat, wall) leaves at the value of the last bond/collision record.
+    // U' adds every duplicate time (and, for the partner, the target's bound).
     if (tid == 0) {
         PS.nowf = S.lazy ? fmaxf(fabsf(ivd(S.now).hi), fabsf(ivd(S.now).lo)) : 0.f;
         float u_t = INFINITY;
         for (int a = 0; a < na; a++) {
             float u = key_f(PS.u_key[a]);
-            double best = INFINIT;
-            for (int d = 0; d < 3; d++) {
-                double tf = M.face[3 * a + d];
-                if (tkey(best) > tkey(tf) && tkey(tf) > 0) best = tf;
-            }
-            if (tkey(best) > 0) u = fminf(u, ivd(best).hi);
-            if (S.thermostat && C.smp_used + a < C.smp_avail) {
-                double th = S.smp[C.smp_used + a] * sqrt(1.0) + 0;
-                th = S.thermo_freq * (th < 0 ? -th : th);
-                if (tkey(th) > 0) u = fminf(u, ivd(th).hi);
-            }
             float up = fmaxf(u, key_f(PS.dup_key[a]));
             if (a == 0) u_t = u;
             else up = fmaxf(up, u_t);      // the target's new event may become a duplicate for the partner
