@@ -174,7 +174,18 @@ static void f32_bracket(double v, float *out) {
 
 struct Screen32 {
     std::vector<float> pair_thr, pair_step, con_thr, con_step, bond;
+    std::vector<long long> pair_key, pair_stepkey, con_key, con_stepkey;
+    std::vector<int32_t> conn_win;
 };
+
+// the device's tkey(): an order-preserving map of non-NaN doubles onto int64
+static long long host_tkey(double d) {
+    long long b;
+    memcpy(&b, &d, 8);
+    return b >= 0 ? b : -(b & 0x7fffffffffffffffLL);
+}
+constexpr int kConnWin = 9;   // ints per atom in conn_win
+constexpr int kMaxPerCell = 64; // screened path: atoms per cell array
 
 // brackets of every FP64 threshold the prediction compares against, computed with
 // the same FP64 operations as the device (d + ZERO, d - ZERO, dmin - ZERO, dmax + ZERO)
@@ -203,6 +214,39 @@ static void build_screen32(const sdmd_system &s, Screen32 &o) {
     for (int k = 0; k < s.n_bonds; k++) {
         f32_bracket(s.bond_dmin[k], &o.bond[4 * (size_t)k]);
         f32_bracket(s.bond_dmax[k], &o.bond[4 * (size_t)k + 2]);
+    }
+    o.pair_key.assign(NT3 * 2, 0);
+    for (size_t k = 0; k < NT3; k++) {
+        o.pair_key[2 * k] = host_tkey(s.pair_dmin[k] - SDMD_ZERO);
+        o.pair_key[2 * k + 1] = host_tkey(s.pair_dmax[k] + SDMD_ZERO);
+    }
+    o.pair_stepkey.assign(((size_t)s.n_pair_steps + 1) * 2, 0);
+    for (int k = 0; k < s.n_pair_steps; k++) {
+        o.pair_stepkey[2 * (size_t)k] = host_tkey(s.pair_step_d[k] + SDMD_ZERO);
+        o.pair_stepkey[2 * (size_t)k + 1] = host_tkey(s.pair_step_d[k] - SDMD_ZERO);
+    }
+    o.con_key.assign(((size_t)s.n_cons + 1) * 2, 0);
+    for (int k = 0; k < s.n_cons; k++) {
+        o.con_key[2 * (size_t)k] = host_tkey(s.con_dmin[k] - SDMD_ZERO);
+        o.con_key[2 * (size_t)k + 1] = host_tkey(s.con_dmax[k] + SDMD_ZERO);
+    }
+    o.con_stepkey.assign(((size_t)s.n_con_steps + 1) * 2, 0);
+    for (int k = 0; k < s.n_con_steps; k++) {
+        o.con_stepkey[2 * (size_t)k] = host_tkey(s.con_step_d[k] + SDMD_ZERO);
+        o.con_stepkey[2 * (size_t)k + 1] = host_tkey(s.con_step_d[k] - SDMD_ZERO);
+    }
+    const int N = s.n_atoms;
+    o.conn_win.assign((size_t)(N + 1) * kConnWin, 0);
+    for (int i = 1; i <= N; i++) {
+        int32_t *w = &o.conn_win[(size_t)i * kConnWin];
+        w[0] = i - 64;
+        for (int k = s.conn_off[i]; k < s.conn_off[i + 1]; k++) {
+            int idx = s.conn_j[k] - (i - 64), bits = s.conn_bits[k];
+            if (idx < 0 || idx >= 128) { w[0] = -1; break; }
+            if (bits & 1) w[1 + (idx >> 5)] |= (int32_t)(1u << (idx & 31));
+            if (bits & 2) w[5 + (idx >> 5)] |= (int32_t)(1u << (idx & 31));
+        }
+        if (w[0] < 0) for (int q = 1; q < kConnWin; q++) w[q] = 0;
     }
 }
 
@@ -274,6 +318,16 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
         d.con_thr32 = cv.take<float>(((size_t)m.n_cons + 1) * 8);
         d.con_step32 = cv.take<float>(((size_t)m.n_con_steps + 1) * 6);
         d.bond32 = cv.take<float>(((size_t)m.n_bonds + 1) * 4);
+        d.pair_key = cv.take<long long>(NT3 * 2);
+        d.pair_stepkey = cv.take<long long>(((size_t)m.n_pair_steps + 1) * 2);
+        d.con_key = cv.take<long long>(((size_t)m.n_cons + 1) * 2);
+        d.con_stepkey = cv.take<long long>(((size_t)m.n_con_steps + 1) * 2);
+        d.conn_win = cv.take<int32_t>(N1 * kConnWin);
+        if (h->opts.screen == SDMD_SCREEN_FP32) {
+            d.maxc = std::min<int32_t>(kMaxPerCell, m.n);
+            d.cell_cnt = cv.take<int32_t>((size_t)m.ncell + 1);
+            d.cell_arr = cv.take<int32_t>(((size_t)m.ncell + 1) * d.maxc);
+        }
         if (copies && s32) {
             const Screen32 &q = (*s32)[k];
             put(*copies, (float *)d.pair_thr32, q.pair_thr.data(), q.pair_thr.size());
@@ -281,6 +335,11 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             put(*copies, (float *)d.con_thr32, q.con_thr.data(), q.con_thr.size());
             put(*copies, (float *)d.con_step32, q.con_step.data(), q.con_step.size());
             put(*copies, (float *)d.bond32, q.bond.data(), q.bond.size());
+            put(*copies, (long long *)d.pair_key, q.pair_key.data(), q.pair_key.size());
+            put(*copies, (long long *)d.pair_stepkey, q.pair_stepkey.data(), q.pair_stepkey.size());
+            put(*copies, (long long *)d.con_key, q.con_key.data(), q.con_key.size());
+            put(*copies, (long long *)d.con_stepkey, q.con_stepkey.data(), q.con_stepkey.size());
+            put(*copies, (int32_t *)d.conn_win, q.conn_win.data(), q.conn_win.size());
         }
         if (copies) {
             auto &c = *copies;
@@ -392,6 +451,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         double cut = s.cutoff * 0.90;   // the prediction's scan radius, as the device computes it
         cut *= cut;
         f32_bracket(cut, d.cut32);
+        d.cut_key = host_tkey(cut);
         f32_bracket(SDMD_ZERO, d.zero32);
         for (int q = 0; q < 3; q++) f32_bracket(s.box[q], d.box32 + 2 * q);
     }

@@ -80,6 +80,20 @@ struct DSys {
     const float *pair_thr32, *pair_step32, *con_thr32, *con_step32, *bond32;
     float cut32[2], zero32[2], box32[6];
     int32_t screen, pad4;
+    // exact refine: the same FP64 thresholds as ordered integer keys (tkey), so a
+    // comparison costs an integer compare instead of an FP64 add and compare.
+    // Per pair entry / constraint 2 keys: fl(dmin - ZERO), fl(dmax + ZERO); per
+    // pooled step 2 keys: fl(d + ZERO), fl(d - ZERO).
+    const long long *pair_key, *pair_stepkey, *con_key, *con_stepkey;
+    long long cut_key;               // tkey((0.9 cutoff)^2)
+    // connection-map bits of atom i for partners i-64 .. i+63: [base, 4 BOND
+    // words, 4 CONSTRAINT words]; base < 0 when the row does not fit the window
+    const int32_t *conn_win;
+    // screened path: per-cell atom arrays, the cell lists in insertion order (the
+    // reference's list head is the last entry); authoritative inside the screened
+    // kernels, which rebuild cell_list from them before they return
+    int32_t *cell_cnt, *cell_arr;
+    int32_t maxc, pad5;
 };
 
 // position component of atom j at the current time (lazy mode extrapolates)

@@ -54,11 +54,15 @@ __device__ inline void sync_atom(const DSys &S, int a) {
 // (27 cells in src/DMD.c:117-121 order, each list head-first: src/TimePrediction.c:60-80)
 __device__ void gather(const DSys &S, int i, int32_t *nbj, int32_t *cnt, Blk &B) {
     int tid = threadIdx.x;
-    int head = 0, c = 0;
+    int head = 0, c = 0, cell = 0;
     if (tid < 27) {
-        head = S.cell_list[S.n + nb_cell(S, i, tid)];
-        for (int a = head; a; a = S.cell_list[a]) {
-            if (++c > S.n) break;   // a corrupted (cyclic) list cannot spin forever
+        cell = nb_cell(S, i, tid);
+        if (S.cell_arr) c = S.cell_cnt[cell];   // screened path: per-cell arrays
+        else {
+            head = S.cell_list[S.n + cell];
+            for (int a = head; a; a = S.cell_list[a]) {
+                if (++c > S.n) break;   // a corrupted (cyclic) list cannot spin forever
+            }
         }
         cnt[tid] = c;
     }
@@ -72,7 +76,12 @@ __device__ void gather(const DSys &S, int i, int32_t *nbj, int32_t *cnt, Blk &B)
     __syncthreads();
     if (tid < 27 && B.err == 0) {
         int o = cnt[tid], m = 0;
-        for (int a = head; a && m < c; a = S.cell_list[a]) nbj[o + m++] = a;
+        if (S.cell_arr) {
+            const int32_t *arr = S.cell_arr + (size_t)cell * S.maxc;
+            for (; m < c; m++) nbj[o + m] = arr[c - 1 - m];
+        } else {
+            for (int a = head; a && m < c; a = S.cell_list[a]) nbj[o + m++] = a;
+        }
     }
     __syncthreads();
 }
@@ -429,20 +438,27 @@ __device__ void imaged(const DSys &S, int t, int a, double p[3]) {
 // exactly as the reference's local does.
 __device__ double hb_energy_change(const DSys &S, int t, int skip, int to_hb, Blk &B, int *bad) {
     double cut = S.cutoff * S.cutoff, energy = 0, acc = 0;
+    auto visit = [&](int j) {
+        int bits = conn_bits(S, t, j);
+        if (!(t != j && !(bits & 1) && !(bits & 2) && j != skip)) return;
+        Kin k; pair_kin(S, t, j, k);
+        if (k.r2 <= cut) {
+            Lim o; int warn = 0;
+            if (!to_hb) { find_pair(S, t, j, K_COLLISION, 0, k.r2, o, 0, -1, 0, &warn, bad); acc = o.acc; }
+            else if (j != S.hb_neighbor[skip]) { find_pair(S, t, j, K_COLLISION, 0, k.r2, o, 0, 1, 0, &warn, bad); acc = o.acc; }
+            B.warn += warn;
+            if (acc == INFINIT) acc = 0;
+            energy += acc;
+        }
+    };
     for (int kc = 0; kc < 27; kc++) {
-        int guard = 0;
-        for (int j = S.cell_list[S.n + nb_cell(S, t, kc)]; j && guard <= S.n; j = S.cell_list[j], guard++) {
-            int bits = conn_bits(S, t, j);
-            if (!(t != j && !(bits & 1) && !(bits & 2) && j != skip)) continue;
-            Kin k; pair_kin(S, t, j, k);
-            if (k.r2 <= cut) {
-                Lim o; int warn = 0;
-                if (!to_hb) { find_pair(S, t, j, K_COLLISION, 0, k.r2, o, 0, -1, 0, &warn, bad); acc = o.acc; }
-                else if (j != S.hb_neighbor[skip]) { find_pair(S, t, j, K_COLLISION, 0, k.r2, o, 0, 1, 0, &warn, bad); acc = o.acc; }
-                B.warn += warn;
-                if (acc == INFINIT) acc = 0;
-                energy += acc;
-            }
+        const int cell = nb_cell(S, t, kc);
+        if (S.cell_arr) {   // screened path: the per-cell arrays, newest first (the list's order)
+            const int32_t *arr = S.cell_arr + (size_t)cell * S.maxc;
+            for (int m = S.cell_cnt[cell] - 1; m >= 0; m--) visit(arr[m]);
+        } else {
+            int guard = 0;
+            for (int j = S.cell_list[S.n + cell]; j && guard <= S.n; j = S.cell_list[j], guard++) visit(j);
         }
     }
     return energy;
@@ -574,7 +590,7 @@ __device__ void thermostat_event(const DSys &S, int t, DScal &C, Blk &B) {
 
 // PBCandCrossCellEvent with PBC("part") and LinkList("part")
 // (src/Events.c:248-272, 207-245, 158-200)
-__device__ void pcc_event(const DSys &S, int t, Blk &B) {
+__device__ void pcc_event(const DSys &S, int t, Blk &B, int32_t *moved = nullptr) {
     int old[3] = {S.cx[t], S.cy[t], S.cz[t]};
     double pos[3] = {S.x[t], S.y[t], S.z[t]};
     for (int d = 0; d < 3; d++) {
@@ -603,6 +619,10 @@ __device__ void pcc_event(const DSys &S, int t, Blk &B) {
         set_err(B, SDMD_ELINK, t); return;
     }
     int newc = cell_lin(S, nc[0], nc[1], nc[2]);
+    if (moved) {   // the screened path keeps per-cell arrays: the move is applied by a warp
+        moved[0] = t; moved[1] = oldc; moved[2] = newc;
+        return;
+    }
     int32_t *L = S.cell_list;
     int at = oldc + N, guard = 0;
     if (L[at] == 0) { set_err(B, SDMD_ELINK, t); return; }
@@ -638,7 +658,7 @@ __device__ void wall_event(const DSys &S, int t, Blk &B) {
 }
 
 // DoEvent (src/Events.c:25-114)
-__device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B) {
+__device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, int32_t *moved = nullptr) {
     int bad = 0;
     switch (S.ev_type[t]) {
         case SDMD_EV_COLLISION: interaction_event(S, t, p, 0, 0, B, &bad); C.c.collision++; break;
@@ -651,7 +671,7 @@ __device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B) {
             C.c.hb++;
         } break;
         case SDMD_EV_THERMOSTAT: thermostat_event(S, t, C, B); C.c.thermostat++; break;
-        case SDMD_EV_PCC: pcc_event(S, t, B); C.c.pcc++; break;
+        case SDMD_EV_PCC: pcc_event(S, t, B, moved); C.c.pcc++; break;
         case SDMD_EV_WALL: wall_event(S, t, B); C.c.wall++; break;
         default: set_err(B, SDMD_EEVENTTYPE, t); break;
     }
@@ -813,6 +833,10 @@ __device__ __forceinline__ void sweep_body(const DSys *systems, int full, DSys &
     Shm M;
     ShmS MS;
     if constexpr (SCR) carve_screen(MS, S.nbcap); else carve(M, S.nbcap);
+    if constexpr (SCR) {
+        cells_from_list(S, B);
+        __syncthreads();
+    }
     if (full) {
         if (S.thermostat && C.smp_avail < S.n) {   // one sample per predicted atom
             if (threadIdx.x == 0) { S.sc->err = SDMD_ECAPACITY; S.sc->err_atom = 0; }
@@ -860,6 +884,7 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
     __shared__ int32_t sh_t, sh_p, sh_exec, sh_go;
     __shared__ double sh_dt;
     __shared__ int32_t rec_partner, rec_type, rec_sub;
+    __shared__ int32_t sh_move[3], sh_cells_ok;
     if (tid == 0) {
         B.err = 0; B.warn = 0; C = *S.sc;
         if (!C.cbt_built && !C.err) { C.err = SDMD_EINVAL; C.err_atom = 0; *S.sc = C; }   // prepare() first
@@ -872,6 +897,11 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
     if (staged) {
         extern __shared__ __align__(16) unsigned char smem_all[];
         stage_state(S, G, smem_all + (SCR ? screen_smem_bytes_dev(S.nbcap) : fp64_smem_bytes_dev(S.nbcap)), true);
+    }
+    if constexpr (SCR) {
+        cells_from_list(S, B);
+        __syncthreads();
+        if (tid == 0) sh_cells_ok = B.err == 0;
     }
     const double t_end = t_end_override > 0 ? t_end_override : S.t_end;
     const int64_t stop_at = C.target_frame;
@@ -915,9 +945,10 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
             else C.time += dt;
             int hazard = p > 0 && S.ev_pcounter[t] < S.ev_counter[p];   // HazardCheck
             sh_exec = !hazard;
+            sh_move[0] = 0;
             if (!hazard) {
                 C.c.frame++;
-                do_event(S, C, t, p, B);
+                do_event(S, C, t, p, B, SCR ? sh_move : nullptr);
                 S.ev_counter[t]++;
                 if (p) S.ev_counter[p]++;
             } else {
@@ -928,6 +959,12 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
             if (!hazard && p) { S.ev_type[p] = SDMD_EV_INVALID; S.ev_time[p] = INFINIT; S.ev_partner[p] = INVALID; }
         }
         __syncthreads();
+        if constexpr (SCR) {
+            if (sh_move[0]) {   // a PCC event moved t between cells: update the cell arrays
+                if (tid < 32) cell_move_warp(S, sh_move[0], sh_move[1], sh_move[2], B);
+                __syncthreads();
+            }
+        }
         if (B.err) break;
         if constexpr (SCR) {
             predict_two(S, t, sh_exec ? p : 0, MS, PS, B, C);
@@ -959,6 +996,10 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
             C.pops++;
         }
         __syncthreads();
+    }
+    if constexpr (SCR) {
+        __syncthreads();
+        if (sh_cells_ok) cells_to_list(S);
     }
     if (staged) {
         __syncthreads();

@@ -136,6 +136,17 @@ __device__ __forceinline__ Iv root_iv(const KIv &k, int st, Iv d2, bool &ok) {
     return t;
 }
 
+// connection-map bits of (i, j) from the per-atom window (row scan outside it)
+__device__ __forceinline__ int conn_bits_w(const DSys &S, int i, int j) {
+    const int32_t *w = S.conn_win + 9 * i;
+    const int base = w[0];
+    if (base < 0) return conn_bits(S, i, j);
+    const unsigned idx = (unsigned)(j - base);
+    if (idx >= 128u) return 0;
+    const unsigned m = 1u << (idx & 31);
+    return (((unsigned)w[1 + (idx >> 5)] & m) ? 1 : 0) | (((unsigned)w[5 + (idx >> 5)] & m) ? 2 : 0);
+}
+
 // ---- screen verdicts ----------------------------------------------------------
 enum : int { SC_NONE = 0, SC_OFFER = 1, SC_REFINE = 2 };
 struct Verdict { int st, warn, dup; Iv t; };
@@ -251,56 +262,9 @@ __device__ void screen_bond(const DSys &S, int i, int q, const PIv &I, Verdict &
     if (t.lo > 0.f) { v.st = SC_OFFER; v.t = t; }
 }
 
-// CollisionTime for one candidate (eval_collision's branches); st NONE also
-// covers "not a candidate"
-__device__ void screen_coll(const DSys &S, int i, int j, const PIv &I, Verdict &v, int always_refine) {
-    v.warn = 0; v.dup = 0; v.st = SC_NONE;
-    if (j == i) return;
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
-        v.st = SC_REFINE; v.dup = 1; return;
-    }
-    if (always_refine) { v.st = SC_REFINE; return; }
-    int bits = conn_bits(S, i, j);
-    if ((bits & 1) || S.hb_bond[i] == j || nb_has(S, i, j)) return;
-    PIv J; atom_piv(S, j, J);
-    KIv k; kin_iv(S, I, J, k);
-    if (k.r2.lo > S.cut32[1]) return;                  // certainly beyond the scan radius
+// HBTime's scan over one candidate (eval_hb_scan's branches), kinematics given
+__device__ void screen_hbs_k(const DSys &S, int i, int j, const KIv &k, Verdict &v) {
     v.st = SC_REFINE;
-    if (!(k.r2.hi <= S.cut32[0])) return;
-    int neg = bsign3(k.b);
-    if (neg == 2) return;
-    const int constrained = bits & 2;
-    FPs o;
-    if (!fp_screen(S, i, j, constrained ? K_CONSTRAINT : K_COLLISION, neg, k.r2, o)) return;
-    if (!constrained && o.lopot0 && o.uppot0) { v.st = SC_NONE; v.warn = o.warn; return; }
-    if (o.inf) return;                                 // constraint beyond its outer limit: exact path
-    int st = 1; Iv d2 = o.up;
-    if (neg) {
-        Iv D = disc_iv(k, o.lo);
-        if (D.lo > 0.f) { st = -1; d2 = o.lo; }
-        else if (!(D.hi <= 0.f)) return;
-    }
-    if (st == 1 && !constrained && o.cs == 1) { v.st = SC_NONE; v.warn = o.warn; return; }
-    bool ok;
-    Iv t = root_iv(k, st, d2, ok);
-    if (!ok) return;
-    if (t.lo > 0.f) { v.st = SC_OFFER; v.t = t; v.warn = o.warn; }
-    else if (t.hi <= 0.f) { v.st = SC_NONE; v.warn = o.warn; }   // JobAssign rejects t <= 0
-}
-
-// HBTime's scan over one candidate (eval_hb_scan's branches)
-__device__ void screen_hbs(const DSys &S, int i, int j, const PIv &I, Verdict &v, int always_refine) {
-    v.warn = 0; v.dup = 0; v.st = SC_NONE;
-    if (!(i != j && hb_pair_ok(S, i, j) && S.hb_bond[j] == 0 &&
-          ((S.protein[i] == S.protein[j] && abs(S.aanum[i] - S.aanum[j]) >= 4) || S.protein[i] != S.protein[j])))
-        return;
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
-        v.st = SC_REFINE; v.dup = 1; return;
-    }
-    v.st = SC_REFINE;
-    if (always_refine) return;
-    PIv J; atom_piv(S, j, J);
-    KIv k; kin_iv(S, I, J, k);
     if (k.r2.lo > S.cut32[1]) { v.st = SC_NONE; return; }
     if (!(k.r2.hi <= S.cut32[0])) return;
     int bad = 0;
@@ -323,34 +287,362 @@ __device__ void screen_hbs(const DSys &S, int i, int j, const PIv &I, Verdict &v
     if (t.lo > 0.f) { v.st = SC_OFFER; v.t = t; v.warn = o.warn; }
 }
 
-// ---- HB-bonded partner: the fresh part of hb_bonded(), evaluated by a lane ------
-struct HbbOut { double t, pot; int sub, warn, bad; };
-__device__ void hbb_fresh(const DSys &S, int i, HbbOut &r) {
-    int j = S.hb_bond[i];
-    Kin kk; pair_kin(S, i, j, kk);
-    Lim o; int warn = 0, bad = 0;
-    int cs = find_pair(S, i, j, K_HB, kk.b, kk.r2, o, 0, 0, 0, &warn, &bad);
-    int st, sub; double d2, pot;
-    if (kk.b < 0 && disc(kk, o.lo) > 0) {
-        st = -1; d2 = o.lo; pot = o.lopot; sub = (cs == 0) ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
-    } else {
-        st = 1; d2 = o.up; pot = o.uppot; sub = (cs == 1) ? SDMD_SUB_TBD_HBBREAK : SDMD_SUB_TBD_ESCAPE;
+// One 27-cell candidate j of atom i: the collision verdict (CollisionTime) and,
+// when the atom scans for hydrogen bonds (hb), the HB-scan verdict, sharing one
+// evaluation of the pair's kinematics.  `always` forces "refine" (the partner's
+// view of the target, whose event is only known after the target's fold).
+__device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, bool hb, int always, Verdict &vc,
+                            Verdict &vh) {
+    vc.warn = 0; vc.dup = 0; vc.st = SC_NONE;
+    vh.warn = 0; vh.dup = 0; vh.st = SC_NONE;
+    if (j == i) return;
+    bool need_c = true;
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
+        vc.st = SC_REFINE; vc.dup = 1; need_c = false;
+    } else if (always) { vc.st = SC_REFINE; need_c = false; }
+    bool need_h = hb && hb_pair_ok(S, i, j) && S.hb_bond[j] == 0 &&
+                  ((S.protein[i] == S.protein[j] && abs(S.aanum[i] - S.aanum[j]) >= 4) || S.protein[i] != S.protein[j]);
+    if (need_h) {
+        if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
+            vh.st = SC_REFINE; vh.dup = 1; need_h = false;
+        } else if (always) { vh.st = SC_REFINE; need_h = false; }
     }
-    double t = root(kk, st, d2);
-    if (t < 0) t = INFINIT;
+    int bits = 0;
+    if (need_c) {
+        bits = conn_bits_w(S, i, j);
+        if ((bits & 1) || S.hb_bond[i] == j || nb_has(S, i, j)) need_c = false;
+    }
+    if (!need_c && !need_h) return;
+    PIv J; atom_piv(S, j, J);
+    KIv k; kin_iv(S, I, J, k);
+    if (need_h) screen_hbs_k(S, i, j, k, vh);
+    if (!need_c) return;
+    Verdict &v = vc;
+    if (k.r2.lo > S.cut32[1]) return;                  // certainly beyond the scan radius
+    v.st = SC_REFINE;
+    if (!(k.r2.hi <= S.cut32[0])) return;
+    int neg = bsign3(k.b);
+    if (neg == 2) return;
+    const int constrained = bits & 2;
+    FPs o;
+    if (!fp_screen(S, i, j, constrained ? K_CONSTRAINT : K_COLLISION, neg, k.r2, o)) return;
+    if (!constrained && o.lopot0 && o.uppot0) { v.st = SC_NONE; v.warn = o.warn; return; }
+    if (o.inf) return;
+    int st = 1; Iv d2 = o.up;
+    if (neg) {
+        Iv D = disc_iv(k, o.lo);
+        if (D.lo > 0.f) { st = -1; d2 = o.lo; }
+        else if (!(D.hi <= 0.f)) return;
+    }
+    if (st == 1 && !constrained && o.cs == 1) { v.st = SC_NONE; v.warn = o.warn; return; }
+    bool ok;
+    Iv t = root_iv(k, st, d2, ok);
+    if (!ok) return;
+    if (t.lo > 0.f) { v.st = SC_OFFER; v.t = t; v.warn = o.warn; }
+    else if (t.hi <= 0.f) { v.st = SC_NONE; v.warn = o.warn; }
+}
+
+// ---- exact refine: the plain path's FP64 arithmetic, integer-key compares --------
+// Each function below performs the same FP64 operations, in the same order, as its
+// plain-path counterpart (eval_bond / eval_collision / eval_hb_scan / find_pair),
+// so every FP64 value is bit-identical.  Comparisons of FP64 values are made on
+// their tkey() images (an order-preserving map, +0 == -0), and thresholds such as
+// fl(d + ZERO) come precomputed from the host, which performs the same IEEE
+// additions.  The target's own position lzx(i) is computed once per prediction.
+constexpr long long KEY_ZERO = 0x3E45798EE2308C3ALL;   // tkey(1e-8)
+
+// x < 0 and x > 0 with IEEE semantics (false for NaN), as integer tests
+__device__ __forceinline__ bool dbl_lt0(double x) {
+    long long b = __double_as_longlong(x);
+    return b < 0 && (b & 0x7fffffffffffffffLL) != 0 && (b & 0x7fffffffffffffffLL) <= 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool dbl_gt0(double x) {
+    long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000LL;
+}
+
+__device__ int find_pair_r(const DSys &S, int a1, int a2, int kind, bool neg, double distance2, Lim &o, int *warn,
+                           int *bad) {
+    int cs = -1;
+    const long long *key, *skey;
+    const double *sd, *se;
+    double dmin, dmax;
+    int sn;
+    if (kind == K_CONSTRAINT) {
+        int k = S.con_off[a1], e = S.con_off[a1 + 1];
+        for (; k < e; k++) if (S.con_j[k] == a2) break;
+        if (k == e) { *bad = 1; return -1; }
+        dmin = S.con_dmin[k]; dmax = S.con_dmax[k]; sn = S.con_step_n[k]; key = S.con_key + 2 * k;
+        int so = S.con_step_off[k];
+        sd = S.con_step_d + so; se = S.con_step_e + so; skey = S.con_stepkey + 2 * so;
+    } else {
+        int e;
+        if (kind == K_COLLISION) {
+            int t1 = S.type[a1], t2 = S.type[a2];
+            if (dbl_pos(S.pair_dmin[tab_idx(0, t1, t2)])) e = tab_idx(0, t1, t2);
+            else {
+                int a = type_change(t1, 0), b = type_change(t2, 0);
+                if (dbl_pos(S.pair_dmin[tab_idx(0, a, t2)])) e = tab_idx(0, a, t2);
+                else if (dbl_pos(S.pair_dmin[tab_idx(0, t1, b)])) e = tab_idx(0, t1, b);
+                else if (dbl_pos(S.pair_dmin[tab_idx(0, a, b)])) e = tab_idx(0, a, b);
+                else { *bad = 1; return -1; }
+            }
+        } else {   // K_HB
+            int tn = hb_model(S, a1, a2, bad);
+            if (tn < 0) { *bad = 1; tn = 0; }
+            e = tab_idx(tn, 0, 0);
+        }
+        dmin = S.pair_dmin[e]; dmax = S.pair_dmax[e]; sn = S.pair_step_n[e]; key = S.pair_key + 2 * e;
+        int so = S.pair_step_off[e];
+        sd = S.pair_step_d + so; se = S.pair_step_e + so; skey = S.pair_stepkey + 2 * so;
+    }
+    const int flag = (sn == 0);
+    if (dbl_is_zero(dmin)) { *bad = 1; return -1; }
+    const int a1bond = a1 ? S.hb_bond[a1] : 0;
+    const bool warnable = !(kind == K_HB && a1bond == 0);
+    const long long kd = tkey(distance2);
+    if (kd < key[0]) {
+        o.lo = INFINIT; o.up = INFINIT; o.acc = INFINIT; o.lopot = 0; o.uppot = 0;
+        if (warnable) ++*warn;
+        return cs;
+    }
+    o.lo = dmin; o.lopot = 0;
+    const int col = neg ? 0 : 1;
+    for (int q = 0; q < sn; q++) {
+        double d = sd[q];
+        if (dbl_is_zero(d)) break;
+        if (kd < skey[2 * q + col]) {
+            o.up = d; o.uppot = -1 * se[q]; o.acc = 0;
+            if (q == 0) return 0;
+            if (kind == K_HB && q == sn - 1 && a1bond > 0) return 1;
+            return cs;
+        }
+        o.lo = d; o.lopot = se[q];
+    }
+    if (kind == K_HB && a1bond > 0) ++*warn;
+    if (dbl_pos(dmax)) {
+        if (kd < key[1]) {
+            o.up = dmax; o.uppot = 0; o.acc = 0;
+            cs = 1;
+            if (flag == 1 && neg) cs = 0;
+            return cs;
+        }
+        o.lo = INFINIT; o.up = INFINIT; o.acc = INFINIT; o.lopot = 0; o.uppot = 0;
+        if (warnable) ++*warn;
+    } else {
+        o.up = INFINIT; o.uppot = INFINIT; o.acc = INFINIT;
+        return 1;
+    }
+    return cs;
+}
+
+// pair_kin() with the target's position given (xi = lzx(i) per dimension)
+__device__ __forceinline__ void pair_kin_r(const DSys &S, const double *xi, int i, int j, Kin &k) {
+    const int ci[3] = {S.cx[i], S.cy[i], S.cz[i]}, cj[3] = {S.cx[j], S.cy[j], S.cz[j]};
+    const double *X[3] = {S.x, S.y, S.z}, *V[3] = {S.vx, S.vy, S.vz};
+    double r[3], v[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double xj = lzx(S, X[d], V[d], j);
+        // xj + 0.0 equals xj except for the sign of a zero, which no later result
+        // can observe (squares, and sums with the other terms), so it is skipped
+        if (ci[d] != cj[d]) {
+            if (ci[d] == 0 && cj[d] == S.cn[d] - 1) xj = xj + -1 * S.box[d];
+            else if (ci[d] == S.cn[d] - 1 && cj[d] == 0) xj = xj + S.box[d];
+        }
+        r[d] = xi[d] - xj;
+        v[d] = V[d][i] - V[d][j];
+    }
+    k.rx = r[0]; k.ry = r[1]; k.rz = r[2];
+    k.r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    k.b = r[0] * v[0] + r[1] * v[1] + r[2] * v[2];
+    k.v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+}
+// CalculateTime with the discriminant given (it is recomputed identically otherwise)
+__device__ __forceinline__ double root_d(const Kin &k, int st, double D) {
+    double s = sqrt(D);
+    return (-k.b + (st > 0 ? s : -s)) / k.v2;
+}
+
+__device__ void eval_bond_r(const DSys &S, const double *xi, int i, int q, Slots &L, int k) {
+    int j = S.bond_j[q];
+    int info = 0;
+    double tdup = 0;
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
+        info |= F_DUP; tdup = S.ev_time[j];
+    }
+    double lng = S.bond_dmax[q], sht = S.bond_dmin[q];
+    Kin kk; pair_kin_r(S, xi, i, j, kk);
+    const long long kb = tkey(kk.b);
+    const bool far = tkey(kk.r2 - lng) > KEY_ZERO;
+    int sub; double t;
+    if (far && kb >= 0) { sub = SDMD_SUB_WELL_BOUNCE; t = 1e-16 * i * j; }
+    else if (!far && tkey(sht - kk.r2) > KEY_ZERO && kb < 0) { sub = SDMD_SUB_CORE; t = 1e-16 * i * j; }
+    else {
+        double D1 = 0;
+        if (kb < 0) D1 = kk.b * kk.b - kk.v2 * (kk.r2 - sht);
+        if (kb < 0 && dbl_gt0(D1)) { sub = SDMD_SUB_CORE; t = root_d(kk, -1, D1); }
+        else { sub = SDMD_SUB_WELL_BOUNCE; t = root_d(kk, 1, kk.b * kk.b - kk.v2 * (kk.r2 - lng)); }
+        if (dbl_lt0(t)) t = INFINIT;
+    }
+    put(L, k, j, info | F_FRESH | (sub << 8), t, tdup, 0.0);
+}
+
+__device__ void eval_collision_r(const DSys &S, const double *xi, int i, int j, Slots &L, int k, int *bad) {
+    int info = 0, warn = 0, sub = SDMD_SUB_INVALID;
+    double tdup = 0, t = 0, pot = 0;
+    if (j == i) { put(L, k, j, -1, 0, 0, 0); return; }
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
+        info |= F_DUP; tdup = S.ev_time[j];
+    }
+    int bits = conn_bits_w(S, i, j);
+    if (!((bits & 1) || S.hb_bond[i] == j || nb_has(S, i, j))) {
+        Kin kk; pair_kin_r(S, xi, i, j, kk);
+        if (tkey(kk.r2) <= S.cut_key) {
+            const bool neg = tkey(kk.b) < 0;
+            Lim o; int cs; bool go = true;
+            const int constrained = bits & 2;
+            cs = find_pair_r(S, i, j, constrained ? K_CONSTRAINT : K_COLLISION, neg, kk.r2, o, &warn, bad);
+            if (!constrained && dbl_is_zero(o.lopot) && dbl_is_zero(o.uppot)) go = false;
+            if (go) {
+                double D1 = 0;
+                if (neg) D1 = kk.b * kk.b - kk.v2 * (kk.r2 - o.lo);
+                if (neg && dbl_gt0(D1)) {
+                    pot = o.lopot;
+                    sub = (cs == 0) ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
+                    t = root_d(kk, -1, D1);
+                    info |= F_FRESH;
+                } else {
+                    pot = o.uppot;
+                    if (constrained) sub = (cs == 1) ? SDMD_SUB_WELL_BOUNCE : SDMD_SUB_TBD_ESCAPE;
+                    else if (cs == 1) go = false;
+                    else sub = SDMD_SUB_TBD_ESCAPE;
+                    if (go) { t = root_d(kk, 1, kk.b * kk.b - kk.v2 * (kk.r2 - o.up)); info |= F_FRESH; }
+                }
+            }
+        }
+    }
+    put(L, k, j, info | (sub << 8) | (warn << 16), t, tdup, pot);
+}
+
+__device__ void eval_hb_scan_r(const DSys &S, const double *xi, int i, int j, Slots &L, int k, int *bad) {
+    if (!(i != j && hb_pair_ok(S, i, j) && S.hb_bond[j] == 0 &&
+          ((S.protein[i] == S.protein[j] && abs(S.aanum[i] - S.aanum[j]) >= 4) || S.protein[i] != S.protein[j]))) {
+        put(L, k, j, -1, 0, 0, 0);
+        return;
+    }
+    int info = 0, warn = 0;
+    double tdup = 0, t = 0, pot = 0;
+    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
+        info |= F_DUP; tdup = S.ev_time[j];
+    }
+    Kin kk; pair_kin_r(S, xi, i, j, kk);
+    if (tkey(kk.r2) <= S.cut_key && pair_match(S, i, j, bad) >= 0) {
+        Lim o;
+        const bool neg = tkey(kk.b) < 0;
+        int cs = find_pair_r(S, i, j, K_HB, neg, kk.r2, o, &warn, bad);
+        if (neg && cs == 1) {
+            double D1 = kk.b * kk.b - kk.v2 * (kk.r2 - o.lo);
+            if (dbl_gt0(D1)) {
+                pot = o.lopot;
+                t = root_d(kk, -1, D1);
+                if (dbl_lt0(t)) t = INFINIT;
+                info |= F_FRESH;
+            }
+        }
+    }
+    put(L, k, j, info | (SDMD_SUB_TBD_HBFORM << 8) | (warn << 16), t, tdup, pot);
+}
+
+// ---- HB-bonded partner: the fresh part of hb_bonded(), evaluated by a lane ------
+struct HbbOut { double t, pot; int sub, warn, bad, pos; };
+__device__ void hbb_fresh(const DSys &S, const double *xi, int i, HbbOut &r) {
+    int j = S.hb_bond[i];
+    Kin kk; pair_kin_r(S, xi, i, j, kk);
+    Lim o; int warn = 0, bad = 0;
+    const bool neg = tkey(kk.b) < 0;
+    int cs = find_pair_r(S, i, j, K_HB, neg, kk.r2, o, &warn, &bad);
+    int sub; double pot, t;
+    double D1 = 0;
+    if (neg) D1 = kk.b * kk.b - kk.v2 * (kk.r2 - o.lo);
+    if (neg && dbl_gt0(D1)) {
+        pot = o.lopot; sub = (cs == 0) ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
+        t = root_d(kk, -1, D1);
+    } else {
+        pot = o.uppot; sub = (cs == 1) ? SDMD_SUB_TBD_HBBREAK : SDMD_SUB_TBD_ESCAPE;
+        t = root_d(kk, 1, kk.b * kk.b - kk.v2 * (kk.r2 - o.up));
+    }
+    if (dbl_lt0(t)) t = INFINIT;
+    r.pos = tkey(t) > 0;
+    if (S.lazy) t = S.now + t;
     r.t = t; r.pot = pot; r.sub = sub; r.warn = warn; r.bad = bad;
+}
+
+// ---- per-cell atom arrays (screened path) --------------------------------------------
+// Cell c holds cell_cnt[c] atoms in cell_arr[c*maxc ...] in insertion order, so the
+// reference's list (head = most recently inserted, src/Events.c:158-200) reads
+// from the end.  Built from cell_list at kernel start, written back at the end.
+__device__ void cells_from_list(const DSys &S, Blk &B) {
+    const int N = S.n, M = S.maxc;
+    for (int c = 1 + threadIdx.x; c <= S.ncell; c += blockDim.x) {
+        int32_t *arr = S.cell_arr + (size_t)c * M;
+        int cnt = 0;
+        for (int a = S.cell_list[N + c]; a; a = S.cell_list[a]) {
+            if (cnt >= M) { set_err(B, SDMD_ECAPACITY, a); break; }
+            arr[cnt++] = a;
+        }
+        for (int k = 0; k < cnt / 2; k++) { int x = arr[k]; arr[k] = arr[cnt - 1 - k]; arr[cnt - 1 - k] = x; }
+        S.cell_cnt[c] = cnt;
+    }
+}
+__device__ void cells_to_list(const DSys &S) {
+    const int N = S.n, M = S.maxc;
+    for (int c = 1 + threadIdx.x; c <= S.ncell; c += blockDim.x) {
+        const int32_t *arr = S.cell_arr + (size_t)c * M;
+        const int cnt = S.cell_cnt[c];
+        S.cell_list[N + c] = cnt ? arr[cnt - 1] : 0;
+        for (int k = cnt - 1; k >= 0; k--) S.cell_list[arr[k]] = k ? arr[k - 1] : 0;
+    }
+}
+// LinkList("part") for one atom (remove from oldc, insert as newest of newc), one warp
+__device__ void cell_move_warp(const DSys &S, int t, int oldc, int newc, Blk &B) {
+    const int lane = threadIdx.x & 31, M = S.maxc;
+    int32_t *ao = S.cell_arr + (size_t)oldc * M;
+    const int cnt = S.cell_cnt[oldc];
+    int pos = -1;
+    for (int base = 0; base < cnt; base += 32) {
+        const int k = base + lane;
+        unsigned m = __ballot_sync(0xffffffffu, k < cnt && ao[k] == t);
+        if (m) { pos = base + __ffs(m) - 1; break; }
+    }
+    if (pos < 0) { if (lane == 0) set_err(B, SDMD_ELINK, t); __syncwarp(); return; }
+    for (int base = pos + 1; base < cnt; base += 32) {
+        const int k = base + lane;
+        const int v = k < cnt ? ao[k] : 0;
+        __syncwarp();
+        if (k < cnt) ao[k - 1] = v;
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (newc == oldc) ao[cnt - 1] = t;
+        else {
+            const int c2 = S.cell_cnt[newc];
+            S.cell_cnt[oldc] = cnt - 1;
+            if (c2 >= M) set_err(B, SDMD_ECAPACITY, t);
+            else { S.cell_arr[(size_t)newc * M + c2] = t; S.cell_cnt[newc] = c2 + 1; }
+        }
+    }
+    __syncwarp();
 }
 
 // ---- warp helpers ----------------------------------------------------------------
 // gather atom i's 27-cell neighbourhood into nbj[] in scan order with one warp
 __device__ int gather_warp(const DSys &S, int i, int32_t *nbj, int nbcap, int *overflow) {
-    const int lane = threadIdx.x & 31;
-    int head = 0, c = 0;
+    const int lane = threadIdx.x & 31, M = S.maxc;
+    int cell = 0, c = 0;
     if (lane < 27) {
-        head = S.cell_list[S.n + nb_cell(S, i, lane)];
-        for (int a = head; a; a = S.cell_list[a]) {
-            if (++c > S.n) break;
-        }
+        cell = nb_cell(S, i, lane);
+        c = S.cell_cnt[cell];
     }
     int incl = c;
 #pragma unroll
@@ -361,8 +653,9 @@ __device__ int gather_warp(const DSys &S, int i, int32_t *nbj, int nbcap, int *o
     int tot = __shfl_sync(0xffffffffu, incl, 31);
     if (tot > nbcap) { *overflow = 1; return 0; }
     if (lane < 27) {
-        int off = incl - c, m = 0;
-        for (int a = head; a && m < c; a = S.cell_list[a]) nbj[off + m++] = a;
+        const int32_t *arr = S.cell_arr + (size_t)cell * M;
+        const int off = incl - c;
+        for (int m = 0; m < c; m++) nbj[off + m] = arr[c - 1 - m];
     }
     __syncwarp();
     return tot;
@@ -431,6 +724,10 @@ struct PairScal {                 // per-atom block scalars of one two-atom pred
     int i[2], nb[2], nn[2], mode[2], E[2], rn[2], over[2], warn_excl[2];
     unsigned u_key[2], dup_key[2];
     float uprime[2], nowf;
+    double xi[2][3];              // lzx(i): the atom's FP64 position now
+    double pcc_abs[2], th_abs[2]; // PCC / thermostat offers as stored (absolute in lazy mode)
+    int pcc_pos[2], th_pos[2];    // the offer's time is > 0 (JobAssign's test)
+    int64_t smp0;                 // sample index of the target's thermostat draw
     PIv P[2];
     HbbOut hbb[2];
 };
@@ -472,6 +769,20 @@ __device__ __forceinline__ float key_f(unsigned k) {
     return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
 }
 
+// JobAssign (src/TimePrediction.c:1140-1158) for an offer whose stored time (absolute
+// in lazy mode) and positivity were computed beforehand by a lane
+__device__ __forceinline__ void job_assign_pre(const DSys &S, Cur &c, int j, double ts, int pos, double pot, int sub,
+                                               int type) {
+    if (!pos) return;
+    const long long kt = tkey(ts);
+    if (c.key > kt) {
+        c.potential = pot; c.sub = sub; c.time = ts; c.key = kt; c.type = type;
+        if (j) { c.partner = j; c.pcounter = S.ev_counter[j]; }
+        else c.partner = INVALID;
+    }
+}
+constexpr int F_POS = 4;   // slot flag: the fresh time is > 0 (set by the refine lane)
+
 // one refined offer of the fold (resolve() for a single slot); `tnew` is the
 // target atom whose fresh event may now duplicate this pair, or -1
 __device__ inline void fold_entry(const DSys &S, Cur &c, const Slots &L, int q, int i, int type, int tnew, Blk &B) {
@@ -487,7 +798,7 @@ __device__ inline void fold_entry(const DSys &S, Cur &c, const Slots &L, int q, 
     }
     if ((info & F_DUP) && dup_assign(S, c, j, tdup, type)) return;
     B.warn += (info >> 16) & 0xff;
-    if (info & F_FRESH) job_assign(S, c, j, L.t[q], L.pot[q], (info >> 8) & 0xff, type);
+    if (info & F_FRESH) job_assign_pre(S, c, j, L.t[q], info & F_POS, L.pot[q], (info >> 8) & 0xff, type);
 }
 
 // Predict's fold for atom a of the pair, in the reference's order (thread 0)
@@ -499,8 +810,14 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
     int q = 0, bad = 0;
     for (; q < rn && M.rl[a][q] < nb + nn; q++)
         fold_entry(S, c, L, q, i, M.rl[a][q] < nb ? SDMD_EV_BOND : SDMD_EV_COLLISION, tnew, B);
-    pcc_time(S, c, M.face + 3 * a);
-    thermostat_time(S, c, C, B);
+    job_assign_pre(S, c, 0, PS.pcc_abs[a], PS.pcc_pos[a], 0, SDMD_SUB_INVALID, SDMD_EV_PCC);
+    if (S.thermostat) {   // ThermostatTime: the sample was evaluated by a lane
+        if (C.smp_used >= C.smp_avail || C.smp_used != PS.smp0 + a) set_err(B, SDMD_ETIMEOUT, 0);
+        else {
+            C.smp_used++;
+            job_assign_pre(S, c, 0, PS.th_abs[a], PS.th_pos[a], 0, SDMD_SUB_INVALID, SDMD_EV_THERMOSTAT);
+        }
+    }
     S.hb_itype[i] = SDMD_HB_NOEVENT;    // HBSkip is one-shot (src/TimePrediction.c:309-327)
     if (PS.mode[a] == 1) {
         const int j = S.hb_bond[i];
@@ -509,7 +826,7 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
             const HbbOut &h = PS.hbb[a];
             B.warn += h.warn;
             if (h.bad) bad = 1;
-            job_assign(S, c, j, h.t, h.pot, h.sub, SDMD_EV_HB);
+            job_assign_pre(S, c, j, h.t, h.pos, h.pot, h.sub, SDMD_EV_HB);
         }
     } else if (PS.mode[a] == 2) {
         for (; q < rn; q++) fold_entry(S, c, L, q, i, SDMD_EV_HB, tnew, B);
@@ -526,7 +843,6 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
 __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, Blk &B, DScal &C) {
     const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
     const int na = p ? 2 : 1;
-    const double cut = [&] { double c = S.cutoff * 0.90; return c * c; }();
     // 1. per-atom set-up and the two 27-cell gathers (one warp each)
     if (tid < na) {
         const int a = tid, i = a ? p : t;
@@ -539,6 +855,7 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         PS.mode[a] = mode;
         PS.u_key[a] = f_key(INFINITY); PS.dup_key[a] = f_key(-INFINITY);
         PS.warn_excl[a] = 0; PS.rn[a] = 0; PS.over[a] = 0;
+        PS.xi[a][0] = lzx(S, S.x, S.vx, i); PS.xi[a][1] = lzx(S, S.y, S.vy, i); PS.xi[a][2] = lzx(S, S.z, S.vz, i);
         atom_piv(S, i, PS.P[a]);
     }
     for (int a = 0; a < na; a++) {
@@ -561,29 +878,32 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
     // 2. PCC faces (exact, FP64) and the FP32 screen of every bond / collision / HB candidate
     if (tid < 3 * na) M.face[tid] = pcc_face(S, PS.i[tid / 3], tid % 3);
     const int E0 = PS.E[0], E1 = na > 1 ? PS.E[1] : 0;
-    for (int g = tid; g < E0 + E1; g += T) {
-        const int a = g < E0 ? 0 : 1, e = a ? g - E0 : g, i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
-        Verdict v;
-        int j;
+    const int S0 = PS.nb[0] + PS.nn[0], S1 = na > 1 ? PS.nb[1] + PS.nn[1] : 0;
+    for (int g = tid; g < S0 + S1; g += T) {
+        const int a = g < S0 ? 0 : 1, e = a ? g - S0 : g, i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
+        Verdict v[2];
+        int j, ne = 1;
         if (e < nb) {
             const int qb = S.bond_off[i] + e;
             j = S.bond_j[qb];
-            screen_bond(S, i, qb, PS.P[a], v, a == 1 && j == t);
-        } else if (e < nb + nn) {
-            j = M.nbj[a][e - nb];
-            screen_coll(S, i, j, PS.P[a], v, a == 1 && j == t);
+            screen_bond(S, i, qb, PS.P[a], v[0], a == 1 && j == t);
         } else {
-            j = M.nbj[a][e - nb - nn];
-            screen_hbs(S, i, j, PS.P[a], v, a == 1 && j == t);
+            j = M.nbj[a][e - nb];
+            const bool hb = PS.mode[a] == 2;
+            screen_cell(S, i, j, PS.P[a], hb, a == 1 && j == t, v[0], v[1]);
+            ne = hb ? 2 : 1;
         }
-        M.stat[a][e] = (uint8_t)(v.st | (v.warn << 2));
-        M.tlo[a][e] = v.t.lo;
-        if (v.st == SC_OFFER && e < nb + nn) atomicMin(&PS.u_key[a], f_key(v.t.hi));
-        else if (v.st == SC_NONE && v.warn) atomicAdd(&PS.warn_excl[a], v.warn);
-        if (v.dup) {   // CheckDuplication may adopt j's stored time: it bounds what can matter
-            double d = S.ev_time[j];
-            if (S.lazy) d = d - S.now;
-            atomicMax(&PS.dup_key[a], f_key(ivd(d).hi));
+        for (int x = 0; x < ne; x++) {
+            const int ee = x ? e + nn : e;
+            M.stat[a][ee] = (uint8_t)(v[x].st | (v[x].warn << 2));
+            M.tlo[a][ee] = v[x].t.lo;
+            if (v[x].st == SC_OFFER && x == 0) atomicMin(&PS.u_key[a], f_key(v[x].t.hi));
+            else if (v[x].st == SC_NONE && v[x].warn) atomicAdd(&PS.warn_excl[a], v[x].warn);
+            if (v[x].dup) {   // CheckDuplication may adopt j's stored time: it bounds what can matter
+                double d = S.ev_time[j];
+                if (S.lazy) d = d - S.now;
+                atomicMax(&PS.dup_key[a], f_key(ivd(d).hi));
+            }
         }
     }
     __syncthreads();
@@ -655,11 +975,42 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
             const int e = M.rl[a][qq], i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
             const int kind = e < nb ? 1 : (e < nb + nn ? 0 : 2);
             if (kind % nw != warp) continue;
-            if (kind == 1) eval_bond(S, i, S.bond_off[i] + e, M.R[a], qq, &bad);
-            else if (kind == 0) eval_collision(S, i, M.nbj[a][e - nb], cut, M.R[a], qq, &bad);
-            else eval_hb_scan(S, i, M.nbj[a][e - nb - nn], cut, M.R[a], qq, &bad);
+            if (kind == 1) eval_bond_r(S, PS.xi[a], i, S.bond_off[i] + e, M.R[a], qq);
+            else if (kind == 0) eval_collision_r(S, PS.xi[a], i, M.nbj[a][e - nb], M.R[a], qq, &bad);
+            else eval_hb_scan_r(S, PS.xi[a], i, M.nbj[a][e - nb - nn], M.R[a], qq, &bad);
+            int info = M.R[a].info[qq];
+            if (info >= 0 && (info & F_FRESH)) {   // JobAssign's "> 0" test and the stored time
+                double tf = M.R[a].t[qq];
+                if (tkey(tf) > 0) info |= F_POS;
+                if (S.lazy) M.R[a].t[qq] = S.now + tf;
+                M.R[a].info[qq] = info;
+            }
         }
-        if (warp == 3 % nw && lane < na && PS.mode[lane] == 1 && !PS.over[lane]) hbb_fresh(S, PS.i[lane], PS.hbb[lane]);
+        // PCC (PBCandCrossCellTime) and thermostat offers of each atom, by lanes of the last warp
+        if (warp == nw - 1 && lane < 2 * na) {
+            const int a = lane >> 1;
+            if ((lane & 1) == 0) {
+                double best = INFINIT;
+                for (int d = 0; d < 3; d++) {
+                    double tf = M.face[3 * a + d];
+                    if (tkey(best) > tkey(tf) && tkey(tf) > 0) best = tf;
+                }
+                PS.pcc_pos[a] = tkey(best) > 0;
+                PS.pcc_abs[a] = S.lazy ? S.now + best : best;
+            } else if (S.thermostat) {
+                const int64_t q = C.smp_used + a;
+                double th = 0;
+                if (q < C.smp_avail) {
+                    double x = S.smp[q] * sqrt(1.0) + 0;
+                    th = S.thermo_freq * (x < 0 ? -x : x);
+                }
+                PS.th_pos[a] = tkey(th) > 0;
+                PS.th_abs[a] = S.lazy ? S.now + th : th;
+                if (a == 0) PS.smp0 = C.smp_used;
+            }
+        }
+        if (warp == 3 % nw && lane < na && PS.mode[lane] == 1 && !PS.over[lane])
+            hbb_fresh(S, PS.xi[lane], PS.i[lane], PS.hbb[lane]);
         if (bad) set_err(B, SDMD_EHBMAP, t);
     }
     __syncthreads();
