@@ -194,9 +194,11 @@ def run_ours(args, D):
     E = args.events_per_step
     host_copy = [s.copy() for s in systems]
 
-    from sdmd_gb300.engine import ADVANCE_EAGER, ADVANCE_LAZY
+    from sdmd_gb300.engine import ADVANCE_EAGER, ADVANCE_LAZY, SCREEN_FP32, SCREEN_FP64
     adv = ADVANCE_LAZY if args.advance == "lazy" else ADVANCE_EAGER
-    eng = Engine(systems, threads=args.threads, device=D.local, advance=adv)
+    scr = SCREEN_FP32 if args.screen == "fp32" else SCREEN_FP64
+    threads = args.threads or (256 if len(systems) == 1 else 64)
+    eng = Engine(systems, threads=threads, device=D.local, advance=adv, screen=scr)
     eng.prepare(full=True)
     sweep_ms = eng.last_ms()[0]
     eng.download()
@@ -212,12 +214,18 @@ def run_ours(args, D):
     eng.download()
     frame0 = sum(s.counters["frame"] for s in systems)
     step_ms = []
+    launches = loop_launches = 0
+    loop_ms = 0.0
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         eng.run(E)
         step_ms.append(eng.last_ms()[1])
+        a, b, c = eng.last_run_stats()
+        launches += a
+        loop_launches += b
+        loop_ms += c
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
     clk = clocks.stop()
@@ -241,7 +249,7 @@ def run_ours(args, D):
     for k in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        with Engine(work, threads=args.threads, device=D.local, advance=adv) as e2:
+        with Engine(work, threads=threads, device=D.local, advance=adv, screen=scr) as e2:
             e2.prepare(full=False)
             e2.run(E)
             e2.download()
@@ -256,15 +264,18 @@ def run_ours(args, D):
     per_event = 2 * P * 56 + 2 * 104 + 2 * logn * 12
     if args.advance == "eager":
         per_event += pops_per_event * after_sweep[0].n * 56   # every pop moves every atom and event time
-    bytes_per_launch = per_event * (events / max(args.steps, 1))
-    launch_s = t_dev / max(args.steps, 1)
+    kname = "loop_kernel_screen" if args.screen == "fp32" else "loop_kernel_fp64"
+    n_launch = max(loop_launches, 1)
+    bytes_per_launch = per_event * events / n_launch
+    launch_s = loop_ms / 1e3 / n_launch          # CUDA events around each event-loop launch
     peak, peak_kind = peaks()
     achieved = bytes_per_launch / launch_s / 1e9
-    traffic = load_traffic().get(f"loop_{args.workload}_bytes_per_event")
+    traffic = load_traffic().get(f"{kname}_{args.workload}_{args.advance}_dram_bytes_per_event")
     roof = {"bound": "hbm", "achieved": round(achieved, 3), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 6), "peak_kind": peak_kind,
-            "traffic": None if traffic is None else traffic * events / max(args.steps, 1),
-            "kernel": "loop_kernel_fp64", "bytes_per_event": round(per_event, 1), "P_candidates": round(P, 2)}
+            "traffic": None if traffic is None else round(traffic * events / n_launch, 1),
+            "kernel": kname, "launches": loop_launches, "bytes_per_event": round(per_event, 1),
+            "P_candidates": round(P, 2)}
     # the full-rebuild sweep (SURVEY 8d bytes) for reference
     s0 = after_sweep[0]
     ncell = int(np.prod(s0.scal["cellnum"]))
@@ -278,17 +289,18 @@ def run_ours(args, D):
 
     if D.rank == 0:
         cfg.update({"n_atoms": natoms, "n_systems": len(systems) * D.world, "events_per_step": E,
-                    "l2": "flushed between steps (256 MiB write)", "advance": args.advance, "screen": "fp64",
-                    "threads_per_system": args.threads or 128, "replicas": "independent per rank" if D.world > 1 else None})
+                    "l2": "flushed between steps (256 MiB write)", "advance": args.advance, "screen": args.screen,
+                    "threads_per_system": threads, "replicas": "independent per rank" if D.world > 1 else None})
         line = {"metric": METRIC, "value": round(value, 3), "unit": "events/s", "n_gpus": D.world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_max * 1e3 / args.steps, 3),
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32+f64" if args.screen == "fp32" else "f64",
                 "data": "synthetic (seeded random-sequence peptides, bundled Library_Ding force field)",
                 "config": cfg,
                 "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "h2d_bytes_per_step": st_b + dy_b,
                         "d2h_bytes_per_step": dy_b},
                 "roofline": roof, "sweep": sweep, "cpu_baseline": cpu, "clocks": clk,
-                "gpu_launches": args.steps * 1, "wall_s_timed": round(wall, 3)}
+                "gpu_launches": launches, "wall_s_timed": round(wall, 3)}
         print(json.dumps(line))
 
 
@@ -357,6 +369,7 @@ def main():
     ap.add_argument("--events-per-step", type=int, default=20000)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--advance", choices=["eager", "lazy"], default="lazy")
+    ap.add_argument("--screen", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

@@ -217,6 +217,11 @@ int  sdmd_gpu_last_ms(sdmd_gpu *h, double *prepare_ms, double *run_ms);
 
 int  sdmd_gpu_last_error(sdmd_gpu *h, sdmd_error_info *info);
 
+/* Kernels launched by the last sdmd_gpu_run (all of them, and event-loop kernels
+ * alone) and the device time (ms) of the event-loop kernels alone, measured with
+ * CUDA events around each of those launches. */
+int  sdmd_gpu_last_run_stats(sdmd_gpu *h, int64_t *launches, int64_t *loop_launches, double *loop_ms);
+
 /* ---- allocation-free re-sweep ------------------------------------------------
  * No counterpart in the reference (its Prepare() allocates nothing on a GPU).
  *

@@ -38,6 +38,9 @@ struct sdmd_gpu {
     void (*sweep_k)(const DSys *, int) = nullptr;            // plain FP64 or FP32-screened kernels
     void (*loop_k)(const DSys *, double, int) = nullptr;
     double prep_ms = 0, run_ms = 0;
+    cudaEvent_t l0 = nullptr, l1 = nullptr;        // around each loop-kernel launch
+    double loop_ms = 0;                            // loop-kernel time of the last run
+    int64_t launches = 0, loop_launches = 0;       // kernels launched by the last run
     sdmd_error_info err{};
 };
 
@@ -395,6 +398,8 @@ extern "C" void sdmd_gpu_destroy(sdmd_gpu *h) {
     if (h->ds) cudaFree(h->ds);
     if (h->e0) cudaEventDestroy(h->e0);
     if (h->e1) cudaEventDestroy(h->e1);
+    if (h->l0) cudaEventDestroy(h->l0);
+    if (h->l1) cudaEventDestroy(h->l1);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -474,6 +479,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     h->arena_bytes = layout(h, systems, nullptr, nullptr) + 256;
     if ((r = cuda_fail(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) ||
         (r = cuda_fail(cudaEventCreate(&h->e0))) || (r = cuda_fail(cudaEventCreate(&h->e1))) ||
+        (r = cuda_fail(cudaEventCreate(&h->l0))) || (r = cuda_fail(cudaEventCreate(&h->l1))) ||
         (r = cuda_fail(cudaMalloc(&h->arena, h->arena_bytes))) ||
         (r = cuda_fail(cudaMalloc(&h->ds, sizeof(DSys) * n_systems)))) {
         sdmd_gpu_destroy(h);
@@ -566,14 +572,22 @@ extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
     // is moved past the consumed draws; systems without a thermostat need one round
     std::vector<DScal> sc(h->n_systems);
     int64_t want = std::min<int64_t>(4 * max_events + 64, 1 << 16);
+    h->launches = 1; h->loop_launches = 0; h->loop_ms = 0;
     for (int round = 0; round < 1 << 20; round++) {
         launch_samples(h, want);
+        CK(cudaEventRecord(h->l0, h->stream));
         h->loop_k<<<h->n_systems, h->threads, h->smem_loop, h->stream>>>(h->ds, t_end, h->staged);
+        CK(cudaEventRecord(h->l1, h->stream));
         samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
         CK(cudaGetLastError());
+        h->launches += 4;
+        h->loop_launches += 1;
         for (int k = 0; k < h->n_systems; k++)
             CK(cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
+        float lms = 0;
+        cudaEventElapsedTime(&lms, h->l0, h->l1);
+        h->loop_ms += lms;
         bool again = false;
         for (auto &c : sc) if (c.paused && !c.err) again = true;
         if (!again) break;
@@ -646,6 +660,14 @@ extern "C" int sdmd_gpu_last_ms(sdmd_gpu *h, double *prepare_ms, double *run_ms)
     if (!h) return SDMD_EINVAL;
     if (prepare_ms) *prepare_ms = h->prep_ms;
     if (run_ms) *run_ms = h->run_ms;
+    return SDMD_OK;
+}
+
+extern "C" int sdmd_gpu_last_run_stats(sdmd_gpu *h, int64_t *launches, int64_t *loop_launches, double *loop_ms) {
+    if (!h) return SDMD_EINVAL;
+    if (launches) *launches = h->launches;
+    if (loop_launches) *loop_launches = h->loop_launches;
+    if (loop_ms) *loop_ms = h->loop_ms;
     return SDMD_OK;
 }
 

@@ -21,7 +21,7 @@ SCREEN_FP64, SCREEN_FP32 = 0, 1
 ABI_FUNCS = ["sdmd_gpu_abi_version", "sdmd_gpu_device_count", "sdmd_gpu_strerror", "sdmd_gpu_create",
              "sdmd_gpu_destroy", "sdmd_gpu_prepare", "sdmd_gpu_run", "sdmd_gpu_download", "sdmd_gpu_trace",
              "sdmd_gpu_last_ms", "sdmd_gpu_last_error", "sdmd_rng_seed", "sdmd_rng_next", "sdmd_rng_skip",
-             "sdmd_gpu_prepare_noalloc"]
+             "sdmd_gpu_prepare_noalloc", "sdmd_gpu_last_run_stats"]
 
 _lib = None
 
@@ -57,6 +57,7 @@ def lib():
         L.sdmd_gpu_trace.argtypes = [C.c_void_p, C.c_int32, P(sdmd_trace_rec), C.c_int32, P(C.c_int32)]
         L.sdmd_gpu_last_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.sdmd_gpu_last_error.argtypes = [C.c_void_p, P(sdmd_error_info)]
+        L.sdmd_gpu_last_run_stats.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_double)]
         L.sdmd_rng_seed.argtypes = [P(sdmd_rng), C.c_uint32]
         L.sdmd_rng_seed.restype = None
         L.sdmd_rng_next.argtypes = [P(sdmd_rng)]
@@ -129,6 +130,12 @@ class Engine:
         a, b = C.c_double(0), C.c_double(0)
         lib().sdmd_gpu_last_ms(self.h, C.byref(a), C.byref(b))
         return a.value, b.value
+
+    def last_run_stats(self):
+        """(kernels launched, event-loop kernels launched, event-loop kernel ms) of the last run."""
+        a, b, c = C.c_int64(0), C.c_int64(0), C.c_double(0)
+        lib().sdmd_gpu_last_run_stats(self.h, C.byref(a), C.byref(b), C.byref(c))
+        return a.value, b.value, c.value
 
     def close(self):
         if getattr(self, "h", None):
