@@ -32,7 +32,7 @@ struct sdmd_gpu {
     unsigned char *arena = nullptr;
     size_t arena_bytes = 0;
     int threads = 128;
-    size_t smem = 0, smem_loop = 0;
+    size_t smem = 0, smem_loop = 0, vsmem = 0;
     int staged = 0;
     std::vector<int32_t> smp_cap_of;
     void (*sweep_k)(const DSys *, int) = nullptr;            // plain FP64 or FP32-screened kernels
@@ -179,7 +179,24 @@ struct Screen32 {
     std::vector<float> pair_thr, pair_step, con_thr, con_step, bond;
     std::vector<long long> pair_key, pair_stepkey, con_key, con_stepkey;
     std::vector<int32_t> conn_win;
+    std::vector<int32_t> leaf0;   // CreateCBT's leaf of every atom (src/CBT.c:16-30)
 };
+
+// The leaf each atom gets from CreateCBT: atoms are inserted in order 1..N and
+// each insertion splits the leaf at position `count` into (old atom, new atom).
+// The layout depends on N alone; atom 1 of a one-atom tree keeps leaf 0.
+static void cbt_leaf_layout(int N, std::vector<int32_t> &leaf) {
+    leaf.assign((size_t)N + 2, 0);
+    std::vector<int32_t> node((size_t)2 * N + 2, 0);
+    int count = 0;
+    for (int a = 1; a <= N; a++) {
+        if (count == 0) { node[1] = a; count = 1; continue; }
+        int i = node[count];
+        node[2 * count] = i; node[2 * count + 1] = a;
+        leaf[i] = 2 * count; leaf[a] = 2 * count + 1;
+        count++;
+    }
+}
 
 // the device's tkey(): an order-preserving map of non-NaN doubles onto int64
 static long long host_tkey(double d) {
@@ -189,6 +206,7 @@ static long long host_tkey(double d) {
 }
 constexpr int kConnWin = 9;   // ints per atom in conn_win
 constexpr int kMaxPerCell = 64; // screened path: atoms per cell array
+constexpr int kResidentBlocks = 608; // parallel sweep: blocks in flight (4 per SM of 152)
 
 // brackets of every FP64 threshold the prediction compares against, computed with
 // the same FP64 operations as the device (d + ZERO, d - ZERO, dmin - ZERO, dmax + ZERO)
@@ -239,6 +257,7 @@ static void build_screen32(const sdmd_system &s, Screen32 &o) {
         o.con_stepkey[2 * (size_t)k + 1] = host_tkey(s.con_step_d[k] - SDMD_ZERO);
     }
     const int N = s.n_atoms;
+    cbt_leaf_layout(N, o.leaf0);
     o.conn_win.assign((size_t)(N + 1) * kConnWin, 0);
     for (int i = 1; i <= N; i++) {
         int32_t *w = &o.conn_win[(size_t)i * kConnWin];
@@ -326,7 +345,11 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
         d.con_key = cv.take<long long>(((size_t)m.n_cons + 1) * 2);
         d.con_stepkey = cv.take<long long>(((size_t)m.n_con_steps + 1) * 2);
         d.conn_win = cv.take<int32_t>(N1 * kConnWin);
+        d.cbt_leaf0 = cv.take<int32_t>(N1 + 1);
         if (h->opts.screen == SDMD_SCREEN_FP32) {
+            d.sw_hbit = cv.take<int32_t>(N1);
+            d.sw_flag = cv.take<int32_t>(N1);
+            d.sw_warn = cv.take<int32_t>(N1);
             d.maxc = std::min<int32_t>(kMaxPerCell, m.n);
             d.cell_cnt = cv.take<int32_t>((size_t)m.ncell + 1);
             d.cell_arr = cv.take<int32_t>(((size_t)m.ncell + 1) * d.maxc);
@@ -343,6 +366,7 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             put(*copies, (long long *)d.con_key, q.con_key.data(), q.con_key.size());
             put(*copies, (long long *)d.con_stepkey, q.con_stepkey.data(), q.con_stepkey.size());
             put(*copies, (int32_t *)d.conn_win, q.conn_win.data(), q.conn_win.size());
+            put(*copies, (int32_t *)d.cbt_leaf0, q.leaf0.data(), q.leaf0.size());
         }
         if (copies) {
             auto &c = *copies;
@@ -453,6 +477,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         d.nbcap = m.nbcap;
         d.n_bonds = s.n_bonds; d.n_cons = s.n_cons; d.n_con_steps = s.n_con_steps; d.n_conn = s.n_conn;
         d.screen = h->opts.screen;
+        d.dup_limit = 0x7fffffff;
         double cut = s.cutoff * 0.90;   // the prediction's scan radius, as the device computes it
         cut *= cut;
         f32_bracket(cut, d.cut32);
@@ -463,6 +488,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     const bool scr = h->opts.screen == SDMD_SCREEN_FP32;
     h->smem = scr ? screen_smem_bytes(nbcap_max) : fp64_smem_bytes(nbcap_max);
     h->sweep_k = scr ? sweep_kernel_screen : sweep_kernel_fp64;
+    h->vsmem = verify_smem_bytes(nbcap_max, 4);
     h->loop_k = scr ? loop_kernel_screen : loop_kernel_fp64;
     // stage whole systems in shared memory when they fit (small systems, batches)
     size_t st_max = 0;
@@ -506,7 +532,13 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     if ((r = cuda_fail(cudaFuncSetAttribute(h->sweep_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             (int)h->smem))) ||
         (r = cuda_fail(cudaFuncSetAttribute(h->loop_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)h->smem_loop)))) {
+                                            (int)h->smem_loop))) ||
+        (scr && ((r = cuda_fail(cudaFuncSetAttribute(sweep_predict_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)h->smem))) ||
+                 (r = cuda_fail(cudaFuncSetAttribute(sweep_fix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)h->smem))) ||
+                 (r = cuda_fail(cudaFuncSetAttribute(sweep_verify_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)h->vsmem)))))) {
         sdmd_gpu_destroy(h);
         return r;
     }
@@ -552,7 +584,23 @@ extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
     for (auto &m : h->meta) nmax = std::max(nmax, m.n);
     CK(cudaEventRecord(h->e0, h->stream));
     if (full_predict) launch_samples(h, (int64_t)nmax + 8);
-    h->sweep_k<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+    if (h->opts.screen == SDMD_SCREEN_FP32) {
+        // parallel sweep: reset + cell arrays, every atom at once, duplicate check,
+        // in-order fix-up and the event tree
+        const unsigned ns = (unsigned)h->n_systems;
+        if (full_predict) {
+            const int per_sys = std::max(1, kResidentBlocks / h->n_systems);
+            const unsigned rx = (unsigned)std::max(1, std::min(per_sys, (nmax + 255) / 256));
+            const unsigned px = (unsigned)std::max(1, std::min(per_sys, nmax));
+            const unsigned vx = (unsigned)std::max(1, std::min(per_sys, (nmax + 3) / 4));
+            sweep_reset_kernel<<<dim3(rx, ns), 256, 0, h->stream>>>(h->ds);
+            sweep_predict_kernel<<<dim3(px, ns), h->threads, h->smem, h->stream>>>(h->ds);
+            sweep_verify_kernel<<<dim3(vx, ns), 128, h->vsmem, h->stream>>>(h->ds);
+        }
+        sweep_fix_kernel<<<ns, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+    } else {
+        h->sweep_k<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+    }
     if (full_predict) samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
     CK(cudaGetLastError());
     CK(cudaEventRecord(h->e1, h->stream));

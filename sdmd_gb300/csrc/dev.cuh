@@ -28,6 +28,8 @@ struct DScal {
     sdmd_rng rng0;           // state at the start of the current sample batch
     int64_t smp_avail, smp_used;
     int64_t target_frame;    // the run stops once c.frame reaches it
+    int32_t sw_nflag;        // parallel sweep: atoms left for the in-order re-prediction
+    int32_t pad;
 };
 
 // one system's device arrays (all 1-based per-atom arrays, entry 0 unused)
@@ -93,7 +95,16 @@ struct DSys {
     // reference's list head is the last entry); authoritative inside the screened
     // kernels, which rebuild cell_list from them before they return
     int32_t *cell_cnt, *cell_arr;
-    int32_t maxc, pad5;
+    int32_t maxc;
+    // CheckDuplication only considers partners j < dup_limit: INT32_MAX in the event
+    // loop; the parallel full-rebuild sweep lowers it (0 while every atom is
+    // predicted at once, i while atom i is re-predicted in atom order)
+    int32_t dup_limit;
+    // the CBT leaf layout CreateCBT produces for N atoms (it depends on N only)
+    const int32_t *cbt_leaf0;
+    // parallel full-rebuild sweep scratch: pre-sweep HB interaction type, and the
+    // atoms whose adopted duplicate differs from their own fresh offer
+    int32_t *sw_hbit, *sw_flag, *sw_warn;
 };
 
 // position component of atom j at the current time (lazy mode extrapolates)

@@ -20,6 +20,13 @@ size_t screen_smem_bytes(int nbcap);
 __global__ void sweep_kernel_screen(const DSys *systems, int full);
 __global__ void loop_kernel_screen(const DSys *systems, double t_end_override, int staged);
 
+// parallel full-rebuild sweep of the screened path (sweep_par.cuh)
+size_t verify_smem_bytes(int nbcap, int warps);
+__global__ void sweep_reset_kernel(const DSys *systems);
+__global__ void sweep_predict_kernel(const DSys *systems);
+__global__ void sweep_verify_kernel(const DSys *systems);
+__global__ void sweep_fix_kernel(const DSys *systems, int full);
+
 // thermostat sample stream (samples.cu)
 __global__ void samples_walk_kernel(const DSys *systems, int n_systems, int64_t want);
 __global__ void samples_values_kernel(const DSys *systems, int64_t want);

@@ -96,7 +96,7 @@ __device__ void eval_bond(const DSys &S, int i, int q, Slots &L, int k, int *bad
     int j = S.bond_j[q];
     int info = 0;
     double tdup = 0;
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
         info |= F_DUP; tdup = S.ev_time[j];
     }
     double lng = S.bond_dmax[q], sht = S.bond_dmin[q];
@@ -119,7 +119,7 @@ __device__ void eval_collision(const DSys &S, int i, int j, double cut, Slots &L
     int info = 0, warn = 0, sub = SDMD_SUB_INVALID;
     double tdup = 0, t = 0, pot = 0;
     if (j == i) { put(L, k, j, -1, 0, 0, 0); return; }   // -1: not a candidate at all
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
         info |= F_DUP; tdup = S.ev_time[j];
     }
     int bits = conn_bits(S, i, j);
@@ -178,7 +178,7 @@ __device__ void eval_hb_scan(const DSys &S, int i, int j, double cut, Slots &L, 
     }
     int info = 0, warn = 0;
     double tdup = 0, t = 0, pot = 0;
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
         info |= F_DUP; tdup = S.ev_time[j];
     }
     Kin kk; pair_kin(S, i, j, kk);
@@ -281,7 +281,7 @@ __device__ void thermostat_time(const DSys &S, Cur &c, DScal &C, Blk &B) {
 // HBTime for an HB-bonded atom (src/TimePrediction.c:329-387)
 __device__ void hb_bonded(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     int j = S.hb_bond[i];
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
         dup_assign(S, c, j, S.ev_time[j], SDMD_EV_HB))
         return;
     Kin kk; pair_kin(S, i, j, kk);
@@ -305,7 +305,7 @@ __device__ void hbnb_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     for (int n = 1; n <= S.nb_status[i]; n++) {
         int j = S.nb_partner[4 * i + n - 1];
         if (flag == 0) S.nb_pnum[i] = n;
-        if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HBNEIGHBOR && S.ev_pcounter[j] == S.ev_counter[i] &&
+        if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HBNEIGHBOR && S.ev_pcounter[j] == S.ev_counter[i] &&
             dup_assign(S, c, j, S.ev_time[j], SDMD_EV_HBNEIGHBOR)) {
             S.nb_pnum[i] = n; flag = 1; continue;
         }
@@ -726,6 +726,7 @@ __device__ inline void carve(Shm &M, int nbcap) {
 
 }  // namespace sdmd
 #include "screen.cuh"
+#include "sweep_par.cuh"
 namespace sdmd {
 
 // ---- whole-system staging in shared memory ------------------------------------
@@ -1028,6 +1029,7 @@ __global__ void loop_kernel_screen(const DSys *systems, double t_end_override, i
 }
 
 size_t screen_smem_bytes(int nbcap) { return screen_smem_bytes_dev(nbcap); }
+size_t verify_smem_bytes(int nbcap, int warps) { return verify_warp_bytes(nbcap) * (size_t)warps; }
 
 }  // namespace sdmd
 

@@ -230,7 +230,7 @@ __device__ bool fp_screen(const DSys &S, int a1, int a2, int kind, int neg, Iv r
 __device__ void screen_bond(const DSys &S, int i, int q, const PIv &I, Verdict &v, int always_refine) {
     v.warn = 0; v.dup = 0;
     int j = S.bond_j[q];
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
         v.st = SC_REFINE; v.dup = 1; return;
     }
     if (always_refine) { v.st = SC_REFINE; return; }
@@ -297,13 +297,13 @@ __device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, bool hb, 
     vh.warn = 0; vh.dup = 0; vh.st = SC_NONE;
     if (j == i) return;
     bool need_c = true;
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
         vc.st = SC_REFINE; vc.dup = 1; need_c = false;
     } else if (always) { vc.st = SC_REFINE; need_c = false; }
     bool need_h = hb && hb_pair_ok(S, i, j) && S.hb_bond[j] == 0 &&
                   ((S.protein[i] == S.protein[j] && abs(S.aanum[i] - S.aanum[j]) >= 4) || S.protein[i] != S.protein[j]);
     if (need_h) {
-        if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
+        if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
             vh.st = SC_REFINE; vh.dup = 1; need_h = false;
         } else if (always) { vh.st = SC_REFINE; need_h = false; }
     }
@@ -468,7 +468,7 @@ __device__ void eval_bond_r(const DSys &S, const double *xi, int i, int q, Slots
     int j = S.bond_j[q];
     int info = 0;
     double tdup = 0;
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
         info |= F_DUP; tdup = S.ev_time[j];
     }
     double lng = S.bond_dmax[q], sht = S.bond_dmin[q];
@@ -492,7 +492,7 @@ __device__ void eval_collision_r(const DSys &S, const double *xi, int i, int j, 
     int info = 0, warn = 0, sub = SDMD_SUB_INVALID;
     double tdup = 0, t = 0, pot = 0;
     if (j == i) { put(L, k, j, -1, 0, 0, 0); return; }
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
         info |= F_DUP; tdup = S.ev_time[j];
     }
     int bits = conn_bits_w(S, i, j);
@@ -533,7 +533,7 @@ __device__ void eval_hb_scan_r(const DSys &S, const double *xi, int i, int j, Sl
     }
     int info = 0, warn = 0;
     double tdup = 0, t = 0, pot = 0;
-    if (S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
+    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
         info |= F_DUP; tdup = S.ev_time[j];
     }
     Kin kk; pair_kin_r(S, xi, i, j, kk);
@@ -792,7 +792,7 @@ __device__ inline void fold_entry(const DSys &S, Cur &c, const Slots &L, int q, 
     double tdup = L.tdup[q];
     if (j == tnew) {   // CheckDuplication sees the target's new event
         info &= ~F_DUP;
-        if (S.ev_partner[j] == i && S.ev_type[j] == type && S.ev_pcounter[j] == S.ev_counter[i]) {
+        if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == type && S.ev_pcounter[j] == S.ev_counter[i]) {
             info |= F_DUP; tdup = S.ev_time[j];
         }
     }
@@ -821,7 +821,7 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
     S.hb_itype[i] = SDMD_HB_NOEVENT;    // HBSkip is one-shot (src/TimePrediction.c:309-327)
     if (PS.mode[a] == 1) {
         const int j = S.hb_bond[i];
-        if (!(S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
+        if (!(j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
               dup_assign(S, c, j, S.ev_time[j], SDMD_EV_HB))) {
             const HbbOut &h = PS.hbb[a];
             B.warn += h.warn;
