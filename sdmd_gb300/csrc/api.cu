@@ -206,7 +206,7 @@ static long long host_tkey(double d) {
 }
 constexpr int kConnWin = 9;   // ints per atom in conn_win
 constexpr int kMaxPerCell = 64; // screened path: atoms per cell array
-constexpr int kResidentBlocks = 608; // parallel sweep: blocks in flight (4 per SM of 152)
+constexpr int kResidentBlocks = 1216; // parallel sweep: blocks in flight (8 per SM of 152)
 
 // brackets of every FP64 threshold the prediction compares against, computed with
 // the same FP64 operations as the device (d + ZERO, d - ZERO, dmin - ZERO, dmax + ZERO)
@@ -594,7 +594,8 @@ extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
             const unsigned px = (unsigned)std::max(1, std::min(per_sys, nmax));
             const unsigned vx = (unsigned)std::max(1, std::min(per_sys, (nmax + 3) / 4));
             sweep_reset_kernel<<<dim3(rx, ns), 256, 0, h->stream>>>(h->ds);
-            sweep_predict_kernel<<<dim3(px, ns), h->threads, h->smem, h->stream>>>(h->ds);
+            // latency-bound single-atom predictions: small blocks keep 4 of them per SM
+            sweep_predict_kernel<<<dim3(px, ns), 64, h->smem, h->stream>>>(h->ds);
             sweep_verify_kernel<<<dim3(vx, ns), 128, h->vsmem, h->stream>>>(h->ds);
         }
         sweep_fix_kernel<<<ns, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);

@@ -14,7 +14,8 @@
 //      fields).  Atoms with any other duplicate are flagged;
 //   3. one block re-predicts the flagged atoms in atom order with
 //      CheckDuplication limited to j < i, exactly as the reference would; if a
-//      result changes, every later atom of its 27-cell neighbourhood is flagged too.
+//      result changes, the later atom its new event names is checked the same way
+//      and flagged when its own offer differs.
 // The thermostat draws its i-th sample for atom i in every phase, as the
 // sequential sweep does.  The event tree is then built bottom-up over CreateCBT's
 // leaf layout (src/CBT.c:16-30): with every time fixed, CreateCBT's incremental
@@ -179,6 +180,37 @@ __global__ void sweep_verify_kernel(const DSys *systems) {
     }
 }
 
+// After atom a's re-prediction changed its event: does the new event, which may
+// name a later atom k as partner, differ from the fresh offer k's own prediction
+// makes for a?  (Only a's new partner can see a new duplicate; an atom that the
+// old event named is correct without it, or was flagged already.)  One lane.
+__device__ bool new_partner_differs(const DSys &S, int a, int k, Slots &L) {
+    const int ty = S.ev_type[a];
+    if (!names(S, a, k, ty)) return false;
+    double xk[3] = {lzx(S, S.x, S.vx, k), lzx(S, S.y, S.vy, k), lzx(S, S.z, S.vz, k)};
+    int bad = 0;
+    if (ty == SDMD_EV_BOND) {
+        for (int q = S.bond_off[k]; q < S.bond_off[k + 1]; q++) {
+            if (S.bond_j[q] == a) { eval_bond_r(S, xk, k, q, L, 0); return !same_offer(S, L, 0, a); }
+        }
+        return true;
+    }
+    if (ty == SDMD_EV_COLLISION) {
+        eval_collision_r(S, xk, k, a, L, 0, &bad);
+        return bad || !same_offer(S, L, 0, a);
+    }
+    if (ty == SDMD_EV_HB) {
+        int mode;
+        if (S.sw_hbit[k] == SDMD_HB_SKIP) mode = 0;
+        else if (S.hb_bond[k] > 0) mode = 1;
+        else { int r = S.hb_role[k]; mode = (r == 'A' || r == 'D' || r == 'S') ? 2 : 0; }
+        if (mode == 2) { eval_hb_scan_r(S, xk, k, a, L, 0, &bad); return bad || !same_offer(S, L, 0, a); }
+        return mode == 1 && S.hb_bond[k] == a;
+    }
+    if (ty == SDMD_EV_HBNEIGHBOR) return nb_has(S, k, a) != 0;
+    return false;
+}
+
 // 3. in-order re-prediction of the flagged atoms, then the event tree (one block per system)
 __global__ void sweep_fix_kernel(const DSys *systems, int full) {
     __shared__ DSys S;
@@ -229,16 +261,11 @@ __global__ void sweep_fix_kernel(const DSys *systems, int full) {
                               o_pc != S.ev_pcounter[a];
                 }
                 __syncthreads();
-                if (changed && tid < 32) {   // later atoms that may see a as a duplicate
-                    int ovf = 0;
-                    const int nn = gather_warp(S, a, MS.nbj[0], S.nbcap, &ovf);
-                    if (ovf && tid == 0) set_err(B, SDMD_ECAPACITY, a);
-                    for (int k = tid; k < nn; k += 32) {
-                        const int j = MS.nbj[0][k];
-                        if (j > a) {
-                            S.sw_flag[j] = 1;
-                            if (j < i0 + T) chunk[j - i0] = 1;
-                        }
+                if (changed && tid == 0) {   // the later atom a's new event names may now see a duplicate
+                    const int k = S.ev_partner[a];
+                    if (k > a && new_partner_differs(S, a, k, MS.R[0])) {
+                        S.sw_flag[k] = 1;
+                        if (k < i0 + T) chunk[k - i0] = 1;
                     }
                 }
                 __syncthreads();
