@@ -217,6 +217,31 @@ int  sdmd_gpu_last_ms(sdmd_gpu *h, double *prepare_ms, double *run_ms);
 
 int  sdmd_gpu_last_error(sdmd_gpu *h, sdmd_error_info *info);
 
+/* Potential (CalPotenE, src/ToolFunctions.c:659-752) and kinetic (CalKinetE,
+ * :626-657) energy of every system, in the reference's summation order. */
+int  sdmd_gpu_energies(sdmd_gpu *h, double *pot, double *kin);
+
+/* ---- replica exchange (REMDRun, src/REMD.c:29-126; rearrange, src/Server.c:145-192).
+ * Every system of the handle is a replica.  After each replica reaches the exchange
+ * point -- every_events executed events (every_events > 0), or else the first
+ * executed event at time >= the next multiple of every_time (the reference's
+ * trigger) -- its CalPotenE is computed and one rearrange() pass over replicas with
+ * neighbouring ladder indices swaps (num, T) records with the Metropolis test
+ * exp(-(1/T_i - 1/T_j)(E_j - E_i)) against the server's rand() stream.  Each replica's
+ * thermostat target becomes its new T.  Runs until n_exchanges exchanges are done or
+ * a replica reaches t_end (<= 0: its own t_end). */
+typedef struct sdmd_remd {
+    int32_t *num;                  /* REMDTempStr.num of each replica (ladder index), in/out */
+    double  *T;                    /* REMDTempStr.T of each replica (reduced), in/out */
+    double  *E;                    /* out (may be NULL): CalPotenE at the last exchange */
+    int64_t  every_events;         /* > 0: exchange every this many executed events per replica */
+    double   every_time;           /* else: the reference's time trigger (ExchangeRate) */
+    sdmd_rng rng;                  /* the exchange server's rand() state, in/out */
+    int64_t  attempted, accepted;  /* cumulative pair attempts / swaps, in/out */
+    int64_t  exchanges_done;       /* out */
+} sdmd_remd;
+int  sdmd_gpu_run_remd(sdmd_gpu *h, int64_t n_exchanges, double t_end, sdmd_remd *remd);
+
 /* Kernels launched by the last sdmd_gpu_run (all of them, and event-loop kernels
  * alone) and the device time (ms) of the event-loop kernels alone, measured with
  * CUDA events around each of those launches. */

@@ -55,6 +55,9 @@ def lib():
         _lib.oracle_log.argtypes = [C.c_double]
         _lib.oracle_log.restype = C.c_double
         _lib.oracle_remd_rearrange.argtypes = [C.c_int32, P(C.c_int32), P(C.c_double), P(C.c_double), P(sdmd_rng)]
+        _lib.oracle_run_until.argtypes = [C.c_void_p, C.c_double, C.c_double, P(C.c_int64)]
+        _lib.oracle_potential_energy_counted.argtypes = [P(sdmd_system)]
+        _lib.oracle_potential_energy_counted.restype = C.c_double
     return _lib
 
 
@@ -83,6 +86,21 @@ class Loop:
                               tr.ctypes.data_as(C.POINTER(sdmd_trace_rec)), int(trace_cap), C.byref(n))
         self.system.pull_scalars(self.st)
         return rc, tr[:min(n.value, trace_cap)], n.value
+
+    def run_until(self, stop_time, t_end=None):
+        """Run until the first executed event at time >= stop_time (REMDRun's exchange point)."""
+        if t_end is None:
+            t_end = self.st.t_end
+        n = C.c_int64(0)
+        rc = lib().oracle_run_until(self.h, float(t_end), float(stop_time), C.byref(n))
+        self.system.pull_scalars(self.st)
+        return rc
+
+    def potential_energy_counted(self):
+        """CalPotenE on the loop's own state, its FindPair warnings counted (REMDRun)."""
+        e = lib().oracle_potential_energy_counted(C.byref(self.st))
+        self.system.pull_scalars(self.st)
+        return e
 
     def cbt(self):
         n = self.system.n

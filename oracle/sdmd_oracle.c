@@ -11,6 +11,7 @@
 #include "sdmd_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -928,14 +929,17 @@ int oracle_cbt(oracle_loop *L, int32_t *node, int32_t *leaf) {
     return 0;
 }
 
-/* ---- the loop: SingleThreadRun (src/SGThread.c:67-155) ---------------------- */
-int oracle_run(oracle_loop *L, int64_t max_events, double t_end,
-               sdmd_trace_rec *trace, int64_t trace_cap, int64_t *n_pops) {
+/* ---- the loop: SingleThreadRun (src/SGThread.c:67-155); with stop_time > 0 it also
+ * stops after the first executed event at time >= stop_time, REMDRun's exchange
+ * point (src/REMD.c:97) ---------------------------------------------------------- */
+static int run_loop(oracle_loop *L, int64_t max_events, double t_end, double stop_time,
+                    sdmd_trace_rec *trace, int64_t trace_cap, int64_t *n_pops) {
     sdmd_system *s = L->s;
     G.err = 0;
     int N = s->n_atoms;
     int64_t start = s->counters.frame, pops = 0;
-    while (s->time <= t_end && s->counters.frame - start < max_events) {
+    int at_stop = 0;
+    while (s->time <= t_end && s->counters.frame - start < max_events && !at_stop) {
         /* AssignJob (src/SGThread.c:237-259) */
         int t = L->node[1];
         double dt = s->ev_time[t];
@@ -959,6 +963,7 @@ int oracle_run(oracle_loop *L, int64_t max_events, double t_end,
             if (G.err) break;
             s->ev_counter[t]++;
             if (p) { s->ev_counter[p]++; n = 2; }
+            if (stop_time > 0 && s->time >= stop_time) at_stop = 1;
         } else {
             s->counters.recal++;
         }
@@ -984,6 +989,15 @@ int oracle_run(oracle_loop *L, int64_t max_events, double t_end,
     return G.err;
 }
 
+int oracle_run(oracle_loop *L, int64_t max_events, double t_end,
+               sdmd_trace_rec *trace, int64_t trace_cap, int64_t *n_pops) {
+    return run_loop(L, max_events, t_end, 0, trace, trace_cap, n_pops);
+}
+
+int oracle_run_until(oracle_loop *L, double t_end, double stop_time, int64_t *n_pops) {
+    return run_loop(L, INT64_MAX, t_end, stop_time, NULL, 0, n_pops);
+}
+
 /* ---- observables ------------------------------------------------------------- */
 /* CalKinetE with no flow (src/ToolFunctions.c:626-656) */
 double oracle_kinetic_energy(const sdmd_system *s) {
@@ -998,8 +1012,12 @@ double oracle_kinetic_energy(const sdmd_system *s) {
 
 /* CalPotenE (src/ToolFunctions.c:659-752): each pair once (pair > i) within the
  * cutoff; HB pairs add their accumulated HB step energy minus the barrier. */
-double oracle_potential_energy(const sdmd_system *sc) {
-    sdmd_system *s = (sdmd_system *)sc;   /* find_pair counts warnings; restore below */
+static double poten(sdmd_system *s, int keep_warnings);
+double oracle_potential_energy(const sdmd_system *sc) { return poten((sdmd_system *)sc, 0); }
+/* CalPotenE as REMDRun calls it (src/REMD.c:98): FindPair's warnings stay counted */
+double oracle_potential_energy_counted(sdmd_system *s) { return poten(s, 1); }
+
+static double poten(sdmd_system *s, int keep_warnings) {
     int64_t w = s->counters.warnings;
     double tpe = 0;
     int N = s->n_atoms;
@@ -1036,7 +1054,7 @@ double oracle_potential_energy(const sdmd_system *sc) {
             }
         }
     }
-    s->counters.warnings = w;
+    if (!keep_warnings) s->counters.warnings = w;
     return tpe;
 }
 

@@ -33,6 +33,10 @@ void oracle_loop_destroy(oracle_loop *L);
  * trace_cap records, the first ones kept); *n_pops receives the pop count. */
 int oracle_run(oracle_loop *L, int64_t max_events, double t_end,
                sdmd_trace_rec *trace, int64_t trace_cap, int64_t *n_pops);
+/* run until the first executed event at time >= stop_time (or t_end) */
+int oracle_run_until(oracle_loop *L, double t_end, double stop_time, int64_t *n_pops);
+/* CalPotenE with FindPair's warnings counted in s->counters (as REMDRun calls it) */
+double oracle_potential_energy_counted(sdmd_system *s);
 
 /* The tree's node[] (2N entries) and leaf[] (N+1 entries), for checks. */
 int oracle_cbt(oracle_loop *L, int32_t *node, int32_t *leaf);

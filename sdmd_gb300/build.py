@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 GPU_LIB = os.path.join(HERE, "libsdmd_gpu.so")
 HOST_LIB = os.path.join(HERE, "libsdmd_host.so")
 
-CUDA_SOURCES = ["api.cu", "loop_fp64.cu", "samples.cu"]
+CUDA_SOURCES = ["api.cu", "loop_fp64.cu", "samples.cu", "remd.cu"]
 # -fmad=false: no multiply-add contraction, so FP64 results are bit-identical to
 # the reference's (gcc -O2 on x86-64 contracts nothing either).  Kernels that want
 # FMA use fma()/__fmaf_rn explicitly.

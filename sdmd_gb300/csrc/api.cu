@@ -38,6 +38,13 @@ struct sdmd_gpu {
     void (*sweep_k)(const DSys *, int) = nullptr;            // plain FP64 or FP32-screened kernels
     void (*loop_k)(const DSys *, double, int) = nullptr;
     double prep_ms = 0, run_ms = 0;
+    // energies / replica exchange scratch (one block: num, T, E, kin, warn, stop, rng, stats)
+    unsigned char *aux = nullptr;
+    int32_t *x_num = nullptr;
+    double *x_T = nullptr, *x_E = nullptr, *x_kin = nullptr, *x_stop = nullptr;
+    int64_t *x_warn = nullptr, *x_stats = nullptr;
+    sdmd_rng *x_rng = nullptr;
+    size_t esmem = 0;
     cudaEvent_t l0 = nullptr, l1 = nullptr;        // around each loop-kernel launch
     double loop_ms = 0;                            // loop-kernel time of the last run
     int64_t launches = 0, loop_launches = 0;       // kernels launched by the last run
@@ -419,6 +426,7 @@ extern "C" void sdmd_gpu_destroy(sdmd_gpu *h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->arena) cudaFree(h->arena);
+    if (h->aux) cudaFree(h->aux);
     if (h->ds) cudaFree(h->ds);
     if (h->e0) cudaEventDestroy(h->e0);
     if (h->e1) cudaEventDestroy(h->e1);
@@ -507,11 +515,20 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         (r = cuda_fail(cudaEventCreate(&h->e0))) || (r = cuda_fail(cudaEventCreate(&h->e1))) ||
         (r = cuda_fail(cudaEventCreate(&h->l0))) || (r = cuda_fail(cudaEventCreate(&h->l1))) ||
         (r = cuda_fail(cudaMalloc(&h->arena, h->arena_bytes))) ||
+        (r = cuda_fail(cudaMalloc(&h->aux, 256 * 9 + (size_t)n_systems * 48))) ||
         (r = cuda_fail(cudaMalloc(&h->ds, sizeof(DSys) * n_systems)))) {
         sdmd_gpu_destroy(h);
         return r;
     }
     cudaMemsetAsync(h->arena, 0, h->arena_bytes, h->stream);
+    {
+        Carver ax{h->aux, 0};
+        h->x_num = ax.take<int32_t>(n_systems); h->x_T = ax.take<double>(n_systems);
+        h->x_E = ax.take<double>(n_systems); h->x_kin = ax.take<double>(n_systems);
+        h->x_warn = ax.take<int64_t>(n_systems); h->x_stop = ax.take<double>(n_systems);
+        h->x_rng = ax.take<sdmd_rng>(1); h->x_stats = ax.take<int64_t>(2);
+    }
+    h->esmem = energy_smem_bytes(nbcap_max);
     std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
     std::vector<Screen32> s32(n_systems);
     for (int k = 0; k < n_systems; k++) build_screen32(systems[k], s32[k]);
@@ -612,6 +629,8 @@ extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
     return collect_errors(h);
 }
 
+static int run_rounds(sdmd_gpu *h, int64_t want, double t_end);
+
 extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
     if (!h || max_events < 0) return SDMD_EINVAL;
     CK(cudaSetDevice(h->opts.device));
@@ -619,9 +638,21 @@ extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
     begin_run_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems, max_events);
     // each round: a sample batch, the loop until it runs low, then the rand() state
     // is moved past the consumed draws; systems without a thermostat need one round
-    std::vector<DScal> sc(h->n_systems);
-    int64_t want = std::min<int64_t>(4 * max_events + 64, 1 << 16);
     h->launches = 1; h->loop_launches = 0; h->loop_ms = 0;
+    int r = run_rounds(h, std::min<int64_t>(4 * max_events + 64, 1 << 16), t_end);
+    if (r) return r;
+    CK(cudaEventRecord(h->e1, h->stream));
+    CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->run_ms = ms;
+    return collect_errors(h);
+}
+
+// sample batch, event loop, RNG commit -- repeated while any system paused because
+// its batch of thermostat samples ran low
+static int run_rounds(sdmd_gpu *h, int64_t want, double t_end) {
+    std::vector<DScal> sc(h->n_systems);
     for (int round = 0; round < 1 << 20; round++) {
         launch_samples(h, want);
         CK(cudaEventRecord(h->l0, h->stream));
@@ -641,12 +672,7 @@ extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
         for (auto &c : sc) if (c.paused && !c.err) again = true;
         if (!again) break;
     }
-    CK(cudaEventRecord(h->e1, h->stream));
-    CK(cudaEventSynchronize(h->e1));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, h->e0, h->e1);
-    h->run_ms = ms;
-    return collect_errors(h);
+    return SDMD_OK;
 }
 
 extern "C" int sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_systems) {
@@ -710,6 +736,79 @@ extern "C" int sdmd_gpu_last_ms(sdmd_gpu *h, double *prepare_ms, double *run_ms)
     if (prepare_ms) *prepare_ms = h->prep_ms;
     if (run_ms) *run_ms = h->run_ms;
     return SDMD_OK;
+}
+
+extern "C" int sdmd_gpu_energies(sdmd_gpu *h, double *pot, double *kin) {
+    if (!h) return SDMD_EINVAL;
+    CK(cudaSetDevice(h->opts.device));
+    energy_kernel<<<h->n_systems, 32, h->esmem, h->stream>>>(h->ds, h->x_E, h->x_kin, h->x_warn);
+    CK(cudaGetLastError());
+    if (pot) CK(cudaMemcpyAsync(pot, h->x_E, sizeof(double) * h->n_systems, cudaMemcpyDeviceToHost, h->stream));
+    if (kin) CK(cudaMemcpyAsync(kin, h->x_kin, sizeof(double) * h->n_systems, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return collect_errors(h);
+}
+
+extern "C" int sdmd_gpu_run_remd(sdmd_gpu *h, int64_t n_exchanges, double t_end, sdmd_remd *x) {
+    if (!h || !x || !x->num || !x->T || n_exchanges < 0) return SDMD_EINVAL;
+    if (!(x->every_events > 0) && !(x->every_time > 0)) return SDMD_EINVAL;
+    CK(cudaSetDevice(h->opts.device));
+    const int n = h->n_systems;
+    std::vector<double> rate(n, 0);
+    if (!(x->every_events > 0)) {   // REMDRun: rate = ((int)(currenttime / outputRate) + 1) * outputRate
+        for (int k = 0; k < n; k++) {
+            DScal c;
+            CK(cudaMemcpy(&c, h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost));
+            rate[k] = (double)((long long)(c.time / x->every_time) + 1) * x->every_time;
+        }
+    }
+    int64_t stats[2] = {x->attempted, x->accepted};
+    CK(cudaMemcpyAsync(h->x_num, x->num, sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->x_T, x->T, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->x_rng, &x->rng, sizeof(sdmd_rng), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->x_stats, stats, sizeof(stats), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaEventRecord(h->e0, h->stream));
+    h->launches = 0; h->loop_launches = 0; h->loop_ms = 0;
+    int64_t done = 0;
+    for (; done < n_exchanges; done++) {
+        if (!(x->every_events > 0))
+            CK(cudaMemcpyAsync(h->x_stop, rate.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+        remd_round_kernel<<<n_blocks(n, 64), 64, 0, h->stream>>>(h->ds, n, x->every_events > 0 ? x->every_events : 0,
+                                                                 x->every_events > 0 ? nullptr : h->x_stop);
+        h->launches += 1;
+        int r = run_rounds(h, std::min<int64_t>(4 * (x->every_events > 0 ? x->every_events : 16384) + 64, 1 << 16),
+                           t_end);
+        if (r) return r;
+        if ((r = collect_errors(h))) return r;
+        // every replica must have reached its exchange point (not the end of the run)
+        bool reached = true;
+        for (int k = 0; k < n; k++) {
+            DScal c;
+            CK(cudaMemcpy(&c, h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost));
+            if (x->every_events > 0 ? c.c.frame < c.target_frame : !c.at_stop) reached = false;
+        }
+        if (!reached) break;
+        energy_kernel<<<n, 32, h->esmem, h->stream>>>(h->ds, h->x_E, h->x_kin, h->x_warn);
+        remd_exchange_kernel<<<1, 1, 0, h->stream>>>(h->ds, n, h->x_num, h->x_T, h->x_E, h->x_warn, h->x_rng,
+                                                     h->x_stats);
+        CK(cudaGetLastError());
+        h->launches += 2;
+        for (int k = 0; k < n; k++) rate[k] += x->every_time;
+    }
+    CK(cudaEventRecord(h->e1, h->stream));
+    CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->run_ms = ms;
+    CK(cudaMemcpy(x->num, h->x_num, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(x->T, h->x_T, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    if (x->E) CK(cudaMemcpy(x->E, h->x_E, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&x->rng, h->x_rng, sizeof(sdmd_rng), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(stats, h->x_stats, sizeof(stats), cudaMemcpyDeviceToHost));
+    x->attempted = stats[0];
+    x->accepted = stats[1];
+    x->exchanges_done = done;
+    return collect_errors(h);
 }
 
 extern "C" int sdmd_gpu_last_run_stats(sdmd_gpu *h, int64_t *launches, int64_t *loop_launches, double *loop_ms) {

@@ -29,7 +29,8 @@ struct DScal {
     int64_t smp_avail, smp_used;
     int64_t target_frame;    // the run stops once c.frame reaches it
     int32_t sw_nflag;        // parallel sweep: atoms left for the in-order re-prediction
-    int32_t pad;
+    int32_t at_stop;         // the loop stopped at stop_time (replica exchange)
+    double stop_time;        // > 0: stop after the first executed event with time >= stop_time
 };
 
 // one system's device arrays (all 1-based per-atom arrays, entry 0 unused)
@@ -189,6 +190,31 @@ __device__ inline double cr_log(double x) {
     dd r = dd_add(el, lm);
     return r.hi + r.lo;
 }
+// 1/n in double-double (n > 0)
+__device__ inline dd dd_inv(int n) {
+    double nd = (double)n, h = 1.0 / nd;
+    dd p = two_prod(h, nd);
+    double rem = (1.0 - p.hi) - p.lo;
+    return quick_two_sum(h, rem / nd);
+}
+// e^x (the replica-exchange test, src/Server.c:169): x = k ln2 + r with the
+// reduction in double-double (|r| <= ln2/2), e^r by its Taylor series in Horner
+// form in double-double, then 2^k.  Correctly rounded unless e^x lies within about
+// 2^-100 relative of a rounding boundary; results in the subnormal range are
+// rounded twice.
+__device__ inline double cr_exp(double x) {
+    if (x != x) return x;
+    if (x > 709.782712893384) return __longlong_as_double(0x7ff0000000000000LL);
+    if (x < -745.2) return 0.0;
+    const double kd = rint(x * 1.4426950408889634);
+    const dd LN2 = {0x1.62e42fefa39efp-1, 0x1.abc9e3b39803fp-56};
+    dd kl = dd_add(two_prod(kd, LN2.hi), {kd * LN2.lo, 0.0});
+    dd r = dd_add({x, 0.0}, {-kl.hi, -kl.lo});
+    dd acc = {1.0, 0.0};
+    for (int n = 22; n >= 1; n--) acc = dd_add({1.0, 0.0}, dd_mul(dd_mul(r, dd_inv(n)), acc));
+    return ldexp(acc.hi + acc.lo, (int)kd);
+}
+
 // Maxwell_Boltzmann_Distribution (src/ToolFunctions.c:544-569).  The rejection
 // loops are bounded: a healthy stream accepts with probability pi/4 per attempt,
 // so 4096 consecutive rejections only happen for a degenerate (e.g. all-zero)

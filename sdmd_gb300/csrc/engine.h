@@ -27,6 +27,13 @@ __global__ void sweep_predict_kernel(const DSys *systems);
 __global__ void sweep_verify_kernel(const DSys *systems);
 __global__ void sweep_fix_kernel(const DSys *systems, int full);
 
+// energies and the replica exchange (remd.cu)
+size_t energy_smem_bytes(int nbcap);
+__global__ void energy_kernel(const DSys *systems, double *pot, double *kin, int64_t *warn);
+__global__ void remd_round_kernel(const DSys *systems, int n, int64_t every_events, const double *stop_time);
+__global__ void remd_exchange_kernel(DSys *systems, int n, int32_t *num, double *T, const double *E,
+                                     const int64_t *warn, sdmd_rng *rng, int64_t *stats);
+
 // thermostat sample stream (samples.cu)
 __global__ void samples_walk_kernel(const DSys *systems, int n_systems, int64_t want);
 __global__ void samples_values_kernel(const DSys *systems, int64_t want);

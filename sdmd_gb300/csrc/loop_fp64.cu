@@ -911,7 +911,7 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
     for (;;) {
         if (tid == 0) {
             if (C.pops >= pop_limit) set_err(B, SDMD_ETIMEOUT, 0);
-            int go = (C.time <= t_end) && (C.c.frame < stop_at) && B.err == 0;
+            int go = (C.time <= t_end) && (C.c.frame < stop_at) && B.err == 0 && !C.at_stop;
             // a pop consumes at most 5 samples (2 predictions + a thermostat event)
             if (go && S.thermostat && C.smp_avail - C.smp_used < 5) { C.paused = 1; go = 0; }
             sh_go = go;
@@ -952,6 +952,8 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
                 do_event(S, C, t, p, B, SCR ? sh_move : nullptr);
                 S.ev_counter[t]++;
                 if (p) S.ev_counter[p]++;
+                // REMDRun's exchange point (src/REMD.c:97): after an executed event at time >= rate
+                if (C.stop_time > 0 && C.time >= C.stop_time) C.at_stop = 1;
             } else {
                 C.c.recal++;
             }

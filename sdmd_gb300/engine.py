@@ -21,9 +21,15 @@ SCREEN_FP64, SCREEN_FP32 = 0, 1
 ABI_FUNCS = ["sdmd_gpu_abi_version", "sdmd_gpu_device_count", "sdmd_gpu_strerror", "sdmd_gpu_create",
              "sdmd_gpu_destroy", "sdmd_gpu_prepare", "sdmd_gpu_run", "sdmd_gpu_download", "sdmd_gpu_trace",
              "sdmd_gpu_last_ms", "sdmd_gpu_last_error", "sdmd_rng_seed", "sdmd_rng_next", "sdmd_rng_skip",
-             "sdmd_gpu_prepare_noalloc", "sdmd_gpu_last_run_stats"]
+             "sdmd_gpu_prepare_noalloc", "sdmd_gpu_last_run_stats", "sdmd_gpu_energies", "sdmd_gpu_run_remd"]
 
 _lib = None
+
+
+class sdmd_remd(C.Structure):
+    _fields_ = [("num", C.POINTER(C.c_int32)), ("T", C.POINTER(C.c_double)), ("E", C.POINTER(C.c_double)),
+                ("every_events", C.c_int64), ("every_time", C.c_double), ("rng", sdmd_rng),
+                ("attempted", C.c_int64), ("accepted", C.c_int64), ("exchanges_done", C.c_int64)]
 
 
 class EngineError(RuntimeError):
@@ -58,6 +64,8 @@ def lib():
         L.sdmd_gpu_last_ms.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.sdmd_gpu_last_error.argtypes = [C.c_void_p, P(sdmd_error_info)]
         L.sdmd_gpu_last_run_stats.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_double)]
+        L.sdmd_gpu_energies.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+        L.sdmd_gpu_run_remd.argtypes = [C.c_void_p, C.c_int64, C.c_double, P(sdmd_remd)]
         L.sdmd_rng_seed.argtypes = [P(sdmd_rng), C.c_uint32]
         L.sdmd_rng_seed.restype = None
         L.sdmd_rng_next.argtypes = [P(sdmd_rng)]
@@ -130,6 +138,38 @@ class Engine:
         a, b = C.c_double(0), C.c_double(0)
         lib().sdmd_gpu_last_ms(self.h, C.byref(a), C.byref(b))
         return a.value, b.value
+
+    def energies(self):
+        """(potential, kinetic) energy of every system: CalPotenE / CalKinetE on the device."""
+        n = len(self.systems)
+        pot, kin = np.zeros(n), np.zeros(n)
+        self._check(lib().sdmd_gpu_energies(self.h, pot.ctypes.data_as(C.POINTER(C.c_double)),
+                                            kin.ctypes.data_as(C.POINTER(C.c_double))), "sdmd_gpu_energies")
+        return pot, kin
+
+    def run_remd(self, n_exchanges, num, T, rng, every_events=0, every_time=0.0, t_end=0.0, attempted=0,
+                 accepted=0):
+        """Replica exchange on the device (every system is a replica).  num / T are the
+        replicas' (ladder index, temperature) records, rng the exchange server's rand()
+        state (33 ints).  Returns dict(num, T, E, rng, attempted, accepted, done)."""
+        n = len(self.systems)
+        num = np.ascontiguousarray(num, np.int32).copy()
+        T = np.ascontiguousarray(T, np.float64).copy()
+        E = np.zeros(n)
+        x = sdmd_remd()
+        x.num = num.ctypes.data_as(C.POINTER(C.c_int32))
+        x.T = T.ctypes.data_as(C.POINTER(C.c_double))
+        x.E = E.ctypes.data_as(C.POINTER(C.c_double))
+        x.every_events = int(every_events)
+        x.every_time = float(every_time)
+        for i in range(31):
+            x.rng.tab[i] = int(rng[i])
+        x.rng.front, x.rng.rear = int(rng[31]), int(rng[32])
+        x.attempted, x.accepted = int(attempted), int(accepted)
+        self._check(lib().sdmd_gpu_run_remd(self.h, int(n_exchanges), float(t_end), C.byref(x)), "sdmd_gpu_run_remd")
+        out_rng = np.array([x.rng.tab[i] for i in range(31)] + [x.rng.front, x.rng.rear], np.int32)
+        return {"num": num, "T": T, "E": E, "rng": out_rng, "attempted": x.attempted, "accepted": x.accepted,
+                "done": x.exchanges_done}
 
     def last_run_stats(self):
         """(kernels launched, event-loop kernels launched, event-loop kernel ms) of the last run."""
