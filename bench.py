@@ -132,7 +132,8 @@ def build_workload(name, rank):
     if name == "c1":
         return [W.c1(seed=1 + rank)], {"workload": "C1: one ALA x 10 chain, 40 A cube, Andersen NVT 300 K"}
     if name == "c3":
-        return W.c3(seed=1 + rank), {"workload": "C3: 64 replicas of ALA x 10, temperatures 270-500 K"}
+        return W.c3(seed=1 + rank), {"workload": "C3: 64 replicas of ALA x 10, temperatures geometric 270-500 K, "
+                                                 "on-device replica exchange every 1e4 events per replica"}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -197,15 +198,37 @@ def run_ours(args, D):
     from sdmd_gb300.engine import ADVANCE_EAGER, ADVANCE_LAZY, SCREEN_FP32, SCREEN_FP64
     adv = ADVANCE_LAZY if args.advance == "lazy" else ADVANCE_EAGER
     scr = SCREEN_FP32 if args.screen == "fp32" else SCREEN_FP64
-    threads = args.threads or (256 if len(systems) == 1 else 64)
+    tuned = None
+    if args.threads:
+        threads = args.threads
+    else:   # CTA size from the autotuner (short runs on copies of the workload)
+        from sdmd_gb300.engine import autotune_threads
+        threads, tuned = autotune_threads(systems, advance=adv, screen=scr, device=D.local,
+                                          candidates=(128, 256) if len(systems) == 1 else (64, 128, 256))
     eng = Engine(systems, threads=threads, device=D.local, advance=adv, screen=scr)
     eng.prepare(full=True)
     sweep_ms = eng.last_ms()[0]
     eng.download()
     after_sweep = [s.copy() for s in systems]
 
+    remd = None
+    if args.workload == "c3":   # one step = one exchange round: E events per replica, then the exchange
+        import numpy as np
+        from sdmd_gb300.system import glibc_rng_state
+        remd = {"num": np.arange(1, len(systems) + 1), "T": np.array([s.scal["temperature"] for s in systems]),
+                "rng": glibc_rng_state(20201), "attempted": 0, "accepted": 0}
+
+    def step():
+        if remd is None:
+            eng.run(E)
+            return
+        out = eng.run_remd(1, remd["num"], remd["T"], remd["rng"], every_events=E, attempted=remd["attempted"],
+                           accepted=remd["accepted"])
+        remd.update(num=out["num"], T=out["T"], rng=out["rng"], attempted=out["attempted"],
+                    accepted=out["accepted"])
+
     for _ in range(args.warmup):
-        eng.run(E)
+        step()
     D.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(D.local)
@@ -220,7 +243,7 @@ def run_ours(args, D):
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        eng.run(E)
+        step()
         step_ms.append(eng.last_ms()[1])
         a, b, c = eng.last_run_stats()
         launches += a
@@ -251,7 +274,10 @@ def run_ours(args, D):
         t0 = time.perf_counter()
         with Engine(work, threads=threads, device=D.local, advance=adv, screen=scr) as e2:
             e2.prepare(full=False)
-            e2.run(E)
+            if remd is None:
+                e2.run(E)
+            else:
+                e2.run_remd(1, remd["num"], remd["T"], remd["rng"], every_events=E)
             e2.download()
         e2e_t.append(time.perf_counter() - t0)
         e2e_events += E * len(work)
@@ -288,7 +314,12 @@ def run_ours(args, D):
         cpu = cpu_baseline(after_sweep[0], args.cpu_seconds)
 
     if D.rank == 0:
-        cfg.update({"n_atoms": natoms, "n_systems": len(systems) * D.world, "events_per_step": E,
+        if tuned is not None:
+            cfg["autotune"] = {str(k): round(v, 1) for k, v in tuned.items()}
+        if remd is not None:
+            cfg["exchange"] = {"every_events": E, "attempted": int(remd["attempted"]),
+                               "accepted": int(remd["accepted"])}
+        cfg.update({"n_atoms": natoms, "n_systems": len(systems) * D.world, "events_per_step": E * len(systems),
                     "l2": "flushed between steps (256 MiB write)", "advance": args.advance, "screen": args.screen,
                     "threads_per_system": threads, "replicas": "independent per rank" if D.world > 1 else None})
         line = {"metric": METRIC, "value": round(value, 3), "unit": "events/s", "n_gpus": D.world,
@@ -322,6 +353,48 @@ def cpu_baseline(system, seconds):
             "sample": f"{n} events of the same system from the post-sweep state (oracle/sdmd_oracle.c, gcc -O2)"}
 
 
+def _ref_worker(job):
+    """One host process of the reference arm: the oracle loop on system k of the batch."""
+    workload, k, n_events = job
+    sys.path.insert(0, REPO)
+    from oracle import oracle as O
+    systems, _ = build_workload(workload, 0)
+    s = systems[k]
+    O.predict_all(s)
+    loop = O.Loop(s)
+    t0 = time.perf_counter()
+    loop.run(n_events)
+    return n_events, time.perf_counter() - t0
+
+
+def run_reference_batch(args, D, systems, cfg):
+    """A batch of independent systems: one single-threaded reference loop per host
+    core, min(#systems, cores) at once, events summed over the wall time."""
+    import multiprocessing as mp
+    cores = min(len(systems), os.cpu_count() or 1)
+    n_ev = max(200, int(args.events_per_step * args.cpu_seconds / 60))   # bounded sample per core and step
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_ref_worker, [(args.workload, k, 200) for k in range(cores)])   # warm-up: imports, builds
+        times, total = [], 0
+        for _ in range(args.steps):
+            res = pool.map(_ref_worker, [(args.workload, k, n_ev) for k in range(cores)])
+            times.append(max(r[1] for r in res))   # the loops run concurrently; their set-up is not timed
+            total += sum(r[0] for r in res)
+    value = total / sum(times)
+    cfg.update({"n_atoms": sum(s.n for s in systems), "n_systems": len(systems),
+                "events_per_step": n_ev * cores})
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "events/s", "n_gpus": D.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(sum(times) * 1e3 / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded random-sequence peptides, bundled Library_Ding force field)", "config": cfg,
+            "cpu_baseline": {"value": round(value, 3), "unit": "events/s", "cores": cores, "kind": "port",
+                             "sample": f"{n_ev} events on each of {cores} systems of the batch per step, one "
+                                       "single-threaded loop per core (the reference runs one replica per process)"},
+            "e2e": {"value": round(value, 3), "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
 def run_reference(args, D):
     """The reference's CPU algorithm (oracle port) on this host's cores."""
     if D.rank != 0:
@@ -332,6 +405,9 @@ def run_reference(args, D):
     from sdmd_gb300 import build as B
     B.build_host()
     systems, cfg = build_workload(args.workload, 0)
+    if len(systems) > 1:
+        run_reference_batch(args, D, systems, cfg)
+        return
     s = systems[0]
     O.predict_all(s)
     loop = O.Loop(s)
@@ -366,7 +442,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="c2")
-    ap.add_argument("--events-per-step", type=int, default=20000)
+    ap.add_argument("--events-per-step", type=int, default=None)
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--advance", choices=["eager", "lazy"], default="lazy")
     ap.add_argument("--screen", choices=["fp32", "fp64"], default="fp32")
@@ -374,6 +450,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.events_per_step is None:
+        args.events_per_step = 10000 if args.workload == "c3" else 20000   # C3: one exchange per 1e4 events
     D = Dist()
     if args.impl == "reference":
         run_reference(args, D)

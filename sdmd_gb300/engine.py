@@ -193,3 +193,22 @@ class Engine:
 
     def __exit__(self, *a):
         self.close()
+
+
+def autotune_threads(systems, advance=ADVANCE_EAGER, screen=SCREEN_FP64, candidates=(64, 128, 256), events=400,
+                     device=0):
+    """Pick the threads per system (CTA size) that runs `events` executed events per
+    system fastest on copies of `systems` (full-rebuild sweep first, one warm-up
+    run, then a timed run).  Returns (best, {threads: events/s})."""
+    rates = {}
+    for t in candidates:
+        work = [s.copy() for s in systems]
+        with Engine(work, advance=advance, screen=screen, threads=t, device=device) as e:
+            e.prepare(full=True)
+            e.run(max(events // 4, 16))
+            e.run(events)
+            ms = e.last_ms()[1]
+        rates[t] = events * len(systems) / max(ms, 1e-6) * 1e3
+    best = max(rates, key=rates.get)
+    return best, rates
+

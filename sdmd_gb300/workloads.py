@@ -77,9 +77,12 @@ def random_sequences(n, length, seed, lo=None, hi=None):
 
 
 def c1(seed=1, temperature_k=300.0, thermostat="Andersen", box=40.0, rng_seed=1575263273):
-    d = _datadir(dict(temp=round(temperature_k * BOLTZMANN, 4), thermostat=thermostat, time=1e9))
-    gro = generate_gro(d, [["ALA"] * 10], (box, box, box), seed=seed)
-    return build_system(d, gro_text=gro, seed=rng_seed)
+    def make():
+        d = _datadir(dict(temp=round(temperature_k * BOLTZMANN, 4), thermostat=thermostat, time=1e9))
+        gro = generate_gro(d, [["ALA"] * 10], (box, box, box), seed=seed)
+        return build_system(d, gro_text=gro, seed=rng_seed)
+
+    return cached(f"c1_{seed}_{temperature_k}_{thermostat}_{box}_{rng_seed}", make)
 
 
 def c2(n_chains=256, length=16, seed=1, temperature_k=300.0, thermostat="Andersen", conc_mM=5.0,
@@ -104,3 +107,27 @@ def c3(n_replicas=64, t_lo=270.0, t_hi=500.0, seed=1):
         s.rng = glibc_rng_state(1000 + k)
         out.append(s)
     return out
+
+
+def c4(n_systems=512, lo=5, hi=60, seed=1, t_lo=280.0, t_hi=400.0, rng_seed0=5000):
+    """512 single chains, lengths uniform lo..hi residues with random sequences, box
+    edge 40 A * (N / 59)^(1/3) (C1's atom density) floored at 27 A (three 9 A
+    cells), temperatures uniform t_lo..t_hi.  Each system is built (and cached)
+    separately; returns the list of Systems."""
+    rng = np.random.default_rng(seed)
+    seqs = random_sequences(n_systems, 0, seed, lo, hi)
+    temps = rng.uniform(t_lo, t_hi, n_systems)
+    out = []
+    for k, seq in enumerate(seqs):
+        T = float(temps[k])
+        natoms_est = 10.45 * len(seq)
+        edge = max(27.0, 40.0 * (natoms_est / 59.0) ** (1.0 / 3.0))
+
+        def make(seq=seq, T=T, edge=edge, k=k):
+            d = _datadir(dict(temp=round(T * BOLTZMANN, 4), thermostat="Andersen", time=1e9))
+            gro = generate_gro(d, [seq], (edge, edge, edge), seed=seed * 100003 + k)
+            return build_system(d, gro_text=gro, seed=rng_seed0 + k)
+
+        out.append(cached(f"c4_{k}_{len(seq)}_{seed}_{round(T, 3)}", make))
+    return out
+
