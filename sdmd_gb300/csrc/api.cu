@@ -187,6 +187,8 @@ struct Screen32 {
     std::vector<long long> pair_key, pair_stepkey, con_key, con_stepkey;
     std::vector<int32_t> conn_win;
     std::vector<int32_t> leaf0;   // CreateCBT's leaf of every atom (src/CBT.c:16-30)
+    std::vector<int16_t> rp_idx;
+    std::vector<int8_t> con_win, con_ok;
 };
 
 // The leaf each atom gets from CreateCBT: atoms are inserted in order 1..N and
@@ -265,6 +267,29 @@ static void build_screen32(const sdmd_system &s, Screen32 &o) {
     }
     const int N = s.n_atoms;
     cbt_leaf_layout(N, o.leaf0);
+    // RightPair: the first of (t1,t2), (t1',t2), (t1,t2'), (t1',t2') with dmin > 0, ' = AtomTypeChange(., 0)
+    auto unhb = [](int t) { return t == 3 ? 1 : t == 4 ? 2 : t == 27 ? 26 : t; };
+    auto idx0 = [](int a, int b) { return a * SDMD_NTYPES + b; };
+    o.rp_idx.assign((size_t)SDMD_NTYPES * SDMD_NTYPES, -1);
+    for (int t1 = 0; t1 < SDMD_NTYPES; t1++)
+        for (int t2 = 0; t2 < SDMD_NTYPES; t2++) {
+            const int a = unhb(t1), b = unhb(t2);
+            const int cand[4] = {idx0(t1, t2), idx0(a, t2), idx0(t1, b), idx0(a, b)};
+            for (int c : cand)
+                if (s.pair_dmin[c] > 0) { o.rp_idx[(size_t)idx0(t1, t2)] = (int16_t)c; break; }
+        }
+    o.con_win.assign((size_t)(N + 1) * 128, -1);
+    o.con_ok.assign((size_t)N + 1, 0);
+    for (int i = 1; i <= N; i++) {
+        int8_t *w = &o.con_win[(size_t)i * 128];
+        bool ok = s.con_off[i + 1] - s.con_off[i] <= 127;
+        for (int k = s.con_off[i]; ok && k < s.con_off[i + 1]; k++) {
+            const int idx = s.con_j[k] - (i - 64);
+            if (idx < 0 || idx >= 128) { ok = false; break; }
+            if (w[idx] < 0) w[idx] = (int8_t)(k - s.con_off[i]);
+        }
+        o.con_ok[i] = ok ? 1 : 0;
+    }
     o.conn_win.assign((size_t)(N + 1) * kConnWin, 0);
     for (int i = 1; i <= N; i++) {
         int32_t *w = &o.conn_win[(size_t)i * kConnWin];
@@ -353,10 +378,16 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
         d.con_stepkey = cv.take<long long>(((size_t)m.n_con_steps + 1) * 2);
         d.conn_win = cv.take<int32_t>(N1 * kConnWin);
         d.cbt_leaf0 = cv.take<int32_t>(N1 + 1);
+        d.rp_idx = cv.take<int16_t>((size_t)SDMD_NTYPES * SDMD_NTYPES);
+        d.con_win = cv.take<int8_t>(N1 * 128);
+        d.con_ok = cv.take<int8_t>(N1);
         if (h->opts.screen == SDMD_SCREEN_FP32) {
             d.sw_hbit = cv.take<int32_t>(N1);
             d.sw_flag = cv.take<int32_t>(N1);
             d.sw_warn = cv.take<int32_t>(N1);
+            d.sx = cv.take<float>(N1); d.sy = cv.take<float>(N1); d.sz = cv.take<float>(N1);
+            d.svx = cv.take<float>(N1); d.svy = cv.take<float>(N1); d.svz = cv.take<float>(N1);
+            d.stl = cv.take<float>(N1);
             d.maxc = std::min<int32_t>(kMaxPerCell, m.n);
             d.cell_cnt = cv.take<int32_t>((size_t)m.ncell + 1);
             d.cell_arr = cv.take<int32_t>(((size_t)m.ncell + 1) * d.maxc);
@@ -374,6 +405,9 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             put(*copies, (long long *)d.con_stepkey, q.con_stepkey.data(), q.con_stepkey.size());
             put(*copies, (int32_t *)d.conn_win, q.conn_win.data(), q.conn_win.size());
             put(*copies, (int32_t *)d.cbt_leaf0, q.leaf0.data(), q.leaf0.size());
+            put(*copies, (int16_t *)d.rp_idx, q.rp_idx.data(), q.rp_idx.size());
+            put(*copies, (int8_t *)d.con_win, q.con_win.data(), q.con_win.size());
+            put(*copies, (int8_t *)d.con_ok, q.con_ok.data(), q.con_ok.size());
         }
         if (copies) {
             auto &c = *copies;
@@ -490,6 +524,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         cut *= cut;
         f32_bracket(cut, d.cut32);
         d.cut_key = host_tkey(cut);
+        d.rq = nextafterf((float)sqrt(cut), INFINITY) * (1.0f + 0x1p-20f);
         f32_bracket(SDMD_ZERO, d.zero32);
         for (int q = 0; q < 3; q++) f32_bracket(s.box[q], d.box32 + 2 * q);
     }

@@ -106,6 +106,19 @@ struct DSys {
     // parallel full-rebuild sweep scratch: pre-sweep HB interaction type, and the
     // atoms whose adopted duplicate differs from their own fresh offer
     int32_t *sw_hbit, *sw_flag, *sw_warn;
+    // RightPair (src/ToolFunctions.c:278-292) of every type pair, resolved on the
+    // host: the table-0 entry of (t1, t2), or -1 (33 x 33)
+    const int16_t *rp_idx;
+    // per atom i: the constraint of i with partner i-64 .. i+63 as an offset into
+    // i's constraint list (first occurrence), -1 for none; con_ok[i] = 0 when a
+    // partner lies outside the window (the list is then searched)
+    const int8_t *con_win, *con_ok;
+    // lazy mode, screened path: FP32 copies (round to nearest) of x, v and of
+    // tloc - T0, for a cheap rigorous distance reject; valid while shadow_ok
+    float *sx, *sy, *sz, *svx, *svy, *svz, *stl;
+    double T0;
+    int32_t shadow_ok;
+    float rq;                // a float above sqrt((0.9 cutoff)^2), for the per-axis reject
 };
 
 // position component of atom j at the current time (lazy mode extrapolates)

@@ -837,6 +837,7 @@ __device__ __forceinline__ void sweep_body(const DSys *systems, int full, DSys &
     if constexpr (SCR) {
         cells_from_list(S, B);
         __syncthreads();
+        stage_rp(S);
     }
     if (full) {
         if (S.thermostat && C.smp_avail < S.n) {   // one sample per predicted atom
@@ -903,6 +904,16 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
         cells_from_list(S, B);
         __syncthreads();
         if (tid == 0) sh_cells_ok = B.err == 0;
+        stage_rp(S);
+        if (S.lazy && S.sx) {   // FP32 shadows of every atom for this launch (epoch T0 = now)
+            if (tid == 0) S.T0 = C.time;
+            __syncthreads();
+            for (int k = 1 + tid; k <= S.n; k += T)
+                for (int f = 0; f < 7; f++) shadow_field(S, k, f);
+            __syncthreads();
+            if (tid == 0) S.shadow_ok = 1;
+            __syncthreads();
+        }
     }
     const double t_end = t_end_override > 0 ? t_end_override : S.t_end;
     const int64_t stop_at = C.target_frame;

@@ -136,6 +136,51 @@ __device__ __forceinline__ Iv root_iv(const KIv &k, int st, Iv d2, bool &ok) {
     return t;
 }
 
+// the constraint of a1 with partner a2 (index into the constraint arrays), or -1
+__device__ __forceinline__ int con_index(const DSys &S, int a1, int a2) {
+    if (S.con_ok[a1]) {
+        const unsigned idx = (unsigned)(a2 - (a1 - 64));
+        if (idx >= 128u) return -1;
+        const int r = S.con_win[(size_t)a1 * 128 + idx];
+        return r < 0 ? -1 : S.con_off[a1] + r;
+    }
+    for (int k = S.con_off[a1], e = S.con_off[a1 + 1]; k < e; k++)
+        if (S.con_j[k] == a2) return k;
+    return -1;
+}
+
+// the predicted atom's own fields, loaded once per prediction
+struct AtomI {
+    int32_t hbb, role, type, prot, aa;
+    int32_t nb[4];
+    int32_t win[9];               // its conn_win row
+    int64_t cnt;                  // ev_counter
+    float pf[3];                  // lzx(i) rounded to float (lazy reject)
+    float nowr;                   // now - T0 rounded to float
+};
+__device__ __forceinline__ void load_atom_i(const DSys &S, int i, const double *xi, AtomI &A) {
+    A.hbb = S.hb_bond[i]; A.role = S.hb_role[i]; A.type = S.type[i]; A.prot = S.protein[i]; A.aa = S.aanum[i];
+    for (int q = 0; q < 4; q++) A.nb[q] = S.nb_partner[4 * i + q];
+    for (int q = 0; q < 9; q++) A.win[q] = S.conn_win[9 * i + q];
+    A.cnt = S.ev_counter[i];
+    if (S.shadow_ok) {
+        for (int d = 0; d < 3; d++) A.pf[d] = __double2float_rn(xi[d]);
+        A.nowr = __double2float_rn(S.now - S.T0);
+    }
+}
+// lazy mode: one field of the FP32 shadow of atom k (f = 0..6: x y z vx vy vz, tloc - T0)
+__device__ __forceinline__ void shadow_field(const DSys &S, int k, int f) {
+    switch (f) {
+        case 0: S.sx[k] = __double2float_rn(S.x[k]); break;
+        case 1: S.sy[k] = __double2float_rn(S.y[k]); break;
+        case 2: S.sz[k] = __double2float_rn(S.z[k]); break;
+        case 3: S.svx[k] = __double2float_rn(S.vx[k]); break;
+        case 4: S.svy[k] = __double2float_rn(S.vy[k]); break;
+        case 5: S.svz[k] = __double2float_rn(S.vz[k]); break;
+        default: S.stl[k] = __double2float_rn(S.tloc[k] - S.T0); break;
+    }
+}
+
 // connection-map bits of (i, j) from the per-atom window (row scan outside it)
 __device__ __forceinline__ int conn_bits_w(const DSys &S, int i, int j) {
     const int32_t *w = S.conn_win + 9 * i;
@@ -154,40 +199,45 @@ struct Verdict { int st, warn, dup; Iv t; };
 __device__ __forceinline__ int bsign3(Iv b) { return b.hi < 0.f ? 1 : (b.lo >= 0.f ? 0 : 2); }   // 1: b < 0
 
 // FindPair as a screen: which step bracket r2 falls in, certain or not.
+// t1 / t2 are the atoms' types (K_COLLISION); the first four steps of the entry are
+// loaded together before the bracket walk.
 struct FPs { int cs, warn; bool lopot0, uppot0, inf; Iv lo, up; };
-__device__ bool fp_screen(const DSys &S, int a1, int a2, int kind, int neg, Iv r2, FPs &o) {
+__device__ bool fp_screen(const DSys &S, int a1, int a2, int kind, int neg, Iv r2, FPs &o, int t1, int t2) {
     const float *thr, *stp;
     const double *se;
     double dmin, dmax;
     int sn;
     if (kind == K_CONSTRAINT) {
-        int k = S.con_off[a1], e = S.con_off[a1 + 1];
-        for (; k < e; k++) if (S.con_j[k] == a2) break;
-        if (k == e) return false;
+        const int k = con_index(S, a1, a2);
+        if (k < 0) return false;
         thr = S.con_thr32 + 8 * k; dmin = S.con_dmin[k]; dmax = S.con_dmax[k]; sn = S.con_step_n[k];
-        int so = S.con_step_off[k];
+        const int so = S.con_step_off[k];
         stp = S.con_step32 + 6 * so; se = S.con_step_e + so;
     } else {
         int e;
         if (kind == K_COLLISION) {
-            int t1 = S.type[a1], t2 = S.type[a2];
-            if (dbl_pos(S.pair_dmin[tab_idx(0, t1, t2)])) e = tab_idx(0, t1, t2);
-            else {
-                int a = type_change(t1, 0), b = type_change(t2, 0);
-                if (dbl_pos(S.pair_dmin[tab_idx(0, a, t2)])) e = tab_idx(0, a, t2);
-                else if (dbl_pos(S.pair_dmin[tab_idx(0, t1, b)])) e = tab_idx(0, t1, b);
-                else if (dbl_pos(S.pair_dmin[tab_idx(0, a, b)])) e = tab_idx(0, a, b);
-                else return false;
-            }
+            e = S.rp_idx[t1 * NT + t2];
+            if (e < 0) return false;
         } else {   // K_HB
             int bad = 0;
-            int tn = hb_model(S, a1, a2, &bad);
+            const int tn = hb_model(S, a1, a2, &bad);
             if (tn < 0 || bad) return false;
             e = tab_idx(tn, 0, 0);
         }
         thr = S.pair_thr32 + 8 * e; dmin = S.pair_dmin[e]; dmax = S.pair_dmax[e]; sn = S.pair_step_n[e];
-        int so = S.pair_step_off[e];
+        const int so = S.pair_step_off[e];
         stp = S.pair_step32 + 6 * so; se = S.pair_step_e + so;
+    }
+    const int col = neg ? 0 : 2;                    // fl(d + ZERO) when approaching, fl(d - ZERO) otherwise
+    float pre[4][4];
+    long long pse[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (q < sn) {
+            const float *p = stp + 6 * q;
+            pre[q][0] = p[col]; pre[q][1] = p[col + 1]; pre[q][2] = p[4]; pre[q][3] = p[5];
+            pse[q] = __double_as_longlong(se[q]);
+        }
     }
     if (dbl_is_zero(dmin)) return false;
     const int a1bond = a1 ? S.hb_bond[a1] : 0;
@@ -195,19 +245,26 @@ __device__ bool fp_screen(const DSys &S, int a1, int a2, int kind, int neg, Iv r
     o.warn = 0; o.inf = false; o.cs = -1;
     if (lt3(r2, thr + 0) != 0) return false;        // inside dmin - ZERO (or undecided): rare, exact path
     o.lo = ivc(thr[4], thr[5]); o.lopot0 = true;
-    const int col = neg ? 0 : 2;                    // fl(d + ZERO) when approaching, fl(d - ZERO) otherwise
     for (int q = 0; q < sn; q++) {
-        const float *p = stp + 6 * q;
-        if (p[4] == 0.f && p[5] == 0.f) break;      // d == 0 ends the list
-        int c = lt3(r2, p + col);
+        float c0, c1, d0, d1;
+        long long eb;
+        if (q < 4) { c0 = pre[q][0]; c1 = pre[q][1]; d0 = pre[q][2]; d1 = pre[q][3]; eb = pse[q]; }
+        else {
+            const float *p = stp + 6 * q;
+            c0 = p[col]; c1 = p[col + 1]; d0 = p[4]; d1 = p[5]; eb = __double_as_longlong(se[q]);
+        }
+        if (d0 == 0.f && d1 == 0.f) break;          // d == 0 ends the list
+        const float cthr[2] = {c0, c1};
+        const int c = lt3(r2, cthr);
         if (c == 2) return false;
+        const bool ezero = (eb << 1) == 0;
         if (c == 1) {
-            o.up = ivc(p[4], p[5]); o.uppot0 = dbl_is_zero(se[q]);
+            o.up = ivc(d0, d1); o.uppot0 = ezero;
             if (q == 0) { o.cs = 0; return true; }
             if (kind == K_HB && q == sn - 1 && a1bond > 0) { o.cs = 1; return true; }
             return true;
         }
-        o.lo = ivc(p[4], p[5]); o.lopot0 = dbl_is_zero(se[q]);
+        o.lo = ivc(d0, d1); o.lopot0 = ezero;
     }
     if (kind == K_HB && a1bond > 0) o.warn++;
     if (dbl_pos(dmax)) {
@@ -274,7 +331,7 @@ __device__ void screen_hbs_k(const DSys &S, int i, int j, const KIv &k, Verdict 
     int neg = bsign3(k.b);
     if (neg == 2) return;
     FPs o;
-    if (!fp_screen(S, i, j, K_HB, neg, k.r2, o)) return;
+    if (!fp_screen(S, i, j, K_HB, neg, k.r2, o, 0, 0)) return;
     if (o.inf) return;
     if (!(neg && o.cs == 1)) { v.st = SC_NONE; v.warn = o.warn; return; }
     Iv D = disc_iv(k, o.lo);
@@ -290,29 +347,71 @@ __device__ void screen_hbs_k(const DSys &S, int i, int j, const KIv &k, Verdict 
 // One 27-cell candidate j of atom i: the collision verdict (CollisionTime) and,
 // when the atom scans for hydrogen bonds (hb), the HB-scan verdict, sharing one
 // evaluation of the pair's kinematics.  `always` forces "refine" (the partner's
-// view of the target, whose event is only known after the target's fold).
-__device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, bool hb, int always, Verdict &vc,
-                            Verdict &vh) {
+// view of the target, whose event is only known after the target's fold).  Every
+// field of j is loaded at once; A holds atom i's own fields.
+__device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, const AtomI &A, bool hb, int always,
+                            Verdict &vc, Verdict &vh) {
     vc.warn = 0; vc.dup = 0; vc.st = SC_NONE;
     vh.warn = 0; vh.dup = 0; vh.st = SC_NONE;
     if (j == i) return;
+    const int evp = S.ev_partner[j], evt = S.ev_type[j];
+    const int64_t evpc = S.ev_pcounter[j];
+    const int rj = S.hb_role[j], tj = S.type[j], hbj = S.hb_bond[j], pj = S.protein[j], aj = S.aanum[j];
+    const int cj[3] = {S.cx[j], S.cy[j], S.cz[j]};
+    const bool named = j < S.dup_limit && evp == i && evpc == A.cnt;
     bool need_c = true;
-    if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_COLLISION && S.ev_pcounter[j] == S.ev_counter[i]) {
-        vc.st = SC_REFINE; vc.dup = 1; need_c = false;
-    } else if (always) { vc.st = SC_REFINE; need_c = false; }
-    bool need_h = hb && hb_pair_ok(S, i, j) && S.hb_bond[j] == 0 &&
-                  ((S.protein[i] == S.protein[j] && abs(S.aanum[i] - S.aanum[j]) >= 4) || S.protein[i] != S.protein[j]);
+    if (named && evt == SDMD_EV_COLLISION) { vc.st = SC_REFINE; vc.dup = 1; need_c = false; }
+    else if (always) { vc.st = SC_REFINE; need_c = false; }
+    const int ri = A.role;
+    const bool pair_ok = (ri == 'A' && rj == 'D') || (ri == 'D' && rj == 'A') || (ri == 'S' && tj == 2) ||
+                         (rj == 'S' && A.type == 2) || (ri == 'S' && rj == 'S');   // hb_pair_ok
+    bool need_h = hb && pair_ok && hbj == 0 && ((A.prot == pj && abs(A.aa - aj) >= 4) || A.prot != pj);
     if (need_h) {
-        if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
-            vh.st = SC_REFINE; vh.dup = 1; need_h = false;
-        } else if (always) { vh.st = SC_REFINE; need_h = false; }
+        if (named && evt == SDMD_EV_HB) { vh.st = SC_REFINE; vh.dup = 1; need_h = false; }
+        else if (always) { vh.st = SC_REFINE; need_h = false; }
     }
     int bits = 0;
     if (need_c) {
-        bits = conn_bits_w(S, i, j);
-        if ((bits & 1) || S.hb_bond[i] == j || nb_has(S, i, j)) need_c = false;
+        if (A.win[0] < 0) bits = conn_bits(S, i, j);
+        else {
+            const unsigned idx = (unsigned)(j - A.win[0]);
+            if (idx < 128u) {
+                const unsigned m = 1u << (idx & 31);
+                bits = (((unsigned)A.win[1 + (idx >> 5)] & m) ? 1 : 0) | (((unsigned)A.win[5 + (idx >> 5)] & m) ? 2 : 0);
+            }
+        }
+        bool nbh = false;
+        for (int q = 0; q < 4; q++) {   // FindElemInList(neighborPartner, j)
+            if (A.nb[q] == 0) break;
+            if (A.nb[q] == j) { nbh = true; break; }
+        }
+        if ((bits & 1) || A.hbb == j || nbh) need_c = false;
     }
     if (!need_c && !need_h) return;
+    if (S.shadow_ok) {
+        // Lazy mode: j's FP64 position lzx(j) is x + v * fl(now - tloc).  From the
+        // float shadows, each axis of r_i - r_j is known to within eb (the rounding
+        // of every operand and step, with a factor 4 to spare); an axis whose
+        // separation certainly exceeds rq puts r2 above the scan radius for both the
+        // collision and the HB scan.
+        const float tlj = S.stl[j], dtj = __fsub_rn(A.nowr, tlj);
+        const float xj[3] = {S.sx[j], S.sy[j], S.sz[j]}, vj[3] = {S.svx[j], S.svy[j], S.svz[j]};
+        const float tsum = fabsf(dtj) + fabsf(A.nowr) + fabsf(tlj);
+        bool far = false;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            float pj = __fmaf_rn(vj[d], dtj, xj[d]), bx = 0.f;
+            if (I.c[d] != cj[d]) {
+                if (I.c[d] == 0 && cj[d] == S.cn[d] - 1) { pj = pj - S.box32[2 * d]; bx = S.box32[2 * d + 1]; }
+                else if (I.c[d] == S.cn[d] - 1 && cj[d] == 0) { pj = pj + S.box32[2 * d]; bx = S.box32[2 * d + 1]; }
+            }
+            const float dx = A.pf[d] - pj;
+            const float eb = 0x1p-19f * (fabsf(A.pf[d]) + fabsf(xj[d]) + fabsf(pj) + fabsf(vj[d]) * tsum + bx +
+                                         fabsf(dx)) + 0x1p-100f;
+            if (fabsf(dx) - eb > S.rq) far = true;
+        }
+        if (far) return;   // both verdicts stay "none": r2 > (0.9 cutoff)^2 certainly
+    }
     PIv J; atom_piv(S, j, J);
     KIv k; kin_iv(S, I, J, k);
     if (need_h) screen_hbs_k(S, i, j, k, vh);
@@ -325,7 +424,7 @@ __device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, bool hb, 
     if (neg == 2) return;
     const int constrained = bits & 2;
     FPs o;
-    if (!fp_screen(S, i, j, constrained ? K_CONSTRAINT : K_COLLISION, neg, k.r2, o)) return;
+    if (!fp_screen(S, i, j, constrained ? K_CONSTRAINT : K_COLLISION, neg, k.r2, o, A.type, tj)) return;
     if (!constrained && o.lopot0 && o.uppot0) { v.st = SC_NONE; v.warn = o.warn; return; }
     if (o.inf) return;
     int st = 1; Iv d2 = o.up;
@@ -369,24 +468,16 @@ __device__ int find_pair_r(const DSys &S, int a1, int a2, int kind, bool neg, do
     double dmin, dmax;
     int sn;
     if (kind == K_CONSTRAINT) {
-        int k = S.con_off[a1], e = S.con_off[a1 + 1];
-        for (; k < e; k++) if (S.con_j[k] == a2) break;
-        if (k == e) { *bad = 1; return -1; }
+        const int k = con_index(S, a1, a2);
+        if (k < 0) { *bad = 1; return -1; }
         dmin = S.con_dmin[k]; dmax = S.con_dmax[k]; sn = S.con_step_n[k]; key = S.con_key + 2 * k;
         int so = S.con_step_off[k];
         sd = S.con_step_d + so; se = S.con_step_e + so; skey = S.con_stepkey + 2 * so;
     } else {
         int e;
         if (kind == K_COLLISION) {
-            int t1 = S.type[a1], t2 = S.type[a2];
-            if (dbl_pos(S.pair_dmin[tab_idx(0, t1, t2)])) e = tab_idx(0, t1, t2);
-            else {
-                int a = type_change(t1, 0), b = type_change(t2, 0);
-                if (dbl_pos(S.pair_dmin[tab_idx(0, a, t2)])) e = tab_idx(0, a, t2);
-                else if (dbl_pos(S.pair_dmin[tab_idx(0, t1, b)])) e = tab_idx(0, t1, b);
-                else if (dbl_pos(S.pair_dmin[tab_idx(0, a, b)])) e = tab_idx(0, a, b);
-                else { *bad = 1; return -1; }
-            }
+            e = S.rp_idx[S.type[a1] * NT + S.type[a2]];   // RightPair, resolved on the host
+            if (e < 0) { *bad = 1; return -1; }
         } else {   // K_HB
             int tn = hb_model(S, a1, a2, bad);
             if (tn < 0) { *bad = 1; tn = 0; }
@@ -578,6 +669,17 @@ __device__ void hbb_fresh(const DSys &S, const double *xi, int i, HbbOut &r) {
     r.t = t; r.pot = pot; r.sub = sub; r.warn = warn; r.bad = bad;
 }
 
+// RightPair's type-pair index in shared memory for the kernel's lifetime (S: the
+// block's shared descriptor)
+__device__ __forceinline__ void stage_rp(DSys &S) {
+    __shared__ int16_t rp_sh[NT * NT];
+    const int16_t *src = S.rp_idx;
+    for (int k = threadIdx.x; k < NT * NT; k += blockDim.x) rp_sh[k] = src[k];
+    __syncthreads();
+    if (threadIdx.x == 0) S.rp_idx = rp_sh;
+    __syncthreads();
+}
+
 // ---- per-cell atom arrays (screened path) --------------------------------------------
 // Cell c holds cell_cnt[c] atoms in cell_arr[c*maxc ...] in insertion order, so the
 // reference's list (head = most recently inserted, src/Events.c:158-200) reads
@@ -725,6 +827,7 @@ struct PairScal {                 // per-atom block scalars of one two-atom pred
     unsigned u_key[2], dup_key[2];
     float uprime[2], nowf;
     double xi[2][3];              // lzx(i): the atom's FP64 position now
+    AtomI A[2];
     double pcc_abs[2], th_abs[2]; // PCC / thermostat offers as stored (absolute in lazy mode)
     int pcc_pos[2], th_pos[2];    // the offer's time is > 0 (JobAssign's test)
     int64_t smp0;                 // sample index of the target's thermostat draw
@@ -856,7 +959,12 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         PS.u_key[a] = f_key(INFINITY); PS.dup_key[a] = f_key(-INFINITY);
         PS.warn_excl[a] = 0; PS.rn[a] = 0; PS.over[a] = 0;
         PS.xi[a][0] = lzx(S, S.x, S.vx, i); PS.xi[a][1] = lzx(S, S.y, S.vy, i); PS.xi[a][2] = lzx(S, S.z, S.vz, i);
+        load_atom_i(S, i, PS.xi[a], PS.A[a]);
         atom_piv(S, i, PS.P[a]);
+    }
+    if (S.shadow_ok && tid >= T - 32 && tid < T - 32 + 7 * na) {   // t and p moved: refresh their shadows
+        const int l = tid - (T - 32);
+        shadow_field(S, l < 7 ? t : p, l % 7);
     }
     for (int a = 0; a < na; a++) {
         if (warp == (a % nw)) {
@@ -890,7 +998,7 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         } else {
             j = M.nbj[a][e - nb];
             const bool hb = PS.mode[a] == 2;
-            screen_cell(S, i, j, PS.P[a], hb, a == 1 && j == t, v[0], v[1]);
+            screen_cell(S, i, j, PS.P[a], PS.A[a], hb, a == 1 && j == t, v[0], v[1]);
             ne = hb ? 2 : 1;
         }
         for (int x = 0; x < ne; x++) {

@@ -70,6 +70,7 @@ __global__ void sweep_predict_kernel(const DSys *systems) {
     }
     __syncthreads();
     if (C.err) return;
+    stage_rp(S);
     ShmS MS;
     carve_screen(MS, S.nbcap);
     const int64_t base = C.smp_used;
@@ -163,6 +164,7 @@ __global__ void sweep_verify_kernel(const DSys *systems) {
     if (threadIdx.x == 0) { S = systems[blockIdx.y]; S.now = S.sc->time; }
     __syncthreads();
     if (S.sc->err) return;
+    stage_rp(S);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     unsigned char *p = smem + w * verify_warp_bytes(S.nbcap);
     int32_t *nbj = (int32_t *)p; p += al16((size_t)S.nbcap * 4);
@@ -231,6 +233,7 @@ __global__ void sweep_fix_kernel(const DSys *systems, int full) {
     }
     __syncthreads();
     if (C.err) return;
+    stage_rp(S);
     ShmS MS;
     carve_screen(MS, S.nbcap);
     const int64_t base = C.smp_used;
