@@ -385,9 +385,9 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             d.sw_hbit = cv.take<int32_t>(N1);
             d.sw_flag = cv.take<int32_t>(N1);
             d.sw_warn = cv.take<int32_t>(N1);
-            d.sx = cv.take<float>(N1); d.sy = cv.take<float>(N1); d.sz = cv.take<float>(N1);
-            d.svx = cv.take<float>(N1); d.svy = cv.take<float>(N1); d.svz = cv.take<float>(N1);
-            d.stl = cv.take<float>(N1);
+            // the records pack a cell index in 10 bits per axis
+            d.shr = s.cellnum[0] <= 1024 && s.cellnum[1] <= 1024 && s.cellnum[2] <= 1024 ? cv.take<float4>(N1 * 4)
+                                                                                        : nullptr;
             d.maxc = std::min<int32_t>(kMaxPerCell, m.n);
             d.cell_cnt = cv.take<int32_t>((size_t)m.ncell + 1);
             d.cell_arr = cv.take<int32_t>(((size_t)m.ncell + 1) * d.maxc);
@@ -524,7 +524,6 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         cut *= cut;
         f32_bracket(cut, d.cut32);
         d.cut_key = host_tkey(cut);
-        d.rq = nextafterf((float)sqrt(cut), INFINITY) * (1.0f + 0x1p-20f);
         f32_bracket(SDMD_ZERO, d.zero32);
         for (int q = 0; q < 3; q++) f32_bracket(s.box[q], d.box32 + 2 * q);
     }

@@ -113,12 +113,14 @@ struct DSys {
     // i's constraint list (first occurrence), -1 for none; con_ok[i] = 0 when a
     // partner lies outside the window (the list is then searched)
     const int8_t *con_win, *con_ok;
-    // lazy mode, screened path: FP32 copies (round to nearest) of x, v and of
-    // tloc - T0, for a cheap rigorous distance reject; valid while shadow_ok
-    float *sx, *sy, *sz, *svx, *svy, *svz, *stl;
+    // lazy mode, screened path: per atom a 64-byte record of outward-rounded FP32
+    // intervals -- {x, y}, {z, vx}, {vy, vz}, {tloc - T0, packed cell} -- so that a
+    // candidate's position interval costs FP32 work only; valid while shadow_ok.
+    // [nlo, nhi] holds now - T0 for the event being predicted.
+    float4 *shr;
     double T0;
     int32_t shadow_ok;
-    float rq;                // a float above sqrt((0.9 cutoff)^2), for the per-axis reject
+    float nlo, nhi;
 };
 
 // position component of atom j at the current time (lazy mode extrapolates)

@@ -886,7 +886,10 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
     __shared__ int32_t sh_t, sh_p, sh_exec, sh_go;
     __shared__ double sh_dt;
     __shared__ int32_t rec_partner, rec_type, rec_sub;
-    __shared__ int32_t sh_move[3], sh_cells_ok;
+    __shared__ int32_t sh_move[3], sh_cells_ok, sh_rebase;
+    // the records' epoch T0 moves to the current time every 4N pops, so that the
+    // interval of now - T0 stays about one mean free flight wide
+    int64_t rebase_at = C.pops + 4 * (int64_t)S.n;
     if (tid == 0) {
         B.err = 0; B.warn = 0; C = *S.sc;
         if (!C.cbt_built && !C.err) { C.err = SDMD_EINVAL; C.err_atom = 0; *S.sc = C; }   // prepare() first
@@ -905,13 +908,13 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
         __syncthreads();
         if (tid == 0) sh_cells_ok = B.err == 0;
         stage_rp(S);
-        if (S.lazy && S.sx) {   // FP32 shadows of every atom for this launch (epoch T0 = now)
+        if (S.lazy && S.shr) {   // interval records of every atom for this launch (epoch T0 = now)
             if (tid == 0) S.T0 = C.time;
             __syncthreads();
             for (int k = 1 + tid; k <= S.n; k += T)
-                for (int f = 0; f < 7; f++) shadow_field(S, k, f);
+                for (int w = 0; w < 4; w++) shadow_word(S, k, w);
             __syncthreads();
-            if (tid == 0) S.shadow_ok = 1;
+            if (tid == 0) { S.shadow_ok = 1; shadow_now(S); }
             __syncthreads();
         }
     }
@@ -932,6 +935,11 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
                 if (S.lazy) {   // absolute event times: the clock jumps to the event
                     sh_dt = S.ev_time[t] - C.time;
                     S.now = S.ev_time[t];
+                    sh_rebase = 0;
+                    if (S.shadow_ok) {
+                        if (C.pops >= rebase_at) { S.T0 = S.now; rebase_at = C.pops + 4 * (int64_t)S.n; sh_rebase = 1; }
+                        shadow_now(S);
+                    }
                 } else {
                     sh_dt = S.ev_time[t];
                 }
@@ -941,6 +949,13 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
         }
         __syncthreads();
         if (!sh_go) break;
+        if constexpr (SCR) {
+            if (S.lazy && S.shadow_ok && sh_rebase) {   // every record against the new epoch
+                for (int k = 1 + tid; k <= S.n; k += T)
+                    for (int w = 0; w < 4; w++) shadow_word(S, k, w);
+                __syncthreads();
+            }
+        }
         const double dt = sh_dt;
         if (!S.lazy) {
             for (int i = 1 + tid; i <= S.n; i += T) {      // UpdateData + TimeForward
@@ -981,6 +996,9 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
         }
         if (B.err) break;
         if constexpr (SCR) {
+            // a denied event still brought p's position to now: its record follows
+            // (predict_two refreshes the atoms it predicts)
+            if (S.shadow_ok && !sh_exec && p && tid < 4) shadow_word(S, p, tid);
             predict_two(S, t, sh_exec ? p : 0, MS, PS, B, C);
             if (tid < 32 && B.err == 0) {
                 cbt_update_warp(S, t);

@@ -90,8 +90,9 @@ __device__ __forceinline__ bool dbl_pos(double d) { return __double_as_longlong(
 // ---- positions and pair kinematics as intervals ---------------------------------
 struct PIv { Iv x[3], v[3]; int c[3]; };
 
-// the FP64 position lzx() would produce, and the velocity, of atom j
-__device__ __forceinline__ void atom_piv(const DSys &S, int j, PIv &P) {
+// the FP64 position lzx() would produce, and the velocity, of atom j, from its
+// FP64 fields (rounded to float and widened: FP64-pipe conversions)
+__device__ __forceinline__ void atom_piv_d(const DSys &S, int j, PIv &P) {
     const double *X[3] = {S.x, S.y, S.z}, *V[3] = {S.vx, S.vy, S.vz};
     Iv dti{0.f, 0.f};
     if (S.lazy) dti = ivd(S.now - S.tloc[j]);
@@ -102,6 +103,50 @@ __device__ __forceinline__ void atom_piv(const DSys &S, int j, PIv &P) {
         P.x[d] = S.lazy ? iadd(xv, imul(vv, dti)) : xv;
     }
     P.c[0] = S.cx[j]; P.c[1] = S.cy[j]; P.c[2] = S.cz[j];
+}
+
+// One word of atom k's interval record (w = 0..3).  x and v are doubles, so
+// [rd, ru] holds them exactly; tloc - T0 is an FP64 difference, one rounding away
+// from the real one, so its bounds step one more float outward.  Then
+// (now - T0) - (tloc - T0) in outward-rounded FP32 holds the real now - tloc,
+// hence also fl(now - tloc), since rounding to nearest is monotone and the
+// bounds are doubles themselves; the same holds for every later step of lzx().
+__device__ __forceinline__ void shadow_word(const DSys &S, int k, int w) {
+    float4 r;
+    switch (w) {
+        case 0: r = make_float4(__double2float_rd(S.x[k]), __double2float_ru(S.x[k]),
+                                __double2float_rd(S.y[k]), __double2float_ru(S.y[k])); break;
+        case 1: r = make_float4(__double2float_rd(S.z[k]), __double2float_ru(S.z[k]),
+                                __double2float_rd(S.vx[k]), __double2float_ru(S.vx[k])); break;
+        case 2: r = make_float4(__double2float_rd(S.vy[k]), __double2float_ru(S.vy[k]),
+                                __double2float_rd(S.vz[k]), __double2float_ru(S.vz[k])); break;
+        default: {
+            const double d = S.tloc[k] - S.T0;
+            r = make_float4(f_dn(__double2float_rd(d)), f_up(__double2float_ru(d)),
+                            __int_as_float(S.cx[k] | S.cy[k] << 10 | S.cz[k] << 20), 0.f);
+        }
+    }
+    S.shr[4 * (size_t)k + w] = r;
+}
+// [nlo, nhi] around the real now - T0 (the same outward step as tloc - T0)
+__device__ __forceinline__ void shadow_now(DSys &S) {
+    const double d = S.now - S.T0;
+    S.nlo = f_dn(__double2float_rd(d));
+    S.nhi = f_up(__double2float_ru(d));
+}
+
+// atom_piv_d()'s intervals, from the record when the records are valid
+__device__ __forceinline__ void atom_piv(const DSys &S, int j, PIv &P) {
+    if (!S.shadow_ok) { atom_piv_d(S, j, P); return; }
+    const float4 *r = S.shr + 4 * (size_t)j;
+    const float4 a = r[0], b = r[1], c = r[2], e = r[3];
+    const Iv dt = isub(ivc(S.nlo, S.nhi), ivc(e.x, e.y));
+    P.v[0] = ivc(b.z, b.w); P.v[1] = ivc(c.x, c.y); P.v[2] = ivc(c.z, c.w);
+    P.x[0] = iadd(ivc(a.x, a.y), imul(P.v[0], dt));
+    P.x[1] = iadd(ivc(a.z, a.w), imul(P.v[1], dt));
+    P.x[2] = iadd(ivc(b.x, b.y), imul(P.v[2], dt));
+    const int cp = __float_as_int(e.z);
+    P.c[0] = cp & 1023; P.c[1] = (cp >> 10) & 1023; P.c[2] = cp >> 20;
 }
 
 struct KIv { Iv r2, b, v2; };
@@ -155,30 +200,12 @@ struct AtomI {
     int32_t nb[4];
     int32_t win[9];               // its conn_win row
     int64_t cnt;                  // ev_counter
-    float pf[3];                  // lzx(i) rounded to float (lazy reject)
-    float nowr;                   // now - T0 rounded to float
 };
 __device__ __forceinline__ void load_atom_i(const DSys &S, int i, const double *xi, AtomI &A) {
     A.hbb = S.hb_bond[i]; A.role = S.hb_role[i]; A.type = S.type[i]; A.prot = S.protein[i]; A.aa = S.aanum[i];
     for (int q = 0; q < 4; q++) A.nb[q] = S.nb_partner[4 * i + q];
     for (int q = 0; q < 9; q++) A.win[q] = S.conn_win[9 * i + q];
     A.cnt = S.ev_counter[i];
-    if (S.shadow_ok) {
-        for (int d = 0; d < 3; d++) A.pf[d] = __double2float_rn(xi[d]);
-        A.nowr = __double2float_rn(S.now - S.T0);
-    }
-}
-// lazy mode: one field of the FP32 shadow of atom k (f = 0..6: x y z vx vy vz, tloc - T0)
-__device__ __forceinline__ void shadow_field(const DSys &S, int k, int f) {
-    switch (f) {
-        case 0: S.sx[k] = __double2float_rn(S.x[k]); break;
-        case 1: S.sy[k] = __double2float_rn(S.y[k]); break;
-        case 2: S.sz[k] = __double2float_rn(S.z[k]); break;
-        case 3: S.svx[k] = __double2float_rn(S.vx[k]); break;
-        case 4: S.svy[k] = __double2float_rn(S.vy[k]); break;
-        case 5: S.svz[k] = __double2float_rn(S.vz[k]); break;
-        default: S.stl[k] = __double2float_rn(S.tloc[k] - S.T0); break;
-    }
 }
 
 // connection-map bits of (i, j) from the per-atom window (row scan outside it)
@@ -354,10 +381,10 @@ __device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, const Ato
     vc.warn = 0; vc.dup = 0; vc.st = SC_NONE;
     vh.warn = 0; vh.dup = 0; vh.st = SC_NONE;
     if (j == i) return;
+    PIv J; atom_piv(S, j, J);                          // loads issued with the rest of j's fields
     const int evp = S.ev_partner[j], evt = S.ev_type[j];
     const int64_t evpc = S.ev_pcounter[j];
     const int rj = S.hb_role[j], tj = S.type[j], hbj = S.hb_bond[j], pj = S.protein[j], aj = S.aanum[j];
-    const int cj[3] = {S.cx[j], S.cy[j], S.cz[j]};
     const bool named = j < S.dup_limit && evp == i && evpc == A.cnt;
     bool need_c = true;
     if (named && evt == SDMD_EV_COLLISION) { vc.st = SC_REFINE; vc.dup = 1; need_c = false; }
@@ -388,31 +415,6 @@ __device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, const Ato
         if ((bits & 1) || A.hbb == j || nbh) need_c = false;
     }
     if (!need_c && !need_h) return;
-    if (S.shadow_ok) {
-        // Lazy mode: j's FP64 position lzx(j) is x + v * fl(now - tloc).  From the
-        // float shadows, each axis of r_i - r_j is known to within eb (the rounding
-        // of every operand and step, with a factor 4 to spare); an axis whose
-        // separation certainly exceeds rq puts r2 above the scan radius for both the
-        // collision and the HB scan.
-        const float tlj = S.stl[j], dtj = __fsub_rn(A.nowr, tlj);
-        const float xj[3] = {S.sx[j], S.sy[j], S.sz[j]}, vj[3] = {S.svx[j], S.svy[j], S.svz[j]};
-        const float tsum = fabsf(dtj) + fabsf(A.nowr) + fabsf(tlj);
-        bool far = false;
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-            float pj = __fmaf_rn(vj[d], dtj, xj[d]), bx = 0.f;
-            if (I.c[d] != cj[d]) {
-                if (I.c[d] == 0 && cj[d] == S.cn[d] - 1) { pj = pj - S.box32[2 * d]; bx = S.box32[2 * d + 1]; }
-                else if (I.c[d] == S.cn[d] - 1 && cj[d] == 0) { pj = pj + S.box32[2 * d]; bx = S.box32[2 * d + 1]; }
-            }
-            const float dx = A.pf[d] - pj;
-            const float eb = 0x1p-19f * (fabsf(A.pf[d]) + fabsf(xj[d]) + fabsf(pj) + fabsf(vj[d]) * tsum + bx +
-                                         fabsf(dx)) + 0x1p-100f;
-            if (fabsf(dx) - eb > S.rq) far = true;
-        }
-        if (far) return;   // both verdicts stay "none": r2 > (0.9 cutoff)^2 certainly
-    }
-    PIv J; atom_piv(S, j, J);
     KIv k; kin_iv(S, I, J, k);
     if (need_h) screen_hbs_k(S, i, j, k, vh);
     if (!need_c) return;
@@ -960,11 +962,11 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         PS.warn_excl[a] = 0; PS.rn[a] = 0; PS.over[a] = 0;
         PS.xi[a][0] = lzx(S, S.x, S.vx, i); PS.xi[a][1] = lzx(S, S.y, S.vy, i); PS.xi[a][2] = lzx(S, S.z, S.vz, i);
         load_atom_i(S, i, PS.xi[a], PS.A[a]);
-        atom_piv(S, i, PS.P[a]);
+        atom_piv_d(S, i, PS.P[a]);                     // its record is being refreshed below
     }
-    if (S.shadow_ok && tid >= T - 32 && tid < T - 32 + 7 * na) {   // t and p moved: refresh their shadows
+    if (S.shadow_ok && tid >= T - 32 && tid < T - 32 + 4 * na) {   // t and p moved: refresh their records
         const int l = tid - (T - 32);
-        shadow_field(S, l < 7 ? t : p, l % 7);
+        shadow_word(S, l < 4 ? t : p, l & 3);
     }
     for (int a = 0; a < na; a++) {
         if (warp == (a % nw)) {
