@@ -14,6 +14,8 @@ packs the dumps into compressed .npz fixtures that travel with the repository:
                doubles (dt, time, v_target, v_partner, new event times)
   ckpt<K>/*    state after K executed events
   final/*      state at the end of the traced run
+  meta/*       event count, checkpoints, the harness summary, and the run's inputs
+               (.gro text, parameter.txt, the test-local Wall.txt when there is one)
 
 Usage: python tests/golden/make_golden.py [case ...]
 """
@@ -129,6 +131,11 @@ def run_case(name, gro_text, params, n_events, ckpts, wall_lib=None, keep_trace_
         arrays["meta/ckpts"] = np.array(ckpts, np.int64)
         arrays["meta/summary"] = np.frombuffer(("\n".join(summary)).encode(), np.uint8)
         arrays["meta/rng_pre"] = rng_state_after(int(arrays["pre/seed"][0]), int(arrays["pre/rand_calls"][0]))
+        # the run's own inputs, so that the host-side builder can be checked against pre/*
+        arrays["meta/gro"] = np.frombuffer(gro_text.encode(), np.uint8)
+        arrays["meta/parameter"] = np.frombuffer(PARAM_TEMPLATE.format(**params).encode(), np.uint8)
+        if wall_lib is not None:
+            arrays["meta/wall_lib"] = np.frombuffer(wall_lib.encode(), np.uint8)
         out = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(out, **arrays)
         print(f"{name}: {summary[0] if summary else ''} -> {os.path.getsize(out) / 1024:.0f} KiB")

@@ -41,7 +41,7 @@ def assert_state_equal(a, ref, keys=DYN):
 
 
 @SCREENS
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl"])
 def test_sweep_matches_reference(golden, engine_mod, case, screen):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -53,7 +53,7 @@ def test_sweep_matches_reference(golden, engine_mod, case, screen):
 
 
 @SCREENS
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl"])
 def test_loop_matches_reference_event_for_event(golden, engine_mod, case, screen):
     d = golden(case)
     ids, dts = d["trace/ids"], d["trace/dt"]
@@ -75,6 +75,8 @@ def test_loop_matches_reference_event_for_event(golden, engine_mod, case, screen
     assert_state_equal(s.a, ref)
     assert s.counters == ref["_counters"]
     assert s.time == ref["_time"]
+    if case == "ala10_cyl":   # WallTime / WallEvent in the cylinder (axis x)
+        assert s.counters["wall"] > 0
 
 
 @SCREENS
@@ -120,6 +122,35 @@ def test_batch_of_systems_matches_oracle(golden, engine_mod, screen):
         assert rc == 0
         assert_state_equal(s.a, r.a)
         assert s.counters == r.counters and s.time == r.time
+
+
+@SCREENS
+def test_batch_of_wall_replicas_matches_oracle(golden, engine_mod, screen):
+    """Eight replicas in the smooth cylinder (the shape of the wall benchmark),
+    each with its own rand() stream and temperature: each equals its oracle run."""
+    from oracle import oracle as O
+    from tests.golden.make_golden import rng_state_after
+    d = golden("ala10_cyl")
+    systems = []
+    for k in range(8):
+        s = from_fixture(d, "pre")
+        s.rng = rng_state_after(100 + k, 0)
+        s.scal["temperature"] = 0.55 + 0.02 * k
+        systems.append(s)
+    refs = [s.copy() for s in systems]
+    with engine_mod.Engine(systems, threads=64, screen=screen) as eng:
+        eng.prepare(full=True)
+        eng.run(6000)
+        eng.download()
+    walls = 0
+    for s, r in zip(systems, refs):
+        O.predict_all(r)
+        rc, _, _ = O.Loop(r).run(6000)
+        assert rc == 0
+        assert_state_equal(s.a, r.a)
+        assert s.counters == r.counters and s.time == r.time
+        walls += s.counters["wall"]
+    assert walls > 0
 
 
 @SCREENS

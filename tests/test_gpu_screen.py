@@ -67,6 +67,16 @@ def test_screen_equals_fp64_on_ala10(golden, engine_mod, advance):
 
 
 @pytest.mark.parametrize("advance", [0, 1], ids=["eager", "lazy"])
+def test_screen_equals_fp64_with_a_cylinder_wall(golden, engine_mod, advance):
+    d = golden("ala10_cyl")
+    a, b = from_fixture(d, "pre"), from_fixture(d, "pre")
+    run(engine_mod, a, 0, advance, 40000)
+    run(engine_mod, b, 1, advance, 40000)
+    assert_same(b, a)
+    assert b.counters["wall"] > 0
+
+
+@pytest.mark.parametrize("advance", [0, 1], ids=["eager", "lazy"])
 def test_screen_equals_fp64_on_mixed_chains(engine_mod, mixed_system, advance):
     a, b = mixed_system.copy(), mixed_system.copy()
     run(engine_mod, a, 0, advance, 20000)

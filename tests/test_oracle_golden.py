@@ -28,7 +28,7 @@ def assert_state_equal(sys_, ref, keys=DYN):
             raise AssertionError(f"{k} differs at {idx}: {a[idx]} vs {b[idx]}")
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl"])
 def test_sweep_and_tree(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -39,7 +39,7 @@ def test_sweep_and_tree(golden, case):
     assert np.array_equal(node, d["cbt/cbt_node"]) and np.array_equal(leaf, d["cbt/cbt_leaf"])
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl"])
 def test_trace_event_for_event(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -59,6 +59,8 @@ def test_trace_event_for_event(golden, case):
     ref = fixture_dynamic(d, "final")
     assert_state_equal(s, ref)
     assert s.counters == ref["_counters"] and s.time == ref["_time"]
+    if case == "ala10_cyl":   # the smooth cylinder wall (WallTime / WallEvent) is exercised
+        assert s.counters["wall"] > 0
 
 
 def test_long_run_checkpoints(golden):
