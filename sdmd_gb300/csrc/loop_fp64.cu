@@ -39,14 +39,22 @@ __device__ inline void set_err(Blk &B, int code, int atom) {
     if (B.err == 0) { B.err = code; B.err_atom = atom; }
 }
 
-// lazy mode: bring atom a's position to the current time before it changes
-__device__ inline void sync_atom(const DSys &S, int a) {
-    if (!S.lazy || a <= 0) return;
-    double dt = S.now - S.tloc[a];
-    S.x[a] = S.x[a] + S.vx[a] * dt;
-    S.y[a] = S.y[a] + S.vy[a] * dt;
-    S.z[a] = S.z[a] + S.vz[a] * dt;
-    S.tloc[a] = S.now;
+// lazy mode: bring the target t and the partner p (when > 0) to the current time
+// before they change, x += v * (now - tloc) per axis.  Lanes 0..5 of warp 0 take
+// one (atom, axis) each: the six independent FP64 chains share warp-instructions.
+__device__ inline void sync_pair_warp0(const DSys &S, int t, int p) {
+    const int l = threadIdx.x;
+    if (!S.lazy || l >= 6) return;
+    const int a = l < 3 ? t : p, d = l % 3;
+    if (a > 0) {
+        double *X = d == 0 ? S.x : (d == 1 ? S.y : S.z);
+        const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
+        const double dt = S.now - S.tloc[a];
+        X[a] = X[a] + V[a] * dt;
+    }
+    __syncwarp(0x3fu);                                 // every axis has read the old tloc
+    if (d == 0 && a > 0) S.tloc[a] = S.now;
+    __syncwarp(0x3fu);
 }
 
 // ---------------------------------------------------------------------------
@@ -930,21 +938,24 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
             if (go && S.thermostat && C.smp_avail - C.smp_used < 5) { C.paused = 1; go = 0; }
             sh_go = go;
             if (go) {
-                int t = S.cbt_node[1];
+                const int t = S.cbt_node[1];
+                // the popped event's fields into registers before any shared store
+                const double tev = S.ev_time[t];
+                const int rp = S.ev_partner[t], rt = S.ev_type[t], rs = S.ev_sub[t];
+                rec_partner = rp; rec_type = rt; rec_sub = rs;
                 sh_t = t;
                 if (S.lazy) {   // absolute event times: the clock jumps to the event
-                    sh_dt = S.ev_time[t] - C.time;
-                    S.now = S.ev_time[t];
+                    sh_dt = tev - C.time;
+                    S.now = tev;
                     sh_rebase = 0;
                     if (S.shadow_ok) {
                         if (C.pops >= rebase_at) { S.T0 = S.now; rebase_at = C.pops + 4 * (int64_t)S.n; sh_rebase = 1; }
                         shadow_now(S);
                     }
                 } else {
-                    sh_dt = S.ev_time[t];
+                    sh_dt = tev;
                 }
-                rec_partner = S.ev_partner[t]; rec_type = S.ev_type[t]; rec_sub = S.ev_sub[t];
-                sh_p = rec_partner > 0 ? rec_partner : 0;
+                sh_p = rp > 0 ? rp : 0;
             }
         }
         __syncthreads();
@@ -967,8 +978,9 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
             __syncthreads();
         }
         const int t = sh_t, p = sh_p;
+        sync_pair_warp0(S, t, p);
         if (tid == 0) {
-            if (S.lazy) { C.time = S.now; sync_atom(S, t); sync_atom(S, p); }
+            if (S.lazy) C.time = S.now;
             else C.time += dt;
             int hazard = p > 0 && S.ev_pcounter[t] < S.ev_counter[p];   // HazardCheck
             sh_exec = !hazard;

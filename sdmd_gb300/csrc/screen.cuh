@@ -756,10 +756,16 @@ __device__ int gather_warp(const DSys &S, int i, int32_t *nbj, int nbcap, int *o
     }
     int tot = __shfl_sync(0xffffffffu, incl, 31);
     if (tot > nbcap) { *overflow = 1; return 0; }
-    if (lane < 27) {
+    if (lane < 27) {   // up to eight independent loads in flight per lane
         const int32_t *arr = S.cell_arr + (size_t)cell * M;
         const int off = incl - c;
-        for (int m = 0; m < c; m++) nbj[off + m] = arr[c - 1 - m];
+        for (int m0 = 0; m0 < c; m0 += 8) {
+            int32_t v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) if (m0 + u < c) v[u] = arr[c - 1 - m0 - u];
+#pragma unroll
+            for (int u = 0; u < 8; u++) if (m0 + u < c) nbj[off + m0 + u] = v[u];
+        }
     }
     __syncwarp();
     return tot;
@@ -906,24 +912,29 @@ __device__ inline void fold_entry(const DSys &S, Cur &c, const Slots &L, int q, 
     if (info & F_FRESH) job_assign_pre(S, c, j, L.t[q], info & F_POS, L.pot[q], (info >> 8) & 0xff, type);
 }
 
-// Predict's fold for atom a of the pair, in the reference's order (thread 0)
-__device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS, Blk &B, DScal &C) {
+// Predict's fold for atom a of the pair, in the reference's order (thread 0).
+// Warnings and errors gather in a register copy of the block scalars and merge
+// once at the end: a store to the shared block scalars between two loads of the
+// state arrays would serialise the loads.
+__device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS, Blk &Bs, DScal &C) {
     const int i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a], rn = PS.rn[a];
     const Slots &L = M.R[a];
+    Blk B = Bs;
+    B.warn = 0;
     Cur c;
     cur_load(S, i, c);
     int q = 0, bad = 0;
     for (; q < rn && M.rl[a][q] < nb + nn; q++)
         fold_entry(S, c, L, q, i, M.rl[a][q] < nb ? SDMD_EV_BOND : SDMD_EV_COLLISION, tnew, B);
     job_assign_pre(S, c, 0, PS.pcc_abs[a], PS.pcc_pos[a], 0, SDMD_SUB_INVALID, SDMD_EV_PCC);
+    int smp_take = 0;
     if (S.thermostat) {   // ThermostatTime: the sample was evaluated by a lane
         if (C.smp_used >= C.smp_avail || C.smp_used != PS.smp0 + a) set_err(B, SDMD_ETIMEOUT, 0);
         else {
-            C.smp_used++;
+            smp_take = 1;
             job_assign_pre(S, c, 0, PS.th_abs[a], PS.th_pos[a], 0, SDMD_SUB_INVALID, SDMD_EV_THERMOSTAT);
         }
     }
-    S.hb_itype[i] = SDMD_HB_NOEVENT;    // HBSkip is one-shot (src/TimePrediction.c:309-327)
     if (PS.mode[a] == 1) {
         const int j = S.hb_bond[i];
         if (!(j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
@@ -938,9 +949,13 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
     }
     hbnb_time(S, i, c, B, &bad);
     if (S.wall) wall_time(S, i, c, B, &bad);
+    S.hb_itype[i] = SDMD_HB_NOEVENT;    // HBSkip is one-shot (src/TimePrediction.c:309-327)
     cur_store(S, i, c);
     B.warn += PS.warn_excl[a];
     if (bad) set_err(B, SDMD_EHBMAP, i);
+    Bs.warn += B.warn;
+    if (B.err && !Bs.err) { Bs.err = B.err; Bs.err_atom = B.err_atom; }
+    C.smp_used += smp_take;
 }
 
 // Predict for the target t and (when p > 0) the partner p, after ResetTarget of
@@ -951,25 +966,35 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
     // 1. per-atom set-up and the two 27-cell gathers (one warp each)
     if (tid < na) {
         const int a = tid, i = a ? p : t;
-        PS.i[a] = i;
-        PS.nb[a] = S.bond_off[i + 1] - S.bond_off[i];
+        // Every load of atom i first, into registers, then the stores to shared
+        // memory: the state arrays may themselves live in shared memory (staged
+        // state), so a store between two loads would serialise their latencies.
+        const int nb = S.bond_off[i + 1] - S.bond_off[i];
+        const int hbit = S.hb_itype[i], hbb = S.hb_bond[i], role = S.hb_role[i];
+        const double xi[3] = {lzx(S, S.x, S.vx, i), lzx(S, S.y, S.vy, i), lzx(S, S.z, S.vz, i)};
+        AtomI A;
+        load_atom_i(S, i, xi, A);
+        PIv P;
+        atom_piv_d(S, i, P);                           // its record is being refreshed below
         int mode;
-        if (S.hb_itype[i] == SDMD_HB_SKIP) mode = 0;
-        else if (S.hb_bond[i] > 0) mode = 1;
-        else { int r = S.hb_role[i]; mode = (r == 'A' || r == 'D' || r == 'S') ? 2 : 0; }
+        if (hbit == SDMD_HB_SKIP) mode = 0;
+        else if (hbb > 0) mode = 1;
+        else mode = (role == 'A' || role == 'D' || role == 'S') ? 2 : 0;
+        PS.i[a] = i;
+        PS.nb[a] = nb;
         PS.mode[a] = mode;
         PS.u_key[a] = f_key(INFINITY); PS.dup_key[a] = f_key(-INFINITY);
         PS.warn_excl[a] = 0; PS.rn[a] = 0; PS.over[a] = 0;
-        PS.xi[a][0] = lzx(S, S.x, S.vx, i); PS.xi[a][1] = lzx(S, S.y, S.vy, i); PS.xi[a][2] = lzx(S, S.z, S.vz, i);
-        load_atom_i(S, i, PS.xi[a], PS.A[a]);
-        atom_piv_d(S, i, PS.P[a]);                     // its record is being refreshed below
+        PS.xi[a][0] = xi[0]; PS.xi[a][1] = xi[1]; PS.xi[a][2] = xi[2];
+        PS.A[a] = A;
+        PS.P[a] = P;
     }
     if (S.shadow_ok && tid >= T - 32 && tid < T - 32 + 4 * na) {   // t and p moved: refresh their records
         const int l = tid - (T - 32);
         shadow_word(S, l < 4 ? t : p, l & 3);
     }
-    for (int a = 0; a < na; a++) {
-        if (warp == (a % nw)) {
+    for (int a = 0; a < na; a++) {   // on warps 1 and 2 when there are: warp 0 does the set-up above
+        if (warp == ((1 + a) % nw)) {
             int ovf = 0;
             int nn = gather_warp(S, a ? p : t, M.nbj[a], S.nbcap, &ovf);
             if (lane == 0) { PS.nn[a] = nn; if (ovf) set_err(B, SDMD_ECAPACITY, a ? p : t); }
