@@ -134,6 +134,9 @@ def build_workload(name, rank):
     if name == "c3":
         return W.c3(seed=1 + rank), {"workload": "C3: 64 replicas of ALA x 10, temperatures geometric 270-500 K, "
                                                  "on-device replica exchange every 1e4 events per replica"}
+    if name == "c4":
+        return W.c4(seed=1 + rank), {"workload": "C4: 512 single random-sequence chains of 5-60 residues, box edge "
+                                                 "40 A * (N/59)^(1/3) (floor 27 A), Andersen NVT 280-400 K"}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -353,13 +356,17 @@ def cpu_baseline(system, seconds):
             "sample": f"{n} events of the same system from the post-sweep state (oracle/sdmd_oracle.c, gcc -O2)"}
 
 
+_WORKER_SYSTEMS = {}
+
+
 def _ref_worker(job):
     """One host process of the reference arm: the oracle loop on system k of the batch."""
     workload, k, n_events = job
     sys.path.insert(0, REPO)
     from oracle import oracle as O
-    systems, _ = build_workload(workload, 0)
-    s = systems[k]
+    if workload not in _WORKER_SYSTEMS:   # built (or loaded) once per worker process
+        _WORKER_SYSTEMS[workload] = build_workload(workload, 0)[0]
+    s = _WORKER_SYSTEMS[workload][k].copy()
     O.predict_all(s)
     loop = O.Loop(s)
     t0 = time.perf_counter()

@@ -109,11 +109,7 @@ def c3(n_replicas=64, t_lo=270.0, t_hi=500.0, seed=1):
     return out
 
 
-def c4(n_systems=512, lo=5, hi=60, seed=1, t_lo=280.0, t_hi=400.0, rng_seed0=5000):
-    """512 single chains, lengths uniform lo..hi residues with random sequences, box
-    edge 40 A * (N / 59)^(1/3) (C1's atom density) floored at 27 A (three 9 A
-    cells), temperatures uniform t_lo..t_hi.  Each system is built (and cached)
-    separately; returns the list of Systems."""
+def _c4_specs(n_systems, lo, hi, seed, t_lo, t_hi, rng_seed0):
     rng = np.random.default_rng(seed)
     seqs = random_sequences(n_systems, 0, seed, lo, hi)
     temps = rng.uniform(t_lo, t_hi, n_systems)
@@ -122,12 +118,41 @@ def c4(n_systems=512, lo=5, hi=60, seed=1, t_lo=280.0, t_hi=400.0, rng_seed0=500
         T = float(temps[k])
         natoms_est = 10.45 * len(seq)
         edge = max(27.0, 40.0 * (natoms_est / 59.0) ** (1.0 / 3.0))
-
-        def make(seq=seq, T=T, edge=edge, k=k):
-            d = _datadir(dict(temp=round(T * BOLTZMANN, 4), thermostat="Andersen", time=1e9))
-            gro = generate_gro(d, [seq], (edge, edge, edge), seed=seed * 100003 + k)
-            return build_system(d, gro_text=gro, seed=rng_seed0 + k)
-
-        out.append(cached(f"c4_{k}_{len(seq)}_{seed}_{round(T, 3)}", make))
+        out.append((k, seq, T, edge, seed * 100003 + k, rng_seed0 + k, f"c4_{k}_{len(seq)}_{seed}_{round(T, 3)}"))
     return out
+
+
+def _c4_one(spec):
+    k, seq, T, edge, gro_seed, rng_seed, key = spec
+
+    def make():
+        d = _datadir(dict(temp=round(T * BOLTZMANN, 4), thermostat="Andersen", time=1e9))
+        gro = generate_gro(d, [seq], (edge, edge, edge), seed=gro_seed)
+        return build_system(d, gro_text=gro, seed=rng_seed)
+
+    return cached(key, make)
+
+
+def c4(n_systems=512, lo=5, hi=60, seed=1, t_lo=280.0, t_hi=400.0, rng_seed0=5000, workers=None):
+    """512 single chains, lengths uniform lo..hi residues with random sequences, box
+    edge 40 A * (N / 59)^(1/3) (C1's atom density) floored at 27 A (three 9 A
+    cells), temperatures uniform t_lo..t_hi.  Each system is built (and cached)
+    separately, the missing ones in parallel on all host cores (spawned worker
+    processes); returns the list of Systems."""
+    specs = _c4_specs(n_systems, lo, hi, seed, t_lo, t_hi, rng_seed0)
+    from .host import HOST_LIB
+    stamp = int(os.path.getmtime(HOST_LIB)) if os.path.exists(HOST_LIB) else 0
+    missing = [sp for sp in specs if not os.path.exists(os.path.join(CACHE, f"{sp[-1]}_{stamp}.npz"))]
+    if len(missing) > 1:
+        import multiprocessing as mp
+        n = workers or min(len(missing), os.cpu_count() or 1)
+        with mp.get_context("spawn").Pool(n) as pool:
+            for _ in pool.imap_unordered(_c4_touch, missing):
+                pass
+    return [_c4_one(sp) for sp in specs]
+
+
+def _c4_touch(spec):
+    _c4_one(spec)
+    return spec[0]
 
