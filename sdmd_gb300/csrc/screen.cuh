@@ -59,22 +59,26 @@ __device__ __forceinline__ Iv imul(Iv a, Iv b) {
     float h1 = __fmul_ru(a.lo, b.lo), h2 = __fmul_ru(a.lo, b.hi), h3 = __fmul_ru(a.hi, b.lo), h4 = __fmul_ru(a.hi, b.hi);
     return {fminf(fminf(l1, l2), fminf(l3, l4)), fmaxf(fmaxf(h1, h2), fmaxf(h3, h4))};
 }
+// The helpers below select their operands first and then run one instruction
+// sequence for every sign case, so lanes of a warp in different cases do not
+// diverge (each case computes the same values as a branch per case would).
 __device__ __forceinline__ Iv isqr(Iv a) {
-    if (a.lo >= 0.f) return {__fmul_rd(a.lo, a.lo), __fmul_ru(a.hi, a.hi)};
-    if (a.hi <= 0.f) return {__fmul_rd(a.hi, a.hi), __fmul_ru(a.lo, a.lo)};
-    return {0.f, fmaxf(__fmul_ru(a.lo, a.lo), __fmul_ru(a.hi, a.hi))};
+    // the smaller magnitude bound: a.lo when a >= 0, -a.hi when a <= 0, else 0
+    const float m = a.lo >= 0.f ? a.lo : (a.hi <= 0.f ? -a.hi : 0.f);
+    return {__fmul_rd(m, m), fmaxf(__fmul_ru(a.lo, a.lo), __fmul_ru(a.hi, a.hi))};
 }
 // sqrt of an interval with a.lo >= 0 (IEEE round-to-nearest, stepped outward)
 __device__ __forceinline__ Iv isqrt(Iv a) {
-    float lo = a.lo > 0.f ? f_dn(__fsqrt_rn(a.lo)) : 0.f;
+    const float sl = __fsqrt_rn(fmaxf(a.lo, 0.f));
+    float lo = a.lo > 0.f ? f_dn(sl) : 0.f;
     return {lo > 0.f ? lo : 0.f, f_up(__fsqrt_rn(a.hi))};
 }
-// a / b with b.lo > 0 (IEEE round-to-nearest quotients, stepped outward)
+// a / b with b.lo > 0 (IEEE round-to-nearest quotients, stepped outward):
+// the lower quotient divides by b.hi when a.lo >= 0 (else b.lo), the upper one
+// by b.hi when a.hi <= 0 (else b.lo)
 __device__ __forceinline__ Iv idiv(Iv a, Iv b) {
-    float ql, qh;
-    if (a.lo >= 0.f) { ql = __fdiv_rn(a.lo, b.hi); qh = __fdiv_rn(a.hi, b.lo); }
-    else if (a.hi <= 0.f) { ql = __fdiv_rn(a.lo, b.lo); qh = __fdiv_rn(a.hi, b.hi); }
-    else { ql = __fdiv_rn(a.lo, b.lo); qh = __fdiv_rn(a.hi, b.lo); }
+    const float ql = __fdiv_rn(a.lo, a.lo >= 0.f ? b.hi : b.lo);
+    const float qh = __fdiv_rn(a.hi, a.hi <= 0.f ? b.hi : b.lo);
     return {f_dn(ql), f_up(qh)};
 }
 // is the FP64 value inside `a` below the FP64 threshold bracketed by thr[0..1]?
@@ -175,7 +179,7 @@ __device__ __forceinline__ Iv root_iv(const KIv &k, int st, Iv d2, bool &ok) {
     ok = D.lo >= 0.f && k.v2.lo > 0.f && D.hi < INFINITY;
     if (!ok) return {0.f, 0.f};
     Iv s = isqrt(D);
-    Iv num = iadd(ineg(k.b), st > 0 ? s : ineg(s));
+    Iv num = iadd(ineg(k.b), st > 0 ? s : ineg(s));   // a select, not a branch
     Iv t = idiv(num, k.v2);
     ok = t.lo <= t.hi;   // false for NaN
     return t;
@@ -501,16 +505,33 @@ __device__ int find_pair_r(const DSys &S, int a1, int a2, int kind, bool neg, do
     }
     o.lo = dmin; o.lopot = 0;
     const int col = neg ? 0 : 1;
+    // the first four steps are loaded together (a dependent load per step otherwise)
+    double pd[4], pe[4];
+    long long pk[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        pd[u] = u < sn ? sd[u] : 0.0;
+        pe[u] = u < sn ? se[u] : 0.0;
+        pk[u] = u < sn ? skey[2 * u + col] : 0;
+    }
     for (int q = 0; q < sn; q++) {
-        double d = sd[q];
+        double d, e;
+        long long kq;
+        if (q < 4) {   // static selects keep the prefetched values in registers
+            d = q == 0 ? pd[0] : (q == 1 ? pd[1] : (q == 2 ? pd[2] : pd[3]));
+            e = q == 0 ? pe[0] : (q == 1 ? pe[1] : (q == 2 ? pe[2] : pe[3]));
+            kq = q == 0 ? pk[0] : (q == 1 ? pk[1] : (q == 2 ? pk[2] : pk[3]));
+        } else {
+            d = sd[q]; e = se[q]; kq = skey[2 * q + col];
+        }
         if (dbl_is_zero(d)) break;
-        if (kd < skey[2 * q + col]) {
-            o.up = d; o.uppot = -1 * se[q]; o.acc = 0;
+        if (kd < kq) {
+            o.up = d; o.uppot = -1 * e; o.acc = 0;
             if (q == 0) return 0;
             if (kind == K_HB && q == sn - 1 && a1bond > 0) return 1;
             return cs;
         }
-        o.lo = d; o.lopot = se[q];
+        o.lo = d; o.lopot = e;
     }
     if (kind == K_HB && a1bond > 0) ++*warn;
     if (dbl_pos(dmax)) {
