@@ -203,12 +203,14 @@ struct AtomI {
     int32_t hbb, role, type, prot, aa;
     int32_t nb[4];
     int32_t win[9];               // its conn_win row
+    int32_t nbs;                  // nb_status: how many HB-neighbour partners
     int64_t cnt;                  // ev_counter
 };
 __device__ __forceinline__ void load_atom_i(const DSys &S, int i, const double *xi, AtomI &A) {
     A.hbb = S.hb_bond[i]; A.role = S.hb_role[i]; A.type = S.type[i]; A.prot = S.protein[i]; A.aa = S.aanum[i];
     for (int q = 0; q < 4; q++) A.nb[q] = S.nb_partner[4 * i + q];
     for (int q = 0; q < 9; q++) A.win[q] = S.conn_win[9 * i + q];
+    A.nbs = S.nb_status[i];
     A.cnt = S.ev_counter[i];
 }
 
@@ -848,6 +850,12 @@ struct ShmS {
     uint32_t *mask[2];            // entries to refine
     int32_t *rl[2];               // refined entries in scan order
     Slots R[2];                   // their exact FP64 results
+    // the partner j's stored event fields that the fold's JobAssign and
+    // CheckDuplication copy (counter, potential, sub-type), loaded by the refine
+    // lanes so that the fold reads shared memory only
+    int64_t *jcnt[2];
+    double *jpot[2];
+    int32_t *jsub[2];
     double *face;                 // PCC face times, 3 per atom
 };
 
@@ -870,6 +878,7 @@ __host__ __device__ inline size_t screen_smem_bytes_dev(int nbcap) {
     size_t b = fp64_smem_bytes_dev(nbcap);
     b += al16(2 * (size_t)nbcap * 4) + al16(2 * ecap) + al16(2 * ecap * 4) + al16(2 * words * 4);
     b += al16(2 * RC * 4) + 2 * (2 * al16(RC * 4) + 3 * al16(RC * 8)) + al16(6 * 8);
+    b += 2 * (2 * al16(RC * 8) + al16(RC * 4));
     return al16(b);
 }
 __device__ inline void carve_screen(ShmS &M, int nbcap) {
@@ -888,6 +897,7 @@ __device__ inline void carve_screen(ShmS &M, int nbcap) {
         M.mask[a] = mk + a * words; M.rl[a] = rl + a * RC;
         M.R[a].j = (int32_t *)take(RC * 4); M.R[a].info = (int32_t *)take(RC * 4);
         M.R[a].t = (double *)take(RC * 8); M.R[a].tdup = (double *)take(RC * 8); M.R[a].pot = (double *)take(RC * 8);
+        M.jcnt[a] = (int64_t *)take(RC * 8); M.jpot[a] = (double *)take(RC * 8); M.jsub[a] = (int32_t *)take(RC * 4);
     }
     M.face = (double *)take(6 * 8);
 }
@@ -917,20 +927,41 @@ constexpr int F_POS = 4;   // slot flag: the fresh time is > 0 (set by the refin
 
 // one refined offer of the fold (resolve() for a single slot); `tnew` is the
 // target atom whose fresh event may now duplicate this pair, or -1
-__device__ inline void fold_entry(const DSys &S, Cur &c, const Slots &L, int q, int i, int type, int tnew, Blk &B) {
+__device__ inline void fold_entry(const DSys &S, Cur &c, const ShmS &M, int a, int q, int i, int type, int tnew,
+                                  Blk &B) {
+    const Slots &L = M.R[a];
     int info = L.info[q];
     if (info < 0) return;
     const int j = L.j[q];
     double tdup = L.tdup[q];
+    // j's counter, potential and sub-type as the refine lanes loaded them; only the
+    // target's event (seen by the partner's fold) has changed since, so it is read live
+    int64_t jc = M.jcnt[a][q];
+    double jpo = M.jpot[a][q];
+    int js = M.jsub[a][q];
     if (j == tnew) {   // CheckDuplication sees the target's new event
         info &= ~F_DUP;
         if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == type && S.ev_pcounter[j] == S.ev_counter[i]) {
             info |= F_DUP; tdup = S.ev_time[j];
         }
+        jc = S.ev_counter[j]; jpo = S.ev_potential[j]; js = S.ev_sub[j];
     }
-    if ((info & F_DUP) && dup_assign(S, c, j, tdup, type)) return;
+    if (info & F_DUP) {   // dup_assign() with j's fields from above
+        const long long kt = tkey(tdup);
+        if (c.key > kt) {
+            c.partner = j; c.potential = jpo; c.sub = js; c.time = tdup; c.key = kt; c.type = type; c.pcounter = jc;
+            return;
+        }
+    }
     B.warn += (info >> 16) & 0xff;
-    if (info & F_FRESH) job_assign_pre(S, c, j, L.t[q], info & F_POS, L.pot[q], (info >> 8) & 0xff, type);
+    if ((info & F_FRESH) && (info & F_POS)) {   // job_assign_pre() with j's counter from above
+        const long long kt = tkey(L.t[q]);
+        if (c.key > kt) {
+            c.potential = L.pot[q]; c.sub = (info >> 8) & 0xff; c.time = L.t[q]; c.key = kt; c.type = type;
+            if (j) { c.partner = j; c.pcounter = jc; }
+            else c.partner = INVALID;
+        }
+    }
 }
 
 // Predict's fold for atom a of the pair, in the reference's order (thread 0).
@@ -939,14 +970,13 @@ __device__ inline void fold_entry(const DSys &S, Cur &c, const Slots &L, int q, 
 // state arrays would serialise the loads.
 __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS, Blk &Bs, DScal &C) {
     const int i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a], rn = PS.rn[a];
-    const Slots &L = M.R[a];
     Blk B = Bs;
     B.warn = 0;
     Cur c;
     cur_load(S, i, c);
     int q = 0, bad = 0;
     for (; q < rn && M.rl[a][q] < nb + nn; q++)
-        fold_entry(S, c, L, q, i, M.rl[a][q] < nb ? SDMD_EV_BOND : SDMD_EV_COLLISION, tnew, B);
+        fold_entry(S, c, M, a, q, i, M.rl[a][q] < nb ? SDMD_EV_BOND : SDMD_EV_COLLISION, tnew, B);
     job_assign_pre(S, c, 0, PS.pcc_abs[a], PS.pcc_pos[a], 0, SDMD_SUB_INVALID, SDMD_EV_PCC);
     int smp_take = 0;
     if (S.thermostat) {   // ThermostatTime: the sample was evaluated by a lane
@@ -966,9 +996,9 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
             job_assign_pre(S, c, j, h.t, h.pos, h.pot, h.sub, SDMD_EV_HB);
         }
     } else if (PS.mode[a] == 2) {
-        for (; q < rn; q++) fold_entry(S, c, L, q, i, SDMD_EV_HB, tnew, B);
+        for (; q < rn; q++) fold_entry(S, c, M, a, q, i, SDMD_EV_HB, tnew, B);
     }
-    hbnb_time(S, i, c, B, &bad);
+    if (PS.A[a].nbs > 0) hbnb_time(S, i, c, B, &bad);   // its loop runs over nb_status[i] partners
     if (S.wall) wall_time(S, i, c, B, &bad);
     S.hb_itype[i] = SDMD_HB_NOEVENT;    // HBSkip is one-shot (src/TimePrediction.c:309-327)
     cur_store(S, i, c);
@@ -1131,6 +1161,13 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
             const int e = M.rl[a][qq], i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
             const int kind = e < nb ? 1 : (e < nb + nn ? 0 : 2);
             if (kind % nw != warp) continue;
+            {   // the partner's stored event fields, for the fold (loads overlap the FP64 work)
+                const int jp = kind == 1 ? S.bond_j[S.bond_off[i] + e] : M.nbj[a][kind == 0 ? e - nb : e - nb - nn];
+                const int64_t jc = S.ev_counter[jp];
+                const double jpo = S.ev_potential[jp];
+                const int js = S.ev_sub[jp];
+                M.jcnt[a][qq] = jc; M.jpot[a][qq] = jpo; M.jsub[a][qq] = js;
+            }
             if (kind == 1) eval_bond_r(S, PS.xi[a], i, S.bond_off[i] + e, M.R[a], qq);
             else if (kind == 0) eval_collision_r(S, PS.xi[a], i, M.nbj[a][e - nb], M.R[a], qq, &bad);
             else eval_hb_scan_r(S, PS.xi[a], i, M.nbj[a][e - nb - nn], M.R[a], qq, &bad);
