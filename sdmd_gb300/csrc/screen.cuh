@@ -1040,6 +1040,8 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         PS.A[a] = A;
         PS.P[a] = P;
     }
+    if (tid == 2)   // |now| bound for step 4's lazy-mode margin (two FP64 conversions, off the chain)
+        PS.nowf = S.lazy ? fmaxf(fabsf(ivd(S.now).hi), fabsf(ivd(S.now).lo)) : 0.f;
     if (S.shadow_ok && tid >= T - 32 && tid < T - 32 + 4 * na) {   // t and p moved: refresh their records
         const int l = tid - (T - 32);
         shadow_word(S, l < 4 ? t : p, l & 3);
@@ -1062,7 +1064,6 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
     __syncthreads();
     if (B.err) return;
     // 2. PCC faces (exact, FP64) and the FP32 screen of every bond / collision / HB candidate
-    if (tid < 3 * na) M.face[tid] = pcc_face(S, PS.i[tid / 3], tid % 3);
     const int E0 = PS.E[0], E1 = na > 1 ? PS.E[1] : 0;
     const int S0 = PS.nb[0] + PS.nn[0], S1 = na > 1 ? PS.nb[1] + PS.nn[1] : 0;
     for (int g = tid; g < S0 + S1; g += T) {
@@ -1099,7 +1100,6 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
     // (PCC, thermostat, wall) leaves at the value of the last bond/collision record.
     // U' adds every duplicate time (and, for the partner, the target's bound).
     if (tid == 0) {
-        PS.nowf = S.lazy ? fmaxf(fabsf(ivd(S.now).hi), fabsf(ivd(S.now).lo)) : 0.f;
         float u_t = INFINITY;
         for (int a = 0; a < na; a++) {
             float u = key_f(PS.u_key[a]);
@@ -1179,7 +1179,12 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
                 M.R[a].info[qq] = info;
             }
         }
-        // PCC (PBCandCrossCellTime) and thermostat offers of each atom, by lanes of the last warp
+        // PCC (PBCandCrossCellTime) and thermostat offers of each atom, by lanes of the last
+        // warp: first the face-crossing times (FP64 divisions, three lanes per atom)
+        if (warp == nw - 1) {
+            if (lane < 3 * na) M.face[lane] = pcc_face(S, PS.i[lane / 3], lane % 3);
+            __syncwarp();
+        }
         if (warp == nw - 1 && lane < 2 * na) {
             const int a = lane >> 1;
             if ((lane & 1) == 0) {
