@@ -1011,10 +1011,10 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
             // a denied event still brought p's position to now: its record follows
             // (predict_two refreshes the atoms it predicts)
             if (S.shadow_ok && !sh_exec && p && tid < 4) shadow_word(S, p, tid);
-            predict_two(S, t, sh_exec ? p : 0, MS, PS, B, C);
+            const bool t_tree = predict_two(S, t, sh_exec ? p : 0, MS, PS, B, C);
             if (tid < 32 && B.err == 0) {
-                cbt_update_warp(S, t);
-                if (sh_exec && p) cbt_update_warp(S, p);
+                if (!t_tree) cbt_update_warp(S, t);
+                if (sh_exec && p) cbt_update_warp(S, p, t_tree);
             }
         } else {
             predict_atom(S, t, M, B, C);

@@ -800,7 +800,11 @@ __device__ int gather_warp(const DSys &S, int i, int32_t *nbj, int nbcap, int *o
 // value did not change.  Every recomputed value is the winner of the path value
 // below and the sibling node (ties go to the right child), i.e. a prefix minimum
 // over (key, rightness) of a and the siblings, which the warp scans in parallel.
-__device__ void cbt_update_warp(const DSys &S, int a) {
+// With `full`, every node on a's path is set to its winner (no early stop): the
+// repair that follows one of another leaf made while a's time was changing.  Since
+// each incremental repair leaves every node the winner of its children, both
+// orders give the same tree.
+__device__ void cbt_update_warp(const DSys &S, int a, bool full = false) {
     const int lane = threadIdx.x & 31;
     int32_t *node = S.cbt_node;
     const double *tm = S.ev_time;
@@ -835,7 +839,7 @@ __device__ void cbt_update_warp(const DSys &S, int a) {
     int first = not_a ? __ffs(not_a) - 1 : depth;   // levels below `first` are the phase that follows a
     unsigned stop = __ballot_sync(0xffffffffu, on && lane >= first && id == old);
     int last = stop ? __ffs(stop) - 1 : depth - 1;
-    if (on && lane <= last && id != old) node[f] = id;
+    if (on && (full || lane <= last) && id != old) node[f] = id;
     __syncwarp();
 }
 
@@ -1010,8 +1014,10 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
 }
 
 // Predict for the target t and (when p > 0) the partner p, after ResetTarget of
-// both: the same results as predict_atom(t) followed by predict_atom(p).
-__device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, Blk &B, DScal &C) {
+// both: the same results as predict_atom(t) followed by predict_atom(p).  Returns
+// true when warp 1 already repaired t's tree path, overlapped with the partner's
+// fold; p's path then takes the full repair (cbt_update_warp(full)).
+__device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, Blk &B, DScal &C) {
     const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = T >> 5;
     const int na = p ? 2 : 1;
     // 1. per-atom set-up and the two 27-cell gathers (one warp each)
@@ -1062,7 +1068,7 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
     const size_t words = (screen_ecap(S.nbcap) + 31) / 32;
     for (size_t w = tid; w < 2 * words; w += T) M.mask[w / words][w % words] = 0;
     __syncthreads();
-    if (B.err) return;
+    if (B.err) return false;
     // 2. PCC faces (exact, FP64) and the FP32 screen of every bond / collision / HB candidate
     const int E0 = PS.E[0], E1 = na > 1 ? PS.E[1] : 0;
     const int S0 = PS.nb[0] + PS.nn[0], S1 = na > 1 ? PS.nb[1] + PS.nn[1] : 0;
@@ -1218,13 +1224,17 @@ __device__ void predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         if (tid == 0 && !B.err) fold_atom(S, 0, -1, M, PS, B, C);
         __syncthreads();
     }
+    bool t_tree = false;
     if (na > 1 && !B.err) {
         if (PS.over[1]) predict_atom(S, p, M.F, B, C);
         else {
+            t_tree = nw > 1;
             if (tid == 0) fold_atom(S, 1, t, M, PS, B, C);
+            else if (t_tree && warp == 1) cbt_update_warp(S, t);   // t's event is final
             __syncthreads();
         }
     }
+    return t_tree;
 }
 
 }  // namespace sdmd
