@@ -1072,8 +1072,21 @@ __device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
     // 2. PCC faces (exact, FP64) and the FP32 screen of every bond / collision / HB candidate
     const int E0 = PS.E[0], E1 = na > 1 ? PS.E[1] : 0;
     const int S0 = PS.nb[0] + PS.nn[0], S1 = na > 1 ? PS.nb[1] + PS.nn[1] : 0;
-    for (int g = tid; g < S0 + S1; g += T) {
-        const int a = g < S0 ? 0 : 1, e = a ? g - S0 : g, i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
+    // When every item fits in one pass, cell candidates take threads from the front
+    // and bonds from the back, so that no warp runs the bond screen and the cell
+    // screen one after the other (results go to their entry index either way).
+    const int NB = PS.nb[0] + (na > 1 ? PS.nb[1] : 0), NC = S0 + S1 - NB;
+    const bool split = S0 + S1 <= T;
+    for (int g = tid; g < (split ? T : S0 + S1); g += T) {
+        int a, e;
+        if (split) {
+            if (g < NC) { a = g < PS.nn[0] ? 0 : 1; e = PS.nb[a] + (a ? g - PS.nn[0] : g); }
+            else if (g >= T - NB) { const int b = T - 1 - g; a = b < PS.nb[0] ? 0 : 1; e = a ? b - PS.nb[0] : b; }
+            else continue;
+        } else {
+            a = g < S0 ? 0 : 1; e = a ? g - S0 : g;
+        }
+        const int i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
         Verdict v[2];
         int j, ne = 1;
         if (e < nb) {
