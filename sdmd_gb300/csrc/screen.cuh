@@ -597,8 +597,11 @@ __device__ void eval_bond_r(const DSys &S, const double *xi, int i, int q, Slots
     else {
         double D1 = 0;
         if (kb < 0) D1 = kk.b * kk.b - kk.v2 * (kk.r2 - sht);
-        if (kb < 0 && dbl_gt0(D1)) { sub = SDMD_SUB_CORE; t = root_d(kk, -1, D1); }
-        else { sub = SDMD_SUB_WELL_BOUNCE; t = root_d(kk, 1, kk.b * kk.b - kk.v2 * (kk.r2 - lng)); }
+        int st;
+        double D;
+        if (kb < 0 && dbl_gt0(D1)) { sub = SDMD_SUB_CORE; st = -1; D = D1; }
+        else { sub = SDMD_SUB_WELL_BOUNCE; st = 1; D = kk.b * kk.b - kk.v2 * (kk.r2 - lng); }
+        t = root_d(kk, st, D);   // one call site: lanes in either case share the sqrt and division
         if (dbl_lt0(t)) t = INFINIT;
     }
     put(L, k, j, info | F_FRESH | (sub << 8), t, tdup, 0.0);
@@ -623,18 +626,20 @@ __device__ void eval_collision_r(const DSys &S, const double *xi, int i, int j, 
             if (go) {
                 double D1 = 0;
                 if (neg) D1 = kk.b * kk.b - kk.v2 * (kk.r2 - o.lo);
+                int st = 0;
+                double D = 0;
                 if (neg && dbl_gt0(D1)) {
                     pot = o.lopot;
                     sub = (cs == 0) ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
-                    t = root_d(kk, -1, D1);
-                    info |= F_FRESH;
+                    st = -1; D = D1;
                 } else {
                     pot = o.uppot;
                     if (constrained) sub = (cs == 1) ? SDMD_SUB_WELL_BOUNCE : SDMD_SUB_TBD_ESCAPE;
                     else if (cs == 1) go = false;
                     else sub = SDMD_SUB_TBD_ESCAPE;
-                    if (go) { t = root_d(kk, 1, kk.b * kk.b - kk.v2 * (kk.r2 - o.up)); info |= F_FRESH; }
+                    if (go) { st = 1; D = kk.b * kk.b - kk.v2 * (kk.r2 - o.up); }
                 }
+                if (st) { t = root_d(kk, st, D); info |= F_FRESH; }   // one call site for both roots
             }
         }
     }
