@@ -580,7 +580,8 @@ __device__ __forceinline__ double root_d(const Kin &k, int st, double D) {
     return (-k.b + (st > 0 ? s : -s)) / k.v2;
 }
 
-__device__ void eval_bond_r(const DSys &S, const double *xi, int i, int q, Slots &L, int k) {
+__device__ void eval_bond_r(const DSys &S, const double *xi, int i, int q, Slots &L, int k,
+                            const Kin *pk = nullptr) {
     int j = S.bond_j[q];
     int info = 0;
     double tdup = 0;
@@ -588,7 +589,8 @@ __device__ void eval_bond_r(const DSys &S, const double *xi, int i, int q, Slots
         info |= F_DUP; tdup = S.ev_time[j];
     }
     double lng = S.bond_dmax[q], sht = S.bond_dmin[q];
-    Kin kk; pair_kin_r(S, xi, i, j, kk);
+    Kin kk;
+    if (pk) kk = *pk; else pair_kin_r(S, xi, i, j, kk);
     const long long kb = tkey(kk.b);
     const bool far = tkey(kk.r2 - lng) > KEY_ZERO;
     int sub; double t;
@@ -607,7 +609,8 @@ __device__ void eval_bond_r(const DSys &S, const double *xi, int i, int q, Slots
     put(L, k, j, info | F_FRESH | (sub << 8), t, tdup, 0.0);
 }
 
-__device__ void eval_collision_r(const DSys &S, const double *xi, int i, int j, Slots &L, int k, int *bad) {
+__device__ void eval_collision_r(const DSys &S, const double *xi, int i, int j, Slots &L, int k, int *bad,
+                                 const Kin *pk = nullptr) {
     int info = 0, warn = 0, sub = SDMD_SUB_INVALID;
     double tdup = 0, t = 0, pot = 0;
     if (j == i) { put(L, k, j, -1, 0, 0, 0); return; }
@@ -616,7 +619,8 @@ __device__ void eval_collision_r(const DSys &S, const double *xi, int i, int j, 
     }
     int bits = conn_bits_w(S, i, j);
     if (!((bits & 1) || S.hb_bond[i] == j || nb_has(S, i, j))) {
-        Kin kk; pair_kin_r(S, xi, i, j, kk);
+        Kin kk;
+        if (pk) kk = *pk; else pair_kin_r(S, xi, i, j, kk);
         if (tkey(kk.r2) <= S.cut_key) {
             const bool neg = tkey(kk.b) < 0;
             Lim o; int cs; bool go = true;
@@ -646,7 +650,8 @@ __device__ void eval_collision_r(const DSys &S, const double *xi, int i, int j, 
     put(L, k, j, info | (sub << 8) | (warn << 16), t, tdup, pot);
 }
 
-__device__ void eval_hb_scan_r(const DSys &S, const double *xi, int i, int j, Slots &L, int k, int *bad) {
+__device__ void eval_hb_scan_r(const DSys &S, const double *xi, int i, int j, Slots &L, int k, int *bad,
+                               const Kin *pk = nullptr) {
     if (!(i != j && hb_pair_ok(S, i, j) && S.hb_bond[j] == 0 &&
           ((S.protein[i] == S.protein[j] && abs(S.aanum[i] - S.aanum[j]) >= 4) || S.protein[i] != S.protein[j]))) {
         put(L, k, j, -1, 0, 0, 0);
@@ -657,7 +662,8 @@ __device__ void eval_hb_scan_r(const DSys &S, const double *xi, int i, int j, Sl
     if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i]) {
         info |= F_DUP; tdup = S.ev_time[j];
     }
-    Kin kk; pair_kin_r(S, xi, i, j, kk);
+    Kin kk;
+    if (pk) kk = *pk; else pair_kin_r(S, xi, i, j, kk);
     if (tkey(kk.r2) <= S.cut_key && pair_match(S, i, j, bad) >= 0) {
         Lim o;
         const bool neg = tkey(kk.b) < 0;
@@ -1180,11 +1186,9 @@ __device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         int bad = 0;
         const int R0 = PS.over[0] ? 0 : PS.rn[0];
         const int R1 = (na > 1 && !PS.over[1]) ? PS.rn[1] : 0;
-        for (int q = lane; q < R0 + R1; q += 32) {
-            const int a = q < R0 ? 0 : 1, qq = a ? q - R0 : q;
-            const int e = M.rl[a][qq], i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
-            const int kind = e < nb ? 1 : (e < nb + nn ? 0 : 2);
-            if (kind % nw != warp) continue;
+        // one refined entry, evaluated by this lane (pk: its kinematics, when precomputed)
+        auto refine_one = [&](int a, int qq, int e, int kind, const Kin *pk) {
+            const int i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
             {   // the partner's stored event fields, for the fold (loads overlap the FP64 work)
                 const int jp = kind == 1 ? S.bond_j[S.bond_off[i] + e] : M.nbj[a][kind == 0 ? e - nb : e - nb - nn];
                 const int64_t jc = S.ev_counter[jp];
@@ -1192,15 +1196,71 @@ __device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
                 const int js = S.ev_sub[jp];
                 M.jcnt[a][qq] = jc; M.jpot[a][qq] = jpo; M.jsub[a][qq] = js;
             }
-            if (kind == 1) eval_bond_r(S, PS.xi[a], i, S.bond_off[i] + e, M.R[a], qq);
-            else if (kind == 0) eval_collision_r(S, PS.xi[a], i, M.nbj[a][e - nb], M.R[a], qq, &bad);
-            else eval_hb_scan_r(S, PS.xi[a], i, M.nbj[a][e - nb - nn], M.R[a], qq, &bad);
+            if (kind == 1) eval_bond_r(S, PS.xi[a], i, S.bond_off[i] + e, M.R[a], qq, pk);
+            else if (kind == 0) eval_collision_r(S, PS.xi[a], i, M.nbj[a][e - nb], M.R[a], qq, &bad, pk);
+            else eval_hb_scan_r(S, PS.xi[a], i, M.nbj[a][e - nb - nn], M.R[a], qq, &bad, pk);
             int info = M.R[a].info[qq];
             if (info >= 0 && (info & F_FRESH)) {   // JobAssign's "> 0" test and the stored time
                 double tf = M.R[a].t[qq];
                 if (tkey(tf) > 0) info |= F_POS;
                 if (S.lazy) M.R[a].t[qq] = S.now + tf;
                 M.R[a].info[qq] = info;
+            }
+        };
+        const int Rt = R0 + R1;
+        int la = 0, lqq = 0, le = 0, lkind = -1;
+        if (lane < Rt) {
+            la = lane < R0 ? 0 : 1; lqq = la ? lane - R0 : lane; le = M.rl[la][lqq];
+            lkind = le < PS.nb[la] ? 1 : (le < PS.nb[la] + PS.nn[la] ? 0 : 2);
+        }
+        const unsigned mine = __ballot_sync(0xffffffffu, lkind >= 0 && lkind % nw == warp);
+        const int nm = __popc(mine);
+        if (Rt <= 32 && nm <= 10) {
+            // Three lanes per entry (one per axis) compute pair_kin_r()'s per-axis
+            // terms; lane 3g adds them in the same order and evaluates entry g.  Same
+            // FP64 operations, about a third of the warp-instructions.
+            const int g = lane / 3, d = lane - 3 * g;
+            unsigned m = mine;
+            for (int k = 0; k < g && m; k++) m &= m - 1;
+            const int src = (g < nm && m) ? __ffs(m) - 1 : 0;
+            const int ga = __shfl_sync(0xffffffffu, la, src), gqq = __shfl_sync(0xffffffffu, lqq, src);
+            const int ge = __shfl_sync(0xffffffffu, le, src), gkind = __shfl_sync(0xffffffffu, lkind, src);
+            const bool ok = g < nm;
+            double r = 0, w = 0;
+            if (ok) {
+                const int i = PS.i[ga], nb = PS.nb[ga], nn = PS.nn[ga];
+                const int j = gkind == 1 ? S.bond_j[S.bond_off[i] + ge] : M.nbj[ga][gkind == 0 ? ge - nb : ge - nb - nn];
+                const double *X = d == 0 ? S.x : (d == 1 ? S.y : S.z), *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
+                const int32_t *Cc = d == 0 ? S.cx : (d == 1 ? S.cy : S.cz);
+                double xj = lzx(S, X, V, j);
+                const int ci = Cc[i], cj = Cc[j];
+                if (ci != cj) {
+                    if (ci == 0 && cj == S.cn[d] - 1) xj = xj + -1 * S.box[d];
+                    else if (ci == S.cn[d] - 1 && cj == 0) xj = xj + S.box[d];
+                }
+                r = PS.xi[ga][d] - xj;
+                w = V[i] - V[j];
+            }
+            const double rr = r * r, rw = r * w, ww = w * w;
+            const double r_1 = __shfl_down_sync(0xffffffffu, r, 1), r_2 = __shfl_down_sync(0xffffffffu, r, 2);
+            const double rr1 = __shfl_down_sync(0xffffffffu, rr, 1), rr2 = __shfl_down_sync(0xffffffffu, rr, 2);
+            const double rw1 = __shfl_down_sync(0xffffffffu, rw, 1), rw2 = __shfl_down_sync(0xffffffffu, rw, 2);
+            const double ww1 = __shfl_down_sync(0xffffffffu, ww, 1), ww2 = __shfl_down_sync(0xffffffffu, ww, 2);
+            if (ok && d == 0) {
+                Kin kk;
+                kk.rx = r; kk.ry = r_1; kk.rz = r_2;
+                kk.r2 = rr + rr1 + rr2;
+                kk.b = rw + rw1 + rw2;
+                kk.v2 = ww + ww1 + ww2;
+                refine_one(ga, gqq, ge, gkind, &kk);
+            }
+        } else {
+            for (int q = lane; q < Rt; q += 32) {
+                const int a = q < R0 ? 0 : 1, qq = a ? q - R0 : q;
+                const int e = M.rl[a][qq], nb = PS.nb[a], nn = PS.nn[a];
+                const int kind = e < nb ? 1 : (e < nb + nn ? 0 : 2);
+                if (kind % nw != warp) continue;
+                refine_one(a, qq, e, kind, nullptr);
             }
         }
         // PCC (PBCandCrossCellTime) and thermostat offers of each atom, by lanes of the last
