@@ -862,7 +862,6 @@ struct ShmS {
     int32_t *nbj[2];
     uint8_t *stat[2];             // verdict | warnings << 2, per entry
     float *tlo[2];                // lower time bound of an offer
-    uint32_t *mask[2];            // entries to refine
     int32_t *rl[2];               // refined entries in scan order
     Slots R[2];                   // their exact FP64 results
     // the partner j's stored event fields that the fold's JobAssign and
@@ -889,9 +888,9 @@ struct PairScal {                 // per-atom block scalars of one two-atom pred
 
 __host__ __device__ inline size_t screen_ecap(int nbcap) { return 64 + 2 * (size_t)nbcap; }
 __host__ __device__ inline size_t screen_smem_bytes_dev(int nbcap) {
-    size_t ecap = screen_ecap(nbcap), words = (ecap + 31) / 32;
+    size_t ecap = screen_ecap(nbcap);
     size_t b = fp64_smem_bytes_dev(nbcap);
-    b += al16(2 * (size_t)nbcap * 4) + al16(2 * ecap) + al16(2 * ecap * 4) + al16(2 * words * 4);
+    b += al16(2 * (size_t)nbcap * 4) + al16(2 * ecap) + al16(2 * ecap * 4);
     b += al16(2 * RC * 4) + 2 * (2 * al16(RC * 4) + 3 * al16(RC * 8)) + al16(6 * 8);
     b += 2 * (2 * al16(RC * 8) + al16(RC * 4));
     return al16(b);
@@ -901,15 +900,14 @@ __device__ inline void carve_screen(ShmS &M, int nbcap) {
     carve(M.F, nbcap);
     unsigned char *p = smem + fp64_smem_bytes_dev(nbcap);
     auto take = [&p](size_t bytes) { unsigned char *r = p; p += al16(bytes); return r; };
-    size_t ecap = screen_ecap(nbcap), words = (ecap + 31) / 32;
+    size_t ecap = screen_ecap(nbcap);
     int32_t *nbj = (int32_t *)take(2 * (size_t)nbcap * 4);
     uint8_t *st = (uint8_t *)take(2 * ecap);
     float *tl = (float *)take(2 * ecap * 4);
-    uint32_t *mk = (uint32_t *)take(2 * words * 4);
     int32_t *rl = (int32_t *)take(2 * RC * 4);
     for (int a = 0; a < 2; a++) {
         M.nbj[a] = nbj + a * nbcap; M.stat[a] = st + a * ecap; M.tlo[a] = tl + a * ecap;
-        M.mask[a] = mk + a * words; M.rl[a] = rl + a * RC;
+        M.rl[a] = rl + a * RC;
         M.R[a].j = (int32_t *)take(RC * 4); M.R[a].info = (int32_t *)take(RC * 4);
         M.R[a].t = (double *)take(RC * 8); M.R[a].tdup = (double *)take(RC * 8); M.R[a].pot = (double *)take(RC * 8);
         M.jcnt[a] = (int64_t *)take(RC * 8); M.jpot[a] = (double *)take(RC * 8); M.jsub[a] = (int32_t *)take(RC * 4);
@@ -1076,8 +1074,6 @@ __device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
         const int a = tid;
         PS.E[a] = PS.nb[a] + PS.nn[a] + (PS.mode[a] == 2 ? PS.nn[a] : 0);
     }
-    const size_t words = (screen_ecap(S.nbcap) + 31) / 32;
-    for (size_t w = tid; w < 2 * words; w += T) M.mask[w / words][w % words] = 0;
     __syncthreads();
     if (B.err) return false;
     // 2. PCC faces (exact, FP64) and the FP32 screen of every bond / collision / HB candidate
@@ -1129,56 +1125,41 @@ __device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
     // exact, including JobAssign's partnerCounter, which a partner-less winner
     // (PCC, thermostat, wall) leaves at the value of the last bond/collision record.
     // U' adds every duplicate time (and, for the partner, the target's bound).
-    if (tid == 0) {
-        float u_t = INFINITY;
-        for (int a = 0; a < na; a++) {
-            float u = key_f(PS.u_key[a]);
-            float up = fmaxf(u, key_f(PS.dup_key[a]));
-            if (a == 0) u_t = u;
-            else up = fmaxf(up, u_t);      // the target's new event may become a duplicate for the partner
-            PS.uprime[a] = up;
-        }
-    }
-    __syncthreads();
-    // 4. mark the candidates that need FP64: undecided ones and offers that may reach U'
-    for (int g = tid; g < E0 + E1; g += T) {
-        const int a = g < E0 ? 0 : 1, e = a ? g - E0 : g;
-        const int st = M.stat[a][e] & 3, w = M.stat[a][e] >> 2;
-        bool refine = st == SC_REFINE;
-        if (st == SC_OFFER) {
-            float tl = M.tlo[a][e], up = PS.uprime[a];
-            // lazy mode compares now + t: keep a margin of a few FP64 ulps of that sum
-            float margin = S.lazy ? __fmul_ru(__fadd_ru(PS.nowf, fabsf(tl)), 0x1p-48f) : 0.f;
-            if (__fsub_rd(tl, up) > margin) { if (w) atomicAdd(&PS.warn_excl[a], w); }
-            else refine = true;
-        }
-        if (refine) atomicOr(&M.mask[a][e >> 5], 1u << (e & 31));
-    }
-    __syncthreads();
-    // 5. refined entries of each atom in scan order (one warp per atom)
+    // 4-5. The entries that need FP64 -- undecided ones and offers that may reach
+    // U' -- listed in scan order.  One warp per atom does all of it.
     for (int a = 0; a < na; a++) {
         if (warp != (a % nw)) continue;
-        const int nwords = (PS.E[a] + 31) >> 5;
-        int base = 0;
-        for (int w0 = 0; w0 < nwords; w0 += 32) {
-            const int w = w0 + lane;
-            uint32_t bits = w < nwords ? M.mask[a][w] : 0u;
-            int cnt = __popc(bits), incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
+        float up = fmaxf(key_f(PS.u_key[a]), key_f(PS.dup_key[a]));
+        if (a == 1) up = fmaxf(up, key_f(PS.u_key[0]));   // the target's new event may become a duplicate
+        const int Ea = PS.E[a];
+        int base = 0, wsum = 0;
+        for (int e0 = 0; e0 < Ea; e0 += 32) {
+            const int e = e0 + lane;
+            bool refine = false;
+            if (e < Ea) {
+                const int st = M.stat[a][e] & 3, w = M.stat[a][e] >> 2;
+                refine = st == SC_REFINE;
+                if (st == SC_OFFER) {
+                    const float tl = M.tlo[a][e];
+                    // lazy mode compares now + t: keep a margin of a few FP64 ulps of that sum
+                    const float margin = S.lazy ? __fmul_ru(__fadd_ru(PS.nowf, fabsf(tl)), 0x1p-48f) : 0.f;
+                    if (__fsub_rd(tl, up) > margin) wsum += w;   // dropped: its warnings still count
+                    else refine = true;
+                }
             }
-            int pos = base + incl - cnt;
-            while (bits) {
-                int b = __ffs(bits) - 1;
-                bits &= bits - 1;
-                if (pos < RC) M.rl[a][pos] = (w << 5) + b;
-                pos++;
-            }
-            base += __shfl_sync(0xffffffffu, incl, 31);
+            const unsigned m = __ballot_sync(0xffffffffu, refine);
+            const int pos = base + __popc(m & ((1u << lane) - 1u));
+            if (refine && pos < RC) M.rl[a][pos] = e;
+            base += __popc(m);
         }
-        if (lane == 0) { PS.rn[a] = base < RC ? base : RC; PS.over[a] = base > RC; }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wsum += __shfl_down_sync(0xffffffffu, wsum, o);
+        if (lane == 0) {
+            PS.uprime[a] = up;
+            PS.warn_excl[a] += wsum;
+            PS.rn[a] = base < RC ? base : RC;
+            PS.over[a] = base > RC;
+        }
     }
     __syncthreads();
     // 6. exact FP64 for the refined entries, packed into lanes; one warp per kind
