@@ -315,6 +315,9 @@ def run_ours(args, D):
     cpu = None
     if D.rank == 0 and D.world >= 1 and not args.no_cpu:
         cpu = cpu_baseline(after_sweep[0], args.cpu_seconds)
+    drift = None
+    if D.rank == 0 and len(systems) == 1 and not args.no_drift:   # outside every timed region
+        drift = measure_nve_drift(after_sweep[0], threads, D.local, adv, scr)
 
     if D.rank == 0:
         if tuned is not None:
@@ -333,9 +336,39 @@ def run_ours(args, D):
                 "config": cfg,
                 "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "h2d_bytes_per_step": st_b + dy_b,
                         "d2h_bytes_per_step": dy_b},
-                "roofline": roof, "sweep": sweep, "cpu_baseline": cpu, "clocks": clk,
+                "roofline": roof, "sweep": sweep, "cpu_baseline": cpu, "nve_drift": drift, "clocks": clk,
                 "gpu_launches": launches, "wall_s_timed": round(wall, 3)}
         print(json.dumps(line))
+
+
+def measure_nve_drift(s0, threads, device, adv, scr, events=200000, events_ref=20000):
+    """The metric's "matched NVE drift": from the same post-sweep state with the
+    thermostat off, the energy change of the measured path (FP32 screen, lazy
+    advance) and of the reference's algorithm (plain FP64, eager advance, fewer
+    events: it is slower), as |dE| / (N kT) per 10^6 executed events.  E is
+    CalKinetE + CalPotenE on the device plus the constraint-step energy the
+    reference's CalPotenE leaves out; HB events change that bookkeeping, so their
+    count is reported with each run."""
+    from sdmd_gb300.energy import constraint_energy, nve_drift
+    from sdmd_gb300.engine import ADVANCE_EAGER, SCREEN_FP64, Engine
+    out = {"unit": "|dE|/(N kT) per 1e6 executed events", "limit": 1e-4, "thermostat": "off"}
+    kT = float(s0.scal["temperature"])
+    for name, a, sc, n in (("measured_path", adv, scr, events), ("fp64_eager", ADVANCE_EAGER, SCREEN_FP64, events_ref)):
+        s = s0.copy()
+        s.scal["thermostat"] = 0
+        with Engine([s], threads=threads, device=device, advance=a, screen=sc) as e:
+            e.prepare(full=True)
+            pot, kin = e.energies()
+            e.download()
+            e0, f0 = pot[0] + kin[0] + constraint_energy(s), s.counters["frame"]
+            e.run(n)
+            pot, kin = e.energies()
+            e.download()
+            e1 = pot[0] + kin[0] + constraint_energy(s)
+        ev = s.counters["frame"] - f0
+        out[name] = {"events": int(ev), "drift": nve_drift(e0, e1, s.n, kT, ev),
+                     "hb_events": int(s.counters["hb"] + s.counters["hbneighbor"])}
+    return out
 
 
 def cpu_baseline(system, seconds):
@@ -455,6 +488,7 @@ def main():
     ap.add_argument("--screen", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-drift", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.events_per_step is None:
