@@ -280,14 +280,14 @@ __device__ inline double take_sample(const DSys &S, DScal &C, Blk &B) {
 }
 
 // ThermostatTime (src/TimePrediction.c:582-595): MB(0, 1) = the sample * sqrt(1) + 0
-__device__ void thermostat_time(const DSys &S, Cur &c, DScal &C, Blk &B) {
+__device__ __noinline__ void thermostat_time(const DSys &S, Cur &c, DScal &C, Blk &B) {
     if (!S.thermostat) return;
     double t = take_sample(S, C, B) * sqrt(1.0) + 0;
     job_assign(S, c, 0, S.thermo_freq * (t < 0 ? -t : t), 0, SDMD_SUB_INVALID, SDMD_EV_THERMOSTAT);
 }
 
 // HBTime for an HB-bonded atom (src/TimePrediction.c:329-387)
-__device__ void hb_bonded(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
+__device__ __noinline__ void hb_bonded(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     int j = S.hb_bond[i];
     if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_HB && S.ev_pcounter[j] == S.ev_counter[i] &&
         dup_assign(S, c, j, S.ev_time[j], SDMD_EV_HB))
@@ -308,7 +308,7 @@ __device__ void hb_bonded(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
 }
 
 // HBNeighborTime (src/TimePrediction.c:486-579)
-__device__ void hbnb_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
+__device__ __noinline__ void hbnb_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     int flag = 0;
     for (int n = 1; n <= S.nb_status[i]; n++) {
         int j = S.nb_partner[4 * i + n - 1];
@@ -340,7 +340,7 @@ __device__ void hbnb_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
 }
 
 // WallTime, smooth walls (src/TimePrediction.c:635-737)
-__device__ void wall_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
+__device__ __noinline__ void wall_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
     double p[3] = {S.x[i], S.y[i], S.z[i]}, v[3] = {S.vx[i], S.vy[i], S.vz[i]};
     if (S.wall == SDMD_WALL_PARALLEL) { p[0] = p[2] = 0; v[0] = v[2] = 0; }
     else if (S.wall == SDMD_WALL_CYLINDER) { p[0] = 0; v[0] = 0; }
@@ -377,7 +377,7 @@ struct Shm {
     double *face;    // 3 PCC face times
 };
 
-__device__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, DScal &C) {
+__device__ __noinline__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, DScal &C) {
     const int tid = threadIdx.x, T = blockDim.x;
     int bad = 0;
     Cur c;
@@ -772,7 +772,7 @@ size_t staged_state_bytes(int n, int ncell, int nb, int nc, int ncs, int nconn) 
 }
 
 // stage (copy == true) or locate (copy == false) the state after the slot buffers
-__device__ void stage_state(DSys &S, const DSys &G, unsigned char *base, bool copy) {
+__device__ __noinline__ void stage_state(DSys &S, const DSys &G, unsigned char *base, bool copy) {
     Stager st{base, copy};
     size_t N1 = (size_t)G.n + 1;
     DSys L = G;
@@ -809,7 +809,7 @@ __device__ void stage_state(DSys &S, const DSys &G, unsigned char *base, bool co
 }
 
 // write the mutable staged arrays back to global memory
-__device__ void unstage_state(const DSys &S, const DSys &G) {
+__device__ __noinline__ void unstage_state(const DSys &S, const DSys &G) {
     size_t N1 = (size_t)G.n + 1;
     for (size_t k = threadIdx.x; k < N1; k += blockDim.x) {
         G.x[k] = S.x[k]; G.y[k] = S.y[k]; G.z[k] = S.z[k];

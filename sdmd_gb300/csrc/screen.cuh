@@ -683,7 +683,7 @@ __device__ void eval_hb_scan_r(const DSys &S, const double *xi, int i, int j, Sl
 
 // ---- HB-bonded partner: the fresh part of hb_bonded(), evaluated by a lane ------
 struct HbbOut { double t, pot; int sub, warn, bad, pos; };
-__device__ void hbb_fresh(const DSys &S, const double *xi, int i, HbbOut &r) {
+__device__ __noinline__ void hbb_fresh(const DSys &S, const double *xi, int i, HbbOut &r) {
     int j = S.hb_bond[i];
     Kin kk; pair_kin_r(S, xi, i, j, kk);
     Lim o; int warn = 0, bad = 0;
@@ -720,7 +720,7 @@ __device__ __forceinline__ void stage_rp(DSys &S) {
 // Cell c holds cell_cnt[c] atoms in cell_arr[c*maxc ...] in insertion order, so the
 // reference's list (head = most recently inserted, src/Events.c:158-200) reads
 // from the end.  Built from cell_list at kernel start, written back at the end.
-__device__ void cells_from_list(const DSys &S, Blk &B) {
+__device__ __noinline__ void cells_from_list(const DSys &S, Blk &B) {
     const int N = S.n, M = S.maxc;
     for (int c = 1 + threadIdx.x; c <= S.ncell; c += blockDim.x) {
         int32_t *arr = S.cell_arr + (size_t)c * M;
@@ -733,7 +733,7 @@ __device__ void cells_from_list(const DSys &S, Blk &B) {
         S.cell_cnt[c] = cnt;
     }
 }
-__device__ void cells_to_list(const DSys &S) {
+__device__ __noinline__ void cells_to_list(const DSys &S) {
     const int N = S.n, M = S.maxc;
     for (int c = 1 + threadIdx.x; c <= S.ncell; c += blockDim.x) {
         const int32_t *arr = S.cell_arr + (size_t)c * M;
@@ -743,7 +743,7 @@ __device__ void cells_to_list(const DSys &S) {
     }
 }
 // LinkList("part") for one atom (remove from oldc, insert as newest of newc), one warp
-__device__ void cell_move_warp(const DSys &S, int t, int oldc, int newc, Blk &B) {
+__device__ __noinline__ void cell_move_warp(const DSys &S, int t, int oldc, int newc, Blk &B) {
     const int lane = threadIdx.x & 31, M = S.maxc;
     int32_t *ao = S.cell_arr + (size_t)oldc * M;
     const int cnt = S.cell_cnt[oldc];
