@@ -686,6 +686,21 @@ __device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, int32_t 
     if (bad) set_err(B, SDMD_EHBMAP, t);
 }
 
+// one pop's trace record (a real call: tracing is off in timed runs)
+__device__ __noinline__ void record_trace(const DSys &S, const DScal &C, int t, int p, int partner, int type, int sub,
+                                          int executed, double dt) {
+    sdmd_trace_rec &r = S.trace[C.pops % S.trace_cap];
+    r.target = t; r.partner = partner; r.type = type; r.sub = sub;
+    r.executed = executed; r.hb_itype_after = S.hb_itype[t];
+    r.t_new_partner = S.ev_partner[t]; r.t_new_type = S.ev_type[t];
+    r.p_new_partner = p ? S.ev_partner[p] : 0; r.p_new_type = p ? S.ev_type[p] : 0;
+    r.system = blockIdx.x; r.pad = 0;
+    r.dt = dt; r.time_now = C.time;
+    r.vt[0] = S.vx[t]; r.vt[1] = S.vy[t]; r.vt[2] = S.vz[t];
+    r.vp[0] = p ? S.vx[p] : 0; r.vp[1] = p ? S.vy[p] : 0; r.vp[2] = p ? S.vz[p] : 0;
+    r.t_new_time = S.ev_time[t]; r.p_new_time = p ? S.ev_time[p] : 0;
+}
+
 // ---- CBT (src/CBT.c) -----------------------------------------------------------
 __device__ void cbt_update(const DSys &S, int a) {   // UpdateCBTRun, src/CBT.c:56-83
     int32_t *node = S.cbt_node;
@@ -1025,18 +1040,7 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
             }
         }
         if (tid == 0) {
-            if (S.trace_cap > 0) {
-                sdmd_trace_rec &r = S.trace[C.pops % S.trace_cap];
-                r.target = t; r.partner = rec_partner; r.type = rec_type; r.sub = rec_sub;
-                r.executed = sh_exec; r.hb_itype_after = S.hb_itype[t];
-                r.t_new_partner = S.ev_partner[t]; r.t_new_type = S.ev_type[t];
-                r.p_new_partner = p ? S.ev_partner[p] : 0; r.p_new_type = p ? S.ev_type[p] : 0;
-                r.system = blockIdx.x; r.pad = 0;
-                r.dt = dt; r.time_now = C.time;
-                r.vt[0] = S.vx[t]; r.vt[1] = S.vy[t]; r.vt[2] = S.vz[t];
-                r.vp[0] = p ? S.vx[p] : 0; r.vp[1] = p ? S.vy[p] : 0; r.vp[2] = p ? S.vz[p] : 0;
-                r.t_new_time = S.ev_time[t]; r.p_new_time = p ? S.ev_time[p] : 0;
-            }
+            if (S.trace_cap > 0) record_trace(S, C, t, p, rec_partner, rec_type, rec_sub, sh_exec, dt);
             C.pops++;
         }
         __syncthreads();
