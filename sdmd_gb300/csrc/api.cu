@@ -593,6 +593,23 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         sdmd_gpu_destroy(h);
         return r;
     }
+    // A batch with more systems than the full build keeps resident at once runs in
+    // waves; the 128-register build fits more CTAs per SM when registers are the
+    // limit (the occupancy calculator decides, for this launch shape).
+    if (scr && n_systems > 1 && h->threads <= 256) {
+        int sms = 0, full = 0, capped = 0;
+        if ((r = cuda_fail(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->opts.device))) ||
+            (r = cuda_fail(cudaFuncSetAttribute(loop_kernel_screen_r128, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)h->smem_loop))) ||
+            (r = cuda_fail(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&full, loop_kernel_screen, h->threads,
+                                                                         h->smem_loop))) ||
+            (r = cuda_fail(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&capped, loop_kernel_screen_r128, h->threads,
+                                                                         h->smem_loop)))) {
+            sdmd_gpu_destroy(h);
+            return r;
+        }
+        if ((long)full * sms < n_systems && capped > full) h->loop_k = loop_kernel_screen_r128;
+    }
     if (h->opts.advance == SDMD_ADVANCE_LAZY) lazy_enter_kernel<<<n_systems, 128, 0, h->stream>>>(h->ds);
     if ((r = cuda_fail(cudaStreamSynchronize(h->stream)))) { sdmd_gpu_destroy(h); return r; }
     *out = h;

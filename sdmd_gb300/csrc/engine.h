@@ -19,6 +19,7 @@ __global__ void lazy_enter_kernel(const DSys *systems);
 size_t screen_smem_bytes(int nbcap);
 __global__ void sweep_kernel_screen(const DSys *systems, int full);
 __global__ void loop_kernel_screen(const DSys *systems, double t_end_override, int staged);
+__global__ void loop_kernel_screen_r128(const DSys *systems, double t_end_override, int staged);
 
 // parallel full-rebuild sweep of the screened path (sweep_par.cuh)
 size_t verify_smem_bytes(int nbcap, int warps);

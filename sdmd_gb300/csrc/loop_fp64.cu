@@ -1075,6 +1075,18 @@ __global__ void loop_kernel_screen(const DSys *systems, double t_end_override, i
     loop_body<true>(systems, t_end_override, staged, S, G, B, C, PS);
 }
 
+// The same loop built for at most 128 registers a thread (up to 256 threads, two
+// CTAs per SM): for batches with more systems than the full build keeps resident,
+// where registers, not shared memory, bound the CTAs per SM.
+__global__ void __launch_bounds__(256, 2) loop_kernel_screen_r128(const DSys *systems, double t_end_override,
+                                                                   int staged) {
+    __shared__ DSys S, G;
+    __shared__ Blk B;
+    __shared__ DScal C;
+    __shared__ PairScal PS;
+    loop_body<true>(systems, t_end_override, staged, S, G, B, C, PS);
+}
+
 size_t screen_smem_bytes(int nbcap) { return screen_smem_bytes_dev(nbcap); }
 size_t verify_smem_bytes(int nbcap, int warps) { return verify_warp_bytes(nbcap) * (size_t)warps; }
 

@@ -153,6 +153,34 @@ def test_batch_of_wall_replicas_matches_oracle(golden, engine_mod, screen):
     assert walls > 0
 
 
+def test_batch_beyond_one_wave_matches_oracle(golden, engine_mod):
+    """160 systems at 256 threads: the full build of the screened loop keeps one
+    CTA per SM (152 on this part), so the engine runs the 128-register build with
+    two.  A system of mixed chains too large to stage in shared memory keeps the
+    batch unstaged, so registers are what limits residency.  Every system must equal
+    its own oracle run."""
+    from oracle import oracle as O
+    from sdmd_gb300 import workloads as W
+    from tests.golden.make_golden import rng_state_after
+    d = golden("ala10_nvt")
+    systems = [W.c2(n_chains=6, length=12, seed=5, conc_mM=20.0)]
+    for k in range(159):
+        s = from_fixture(d, "pre")
+        s.rng = rng_state_after(300 + k, 0)
+        systems.append(s)
+    refs = [s.copy() for s in systems]
+    with engine_mod.Engine(systems, threads=256, screen=1) as eng:
+        eng.prepare(full=True)
+        eng.run(400)
+        eng.download()
+    for s, r in zip(systems, refs):
+        O.predict_all(r)
+        rc, _, _ = O.Loop(r).run(400)
+        assert rc == 0
+        assert_state_equal(s.a, r.a)
+        assert s.counters == r.counters and s.time == r.time
+
+
 @SCREENS
 @pytest.mark.parametrize("threads", [32, 96, 256])
 def test_block_size_does_not_change_results(golden, engine_mod, threads, screen):
