@@ -37,6 +37,39 @@ __device__ inline bool polar_accept(int32_t r1, int32_t r2) {
     return s < 1;
 }
 
+// glibc's TYPE_3 state keeps front == rear + 3 (mod 31).  With the table rotated
+// so that rear is at index 0 (R[k] = tab[(rear + k) % 31]), draw s of a block
+// writes R[(3 + s) % 31] += R[s % 31]; after 31 draws the pattern repeats.  A
+// fully unrolled block therefore indexes the table statically and keeps it in
+// registers.
+__device__ inline bool ring_ok(const sdmd_rng &r) {
+    return r.rear >= 0 && r.rear < 31 && r.front == (r.rear + 3) % 31;
+}
+__device__ inline void ring_load(const sdmd_rng &r, int32_t (&R)[31]) {
+#pragma unroll
+    for (int k = 0; k < 31; k++) {
+        int q = r.rear + k;
+        R[k] = r.tab[q >= 31 ? q - 31 : q];
+    }
+}
+// the state after `m` draws from the one ring_load() read (rear advanced by m)
+__device__ inline void ring_store(sdmd_rng &r, const int32_t (&R)[31], int64_t m) {
+    const int rear0 = r.rear;
+#pragma unroll
+    for (int k = 0; k < 31; k++) {
+        int q = rear0 + k;
+        r.tab[q >= 31 ? q - 31 : q] = R[k];
+    }
+    r.rear = (int)((rear0 + m) % 31);
+    r.front = (r.rear + 3) % 31;
+}
+#define RING_DRAW(R, k, out)                                                        \
+    do {                                                                            \
+        const uint32_t v_ = (uint32_t)R[(3 + (k)) % 31] + (uint32_t)R[(k)];         \
+        R[(3 + (k)) % 31] = (int32_t)v_;                                            \
+        (out) = (int32_t)((v_ >> 1) & 0x7fffffffu);                                 \
+    } while (0)
+
 __global__ void samples_walk_kernel(const DSys *systems, int n_systems, int64_t want) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n_systems) return;
@@ -48,24 +81,45 @@ __global__ void samples_walk_kernel(const DSys *systems, int n_systems, int64_t 
     C->paused = 0;
     if (!S.thermostat || C->err) return;
     sdmd_rng r = C->rng;
-    int64_t n = want < S.smp_cap ? want : S.smp_cap, cum = 0;
-    for (int64_t q = 0; q < n; q++) {
-        int32_t r1, r2;
-        int tries = 0;
-        for (;;) {
-            r1 = rng_next(r);
-            r2 = rng_next(r);
-            cum += 2;
-            if (polar_accept(r1, r2)) break;
+    int64_t n = want < S.smp_cap ? want : S.smp_cap, cum = 0, q = 0;
+    int32_t r1 = 0, r2 = 0;
+    int phase = 0, tries = 0;   // phase 0: next draw is a, 1: b, 2: the coin
+    // one draw consumed by the polar Box-Muller walk (src/ToolFunctions.c:544-569)
+    auto take = [&](int32_t out) -> bool {
+        cum++;
+        if (phase == 0) { r1 = out; phase = 1; return true; }
+        if (phase == 1) {
+            r2 = out;
+            if (polar_accept(r1, r2)) { phase = 2; tries = 0; return true; }
+            phase = 0;
             if (++tries >= 4096) {   // only a degenerate state rejects this often
                 C->err = SDMD_ETIMEOUT; C->err_atom = 0; C->err_event = C->c.frame;
-                return;
+                return false;
+            }
+            return true;
+        }
+        S.smp_raw[3 * q] = r1; S.smp_raw[3 * q + 1] = r2; S.smp_raw[3 * q + 2] = out;
+        S.smp_cum[q] = cum;
+        q++;
+        phase = 0;
+        return true;
+    };
+    if (ring_ok(r)) {
+        int32_t R[31];
+        ring_load(r, R);
+        bool go = true;
+        while (go && q < n) {
+#pragma unroll
+            for (int s = 0; s < 31; s++) {
+                int32_t out;
+                RING_DRAW(R, s, out);
+                if (go && q < n) go = take(out);
             }
         }
-        int32_t r3 = rng_next(r);
-        cum += 1;
-        S.smp_raw[3 * q] = r1; S.smp_raw[3 * q + 1] = r2; S.smp_raw[3 * q + 2] = r3;
-        S.smp_cum[q] = cum;
+        if (!go) return;
+    } else {
+        while (q < n)
+            if (!take(rng_next(r))) return;
     }
     C->smp_avail = n;
 }
@@ -91,8 +145,31 @@ __global__ void samples_commit_kernel(const DSys *systems, int n_systems) {
     DScal *C = S.sc;
     if (C->smp_used <= 0) { C->rng = C->rng0; return; }
     sdmd_rng r = C->rng0;
-    int64_t n = S.smp_cum[C->smp_used - 1];
-    for (int64_t q = 0; q < n; q++) rng_next(r);
+    const int64_t n = S.smp_cum[C->smp_used - 1];
+    if (ring_ok(r)) {   // whole blocks of 31 draws with the table in registers, then the rest
+        int32_t R[31];
+        ring_load(r, R);
+        for (int64_t b = 0; b < n / 31; b++) {
+#pragma unroll
+            for (int s = 0; s < 31; s++) {
+                int32_t out;
+                RING_DRAW(R, s, out);
+                (void)out;
+            }
+        }
+        const int rem = (int)(n % 31);
+#pragma unroll
+        for (int s = 0; s < 31; s++) {
+            if (s < rem) {
+                int32_t out;
+                RING_DRAW(R, s, out);
+                (void)out;
+            }
+        }
+        ring_store(r, R, n);
+    } else {
+        for (int64_t q = 0; q < n; q++) rng_next(r);
+    }
     C->rng = r;
     C->smp_avail = 0;
     C->smp_used = 0;
