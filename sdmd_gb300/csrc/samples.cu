@@ -41,7 +41,8 @@ __device__ inline bool polar_accept(int32_t r1, int32_t r2) {
 // so that rear is at index 0 (R[k] = tab[(rear + k) % 31]), draw s of a block
 // writes R[(3 + s) % 31] += R[s % 31]; after 31 draws the pattern repeats.  A
 // fully unrolled block therefore indexes the table statically and keeps it in
-// registers.
+// registers.  The commit uses it to skip the consumed draws; the walk keeps the
+// plain generator (its sample logic would be unrolled 31 times).
 __device__ inline bool ring_ok(const sdmd_rng &r) {
     return r.rear >= 0 && r.rear < 31 && r.front == (r.rear + 3) % 31;
 }
@@ -81,45 +82,24 @@ __global__ void samples_walk_kernel(const DSys *systems, int n_systems, int64_t 
     C->paused = 0;
     if (!S.thermostat || C->err) return;
     sdmd_rng r = C->rng;
-    int64_t n = want < S.smp_cap ? want : S.smp_cap, cum = 0, q = 0;
-    int32_t r1 = 0, r2 = 0;
-    int phase = 0, tries = 0;   // phase 0: next draw is a, 1: b, 2: the coin
-    // one draw consumed by the polar Box-Muller walk (src/ToolFunctions.c:544-569)
-    auto take = [&](int32_t out) -> bool {
-        cum++;
-        if (phase == 0) { r1 = out; phase = 1; return true; }
-        if (phase == 1) {
-            r2 = out;
-            if (polar_accept(r1, r2)) { phase = 2; tries = 0; return true; }
-            phase = 0;
+    int64_t n = want < S.smp_cap ? want : S.smp_cap, cum = 0;
+    for (int64_t q = 0; q < n; q++) {
+        int32_t r1, r2;
+        int tries = 0;
+        for (;;) {
+            r1 = rng_next(r);
+            r2 = rng_next(r);
+            cum += 2;
+            if (polar_accept(r1, r2)) break;
             if (++tries >= 4096) {   // only a degenerate state rejects this often
                 C->err = SDMD_ETIMEOUT; C->err_atom = 0; C->err_event = C->c.frame;
-                return false;
+                return;
             }
-            return true;
         }
-        S.smp_raw[3 * q] = r1; S.smp_raw[3 * q + 1] = r2; S.smp_raw[3 * q + 2] = out;
+        int32_t r3 = rng_next(r);
+        cum += 1;
+        S.smp_raw[3 * q] = r1; S.smp_raw[3 * q + 1] = r2; S.smp_raw[3 * q + 2] = r3;
         S.smp_cum[q] = cum;
-        q++;
-        phase = 0;
-        return true;
-    };
-    if (ring_ok(r)) {
-        int32_t R[31];
-        ring_load(r, R);
-        bool go = true;
-        while (go && q < n) {
-#pragma unroll
-            for (int s = 0; s < 31; s++) {
-                int32_t out;
-                RING_DRAW(R, s, out);
-                if (go && q < n) go = take(out);
-            }
-        }
-        if (!go) return;
-    } else {
-        while (q < n)
-            if (!take(rng_next(r))) return;
     }
     C->smp_avail = n;
 }
