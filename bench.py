@@ -1,5 +1,5 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 event-loop engine on BASELINE's headline workload.
+"""Benchmark of the GB300 event-loop engine: executed events/s on sDMD's event loop.
 
 Workload (default, --workload c2): the full-rebuild-sweep configuration -- 256
 random-sequence 16-residue peptides at 5 mM in a periodic 440 A cube
@@ -13,6 +13,10 @@ upload, tree build, run, download inside the timed region).
 --impl reference times the reference's CPU algorithm (the oracle's C
 restatement, compiled on this host) on the same workload and prints the same
 line with "impl": "reference".
+
+Besides the timed value, the line reports the loop kernel's roofline figures, the
+oracle on one host core (`cpu_baseline`) and, for single systems, the NVE energy
+drift of the measured path and of plain FP64 from the same state (`nve_drift`).
 
 Multi-GPU (torchrun): the event loop of one system is sequential, so ranks run
 independent replicas (different seeds): "replicas only", weak scaling.
@@ -305,7 +309,8 @@ def run_ours(args, D):
             "traffic": None if traffic is None else round(traffic * events / n_launch, 1),
             "kernel": kname, "launches": loop_launches, "bytes_per_event": round(per_event, 1),
             "P_candidates": round(P, 2)}
-    # the full-rebuild sweep (SURVEY 8d bytes) for reference
+    # the full-rebuild sweep: its algorithmic bytes (every atom's state read once,
+    # its new event written, the cell list and bond lists read) over its device time
     s0 = after_sweep[0]
     ncell = int(np.prod(s0.scal["cellnum"]))
     b_sweep = 104 * s0.n + 4 * (ncell + s0.n) + 4 * int(s0.a["bond_j"].size)

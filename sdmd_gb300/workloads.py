@@ -12,8 +12,12 @@ and the force-field tables of Library_Ding.  No public dataset is involved.
   C3  64 replicas of C1, temperatures geometric 270-500 K
   C4  512 single chains of 5-60 residues, box edge scaled to C1's density,
       temperatures 280-400 K
-  C5  replicas of 400 ten-residue chains in a cylinder (radius 60 A, axis x,
-      120 A periodic), NVT 310 K
+
+Not generated here: 8 replicas of 400 ten-residue chains in a cylinder of radius
+60 A (axis x, 120 A periodic), NVT 310 K.  Their 0.031 atoms per A^3 is beyond
+what overlap-free random insertion of extended chains reaches; building it would
+need a compressive equilibration.  The wall code such a system runs is covered by
+the cylinder-wall golden case instead.
 """
 import json
 import os
