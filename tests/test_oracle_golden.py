@@ -28,7 +28,7 @@ def assert_state_equal(sys_, ref, keys=DYN):
             raise AssertionError(f"{k} differs at {idx}: {a[idx]} vs {b[idx]}")
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "mixed6"])
 def test_sweep_and_tree(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -39,7 +39,7 @@ def test_sweep_and_tree(golden, case):
     assert np.array_equal(node, d["cbt/cbt_node"]) and np.array_equal(leaf, d["cbt/cbt_leaf"])
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "mixed6"])
 def test_trace_event_for_event(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
