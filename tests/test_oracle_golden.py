@@ -28,7 +28,7 @@ def assert_state_equal(sys_, ref, keys=DYN):
             raise AssertionError(f"{k} differs at {idx}: {a[idx]} vs {b[idx]}")
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "mixed6"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "mixed6", "sheet2"])
 def test_sweep_and_tree(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -63,8 +63,11 @@ def test_trace_event_for_event(golden, case):
         assert s.counters["wall"] > 0
 
 
-def test_long_run_checkpoints(golden):
-    d = golden("ala10_nvt_long")
+@pytest.mark.parametrize("case", ["ala10_nvt_long", "sheet2"])
+def test_long_run_checkpoints(golden, case):
+    """Long runs with HB formation and breaking; sheet2's bonds form between its two
+    chains (a two-strand sheet), so the inter-protein branches are exercised."""
+    d = golden(case)
     s = from_fixture(d, "pre")
     O.predict_all(s)
     loop = O.Loop(s)
@@ -77,6 +80,9 @@ def test_long_run_checkpoints(golden):
         assert_state_equal(s, ref)
         assert s.counters == ref["_counters"]
     assert s.counters["hb"] > 0 and s.counters["hbneighbor"] > 0
+    if case == "sheet2":   # some of its HB events pair atoms of different chains
+        half = s.n // 2
+        assert any(r[2] == 2 and (r[0] <= half) != (r[1] <= half) for r in d["trace/sparse_i"])
 
 
 def test_rng_matches_glibc_rand():
