@@ -17,7 +17,10 @@ packs the dumps into compressed .npz fixtures that travel with the repository:
   meta/*       event count, checkpoints, the harness summary, and the run's inputs
                (.gro text, parameter.txt, the test-local Wall.txt when there is one)
 
-Usage: python tests/golden/make_golden.py [case ...]
+Usage: python tests/golden/make_golden.py [case ... | remd]
+
+remd_rearrange.npz holds the exchange server's rearrange() on seeded replica
+ladders, run by the reference's own Server.c.
 """
 import os
 import shutil
@@ -214,6 +217,41 @@ def bundle_force_field():
                 "Copyright (c) 2018 Size Zheng.  Copied unchanged by tests/golden/make_golden.py as input data.\n")
 
 
+SERVER = os.path.join(REPO, "oracle", "_ref", "sdmd_ref_server_rearrange")
+
+
+def remd_golden():
+    """The exchange server's rearrange() (src/Server.c:145-192) run by the reference
+    itself (oracle/ref/server_driver.c) on seeded replica ladders: per case, the
+    srand seed, the starting (num, T) records, every round's energies, and every
+    round's resulting (num, T).  Energies are drawn around a common mean with a
+    spread comparable to the temperature gaps, so swaps are both accepted and
+    rejected."""
+    rng = np.random.default_rng(20201)
+    arrays = {}
+    for case, (n, rounds, seed) in enumerate([(8, 60, 1), (16, 60, 7), (64, 40, 20201), (3, 80, 99)]):
+        T0 = 270.0 * (500.0 / 270.0) ** (np.arange(n) / max(n - 1, 1)) * 0.0019872041
+        num0 = np.arange(1, n + 1, dtype=np.int32)
+        E = -150.0 + rng.normal(0.0, 2.0, (rounds, n))
+        lines = [f"{seed} {n} {rounds}"]
+        for r in range(rounds):
+            for i in range(n):
+                lines.append(f"{num0[i]} {float(T0[i])!r} {float(E[r, i])!r}")
+        res = subprocess.run([SERVER], input="\n".join(lines) + "\n", capture_output=True, text=True, check=True)
+        out = [l.split() for l in res.stdout.splitlines()]
+        assert len(out) == rounds * n
+        arrays[f"c{case}/seed"] = np.array([seed], np.int64)
+        arrays[f"c{case}/T0"] = T0
+        arrays[f"c{case}/num0"] = num0
+        arrays[f"c{case}/E"] = E
+        arrays[f"c{case}/num"] = np.array([int(o[0]) for o in out], np.int32).reshape(rounds, n)
+        arrays[f"c{case}/T"] = np.array([float.fromhex(o[1]) for o in out]).reshape(rounds, n)
+    arrays["meta/cases"] = np.array([4], np.int64)
+    out = os.path.join(HERE, "remd_rearrange.npz")
+    np.savez_compressed(out, **arrays)
+    print(f"remd_rearrange: 4 cases -> {os.path.getsize(out) / 1024:.0f} KiB")
+
+
 def main(argv):
     if not os.path.isdir(REF):
         sys.exit("the reference sources are not present; golden fixtures can only be regenerated where they are")
@@ -221,10 +259,15 @@ def main(argv):
     if argv == ["--force-field-only"]:
         return
     build_harness()
+    if argv == ["remd"]:
+        remd_golden()
+        return
     all_cases = cases()
     names = argv or list(all_cases)
     for n in names:
         run_case(n, **all_cases[n])
+    if not argv:
+        remd_golden()
 
 
 if __name__ == "__main__":
