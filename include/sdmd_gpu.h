@@ -260,14 +260,20 @@ int  sdmd_gpu_last_run_stats(sdmd_gpu *h, int64_t *launches, int64_t *loop_launc
  * allocator holds the rest of device memory, or a host loop that must not take
  * the allocator's locks or its implicit device synchronisation.
  *
+ * Results equal sdmd_gpu_prepare's bit for bit on both prediction paths, but
+ * the sweep runs sequentially over each system's atoms (one block per system):
+ * on the FP32 screened path sdmd_gpu_prepare runs a parallel sweep instead, so
+ * this call takes longer on large systems (about 0.7 s against 18 ms at 42k atoms).
+ *
  * Limits and rules:
  *   - the batch must fit: 256-aligned n_systems descriptors plus, with
  *     full_predict and per system with a thermostat, about 28 bytes per atom.
  *     Larger batches return SDMD_ECAPACITY with a message on stderr and change
  *     nothing; use sdmd_gpu_prepare for them.
  *   - the first call on a device looks up the array's address
- *     (cudaGetSymbolAddress) with the handle's device current; make that first
- *     call before any stream capture that could contain it.
+ *     (cudaGetSymbolAddress) with the handle's device current and keeps it for
+ *     the life of the process; make that first call before any stream capture
+ *     that could contain it, and make no call after a cudaDeviceReset.
  *   - the array is shared by every handle on a device and keeps its contents
  *     between calls.  Nothing in it must start at zero (each call writes what it
  *     reads), but calls that overlap in time race: serialise them per device.

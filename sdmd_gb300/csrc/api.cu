@@ -32,6 +32,7 @@ struct sdmd_gpu {
     unsigned char *arena = nullptr;
     size_t arena_bytes = 0;
     int threads = 128;
+    int sms = 0;                                   // the device's SM count
     size_t smem = 0, smem_loop = 0, vsmem = 0;
     int staged = 0;
     std::vector<int32_t> smp_cap_of;
@@ -215,7 +216,7 @@ static long long host_tkey(double d) {
 }
 constexpr int kConnWin = 9;   // ints per atom in conn_win
 constexpr int kMaxPerCell = 64; // screened path: atoms per cell array
-constexpr int kResidentBlocks = 1216; // parallel sweep: blocks in flight (8 per SM of 152)
+constexpr int kSweepBlocksPerSM = 8;   // parallel sweep: blocks in flight per SM
 
 // brackets of every FP64 threshold the prediction compares against, computed with
 // the same FP64 operations as the device (d + ZERO, d - ZERO, dmin - ZERO, dmax + ZERO)
@@ -545,7 +546,8 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     if (h->threads < 32 || h->threads > 1024 || (h->threads & 31)) { delete h; return SDMD_EINVAL; }
     if (h->smem > 227 * 1024) { delete h; return SDMD_ECAPACITY; }
     h->arena_bytes = layout(h, systems, nullptr, nullptr) + 256;
-    if ((r = cuda_fail(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) ||
+    if ((r = cuda_fail(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->opts.device))) ||
+        (r = cuda_fail(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) ||
         (r = cuda_fail(cudaEventCreate(&h->e0))) || (r = cuda_fail(cudaEventCreate(&h->e1))) ||
         (r = cuda_fail(cudaEventCreate(&h->l0))) || (r = cuda_fail(cudaEventCreate(&h->l1))) ||
         (r = cuda_fail(cudaMalloc(&h->arena, h->arena_bytes))) ||
@@ -657,7 +659,7 @@ extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
         // in-order fix-up and the event tree
         const unsigned ns = (unsigned)h->n_systems;
         if (full_predict) {
-            const int per_sys = std::max(1, kResidentBlocks / h->n_systems);
+            const int per_sys = std::max(1, kSweepBlocksPerSM * h->sms / h->n_systems);
             const unsigned rx = (unsigned)std::max(1, std::min(per_sys, (nmax + 255) / 256));
             const unsigned px = (unsigned)std::max(1, std::min(per_sys, nmax));
             const unsigned vx = (unsigned)std::max(1, std::min(per_sys, (nmax + 3) / 4));
@@ -904,10 +906,14 @@ extern "C" void sdmd_rng_skip(sdmd_rng *r, int64_t n) {
 }
 
 // ---- allocation-free full-rebuild sweep -------------------------------------------
-// sdmd_gpu_prepare_noalloc runs the same kernels as sdmd_gpu_prepare, but the
-// scratch they need -- the descriptor table the launches read and each system's
-// thermostat sample buffers -- lives in one file-scope device array instead of the
-// handle's arena, and the host side uses no heap.  Layout of the array:
+// sdmd_gpu_prepare_noalloc gives the results of sdmd_gpu_prepare, but the scratch
+// it needs -- the descriptor table the launches read and each system's thermostat
+// sample buffers -- lives in one file-scope device array instead of the handle's
+// arena, and the host side uses no heap.  On both prediction paths it runs the
+// sequential sweep kernel (one block per system, atoms in order): on the FP32
+// screened path that is sweep_kernel_screen, whose results equal the parallel
+// sweep's bit for bit but which takes longer on large systems (about 0.7 s
+// against 18 ms for 42k atoms).  Layout of the array:
 //   [descriptor table: n_systems DSys, 256-aligned]
 //   [first-error record, 256-aligned]
 //   per system with a thermostat: [smp: cap doubles][smp_raw: 3 cap int32][smp_cum: cap int64],
@@ -918,7 +924,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[SDMD_NOALLOC_SC
 
 namespace {
 constexpr int kNoallocMaxDevices = 64;
-unsigned char *g_noalloc_addr[kNoallocMaxDevices];   // resolved once per device
+// The array's device address, resolved once per device by the first call there.
+// The cache assumes the device's primary context lives as long as the process:
+// after a cudaDeviceReset the next call would use a stale address.
+unsigned char *g_noalloc_addr[kNoallocMaxDevices];
 
 __host__ __device__ inline size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
 __host__ __device__ inline int64_t noalloc_cap(int32_t n, int32_t thermostat) { return thermostat ? (int64_t)n + 8 : 0; }
@@ -929,16 +938,18 @@ __host__ __device__ inline size_t noalloc_head_bytes(int n_systems) {
     return al256(sizeof(DSys) * (size_t)n_systems) + al256(sizeof(sdmd_error_info));
 }
 
-// copy the handle's descriptors into the table, pointing the sample buffers into the array
-__global__ void noalloc_table_kernel(const DSys *src, int n_systems, unsigned char *base) {
+// copy the handle's descriptors into the table; with full_predict the sample
+// buffers point into the array (continue mode draws no sample and keeps the
+// handle's buffers, which the host-side size check did not count)
+__global__ void noalloc_table_kernel(const DSys *src, int n_systems, unsigned char *base, int full_predict) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     DSys *table = reinterpret_cast<DSys *>(base);
     size_t off = noalloc_head_bytes(n_systems);
     for (int k = 0; k < n_systems; k++) {
         DSys s = src[k];
-        int64_t cap = noalloc_cap(s.n, s.thermostat);
-        s.smp_cap = (int32_t)cap;
+        const int64_t cap = full_predict ? noalloc_cap(s.n, s.thermostat) : 0;
         if (cap) {
+            s.smp_cap = (int32_t)cap;
             s.smp = reinterpret_cast<double *>(base + off);
             s.smp_raw = reinterpret_cast<int32_t *>(base + off + al256((size_t)cap * 8));
             s.smp_cum = reinterpret_cast<int64_t *>(base + off + al256((size_t)cap * 8) + al256((size_t)cap * 12));
@@ -988,7 +999,7 @@ extern "C" int sdmd_gpu_prepare_noalloc(sdmd_gpu *h, int32_t full_predict) {
     sdmd_error_info *first = reinterpret_cast<sdmd_error_info *>(base + al256(sizeof(DSys) * (size_t)h->n_systems));
 
     CK(cudaEventRecord(h->e0, h->stream));
-    noalloc_table_kernel<<<1, 1, 0, h->stream>>>(h->ds, h->n_systems, base);
+    noalloc_table_kernel<<<1, 1, 0, h->stream>>>(h->ds, h->n_systems, base, full_predict ? 1 : 0);
     if (full_predict) {
         const int64_t want = (int64_t)nmax + 8;
         samples_walk_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(table, h->n_systems, want);

@@ -29,7 +29,7 @@ from .host import AMINO_ACIDS, build_system, generate_gro, params_text
 from .system import glibc_rng_state
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-DATA = os.path.join(REPO, "tests", "golden")          # holds Library_Ding (force-field input tables)
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")   # holds Library_Ding (force-field tables)
 BOLTZMANN = 0.0019872041                               # kcal/mol/K (src/REMDExec.c:19)
 
 

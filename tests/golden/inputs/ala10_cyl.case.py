@@ -5,9 +5,12 @@
 # wall events come early; the wall library is a test-local copy naming an
 # existing atom type (CA): the shipped Wall.txt names PHO, which AtomModel lacks
 # (src/Models.c:129-206), so ReadWall would exit.
+import os as _os
+
 import numpy as _np
 
-with open("/root/reference/input/ala10.gro") as _f:
+# REF: the reference checkout, given by make_golden.py
+with open(_os.path.join(REF, "input", "ala10.gro")) as _f:
     _lines = _f.read().splitlines()
 _n = int(_lines[1])
 _body = _lines[2:2 + _n]

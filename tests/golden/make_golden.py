@@ -1,9 +1,9 @@
 #!/usr/bin/env python3
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
-Runs in the build container only (it needs the reference sources at
-/root/reference): builds the reference's unmodified C sources with the oracle
-recipe (oracle/ref/Makefile -> oracle/_ref/sdmd_ref_harness), runs each case, and
+Runs only where the reference's sources are (the checkout named by the
+SDMD_REFERENCE environment variable, /root/reference by default): builds the
+reference's unmodified C sources with the oracle recipe (oracle/ref/Makefile -> oracle/_ref/sdmd_ref_harness), runs each case, and
 packs the dumps into compressed .npz fixtures that travel with the repository:
 
   pre/*        state after SDEnergyMin/PBC/LinkList, before the full-rebuild sweep
@@ -32,7 +32,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = "/root/reference"
+REF = os.environ.get("SDMD_REFERENCE", "/root/reference")   # the reference checkout
 HARNESS = os.path.join(REPO, "oracle", "_ref", "sdmd_ref_harness")
 
 PARAM_TEMPLATE = """Continue?          new
@@ -195,17 +195,18 @@ def cases():
             if fn.endswith(".case.py"):
                 spec = {}
                 with open(os.path.join(extra, fn)) as f:
-                    exec(f.read(), {"base_params": base_params, "extra": extra}, spec)
+                    exec(f.read(), {"base_params": base_params, "extra": extra, "REF": REF}, spec)
                 out[fn[:-len(".case.py")]] = spec["CASE"]
     return out
 
 
 def bundle_force_field():
     """Copy the reference's force-field input tables (Library_Ding, MIT licence,
-    input/Library_Ding/ of alexzheng42/sDMD) next to the fixtures: the tests and
-    the benchmark build systems from them on machines without the reference."""
+    input/Library_Ding/ of alexzheng42/sDMD) into the package's data directory:
+    the workload generator, the tests and the benchmark build systems from them on
+    machines without the reference."""
     src = os.path.join(REF, "input", "Library_Ding")
-    dst = os.path.join(HERE, "Library_Ding")
+    dst = os.path.join(REPO, "sdmd_gb300", "data", "Library_Ding")
     if os.path.isdir(dst):
         shutil.rmtree(dst)
     shutil.copytree(src, dst)

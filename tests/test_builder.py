@@ -18,6 +18,7 @@ from sdmd_gb300.host import build_system
 from sdmd_gb300.system import from_fixture
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
 POOLED = {"con_step_off", "pair_step_off", "con_step_d", "con_step_e", "con_step_acc", "pair_step_d", "pair_step_e",
           "pair_step_acc"}
 
@@ -31,7 +32,7 @@ def steps(s, kind, k):
 def test_builder_reproduces_the_reference_initial_state(golden, case, tmp_path):
     d = golden(case)
     lib = tmp_path / "Library_Ding"
-    shutil.copytree(os.path.join(HERE, "golden", "Library_Ding"), lib)
+    shutil.copytree(os.path.join(REPO, "sdmd_gb300", "data", "Library_Ding"), lib)
     if "meta/wall_lib" in d.files:
         (lib / "Wall.txt").write_bytes(bytes(d["meta/wall_lib"]))
     (tmp_path / "parameter.txt").write_bytes(bytes(d["meta/parameter"]))

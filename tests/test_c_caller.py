@@ -57,7 +57,7 @@ def test_plain_c_caller(golden, tmp_path):
     d = golden("ala10_nvt")
     data = tmp_path / "data"
     data.mkdir()
-    shutil.copytree(os.path.join(REPO, "tests", "golden", "Library_Ding"), data / "Library_Ding")
+    shutil.copytree(os.path.join(REPO, "sdmd_gb300", "data", "Library_Ding"), data / "Library_Ding")
     (data / "parameter.txt").write_bytes(bytes(d["meta/parameter"]))
     (data / "sys.gro").write_bytes(bytes(d["meta/gro"]))
     src = tmp_path / "caller.c"

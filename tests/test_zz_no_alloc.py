@@ -50,9 +50,15 @@ def assert_same(a, b):
         assert ta == tb
 
 
-def test_noalloc_sweep_equals_prepare_on_two_calls_in_a_row(golden, engine_mod):
+@pytest.mark.parametrize("screen", ["fp64", "fp32"])
+@pytest.mark.parametrize("advance", ["eager", "lazy"])
+def test_noalloc_sweep_equals_prepare_on_two_calls_in_a_row(golden, engine_mod, screen, advance):
+    # on the FP32 screened path sdmd_gpu_prepare runs the parallel sweep and the
+    # allocation-free call the sequential one: both must give the same state
+    opts = dict(screen=engine_mod.SCREEN_FP32 if screen == "fp32" else engine_mod.SCREEN_FP64,
+                advance=engine_mod.ADVANCE_LAZY if advance == "lazy" else engine_mod.ADVANCE_EAGER)
     ref, got = batch(golden, 3), batch(golden, 3)
-    with engine_mod.Engine(ref) as e_ref, engine_mod.Engine(got) as e_got:
+    with engine_mod.Engine(ref, **opts) as e_ref, engine_mod.Engine(got, **opts) as e_got:
         for call in range(2):
             e_ref.prepare(full=True)
             e_got.prepare_noalloc(full=True)
