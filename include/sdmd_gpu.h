@@ -173,7 +173,12 @@ typedef struct sdmd_opts {
     int32_t threads_per_system;    /* 32 (one warp) .. 256; 0 = autotuned */
     int32_t device;                /* CUDA device ordinal */
     int32_t trace_capacity;        /* records kept by sdmd_gpu_run when tracing (0 = off) */
-    int32_t reserved[7];
+    /* eager advance on the FP32 screened path: blocks on other SMs that advance
+     * every atom the pop does not involve, in one cooperative launch with the
+     * systems' own blocks (0 = automatic: for up to SMs/2 systems of at least 2,048
+     * atoms, every SM the systems leave free; -1 = off; k > 0 = k blocks) */
+    int32_t helper_blocks;
+    int32_t reserved[6];
 } sdmd_opts;
 
 typedef struct sdmd_gpu sdmd_gpu;   /* opaque handle */
@@ -246,6 +251,13 @@ int  sdmd_gpu_run_remd(sdmd_gpu *h, int64_t n_exchanges, double t_end, sdmd_remd
  * alone) and the device time (ms) of the event-loop kernels alone, measured with
  * CUDA events around each of those launches. */
 int  sdmd_gpu_last_run_stats(sdmd_gpu *h, int64_t *launches, int64_t *loop_launches, double *loop_ms);
+
+/* How the handle launches its event loop: threads per system block, helper blocks
+ * of the eager advance (0: none), whether whole systems are staged in shared
+ * memory, and which loop kernel runs (SDMD_LOOP_*).  Any pointer may be NULL. */
+enum { SDMD_LOOP_FP64 = 0, SDMD_LOOP_SCREEN = 1, SDMD_LOOP_SCREEN_R128 = 2, SDMD_LOOP_SCREEN_HELPERS = 3 };
+int  sdmd_gpu_launch_info(sdmd_gpu *h, int32_t *threads, int32_t *helper_blocks, int32_t *staged,
+                          int32_t *loop_kernel);
 
 /* ---- allocation-free re-sweep ------------------------------------------------
  * No counterpart in the reference (its Prepare() allocates nothing on a GPU).

@@ -38,6 +38,8 @@ struct sdmd_gpu {
     std::vector<int32_t> smp_cap_of;
     void (*sweep_k)(const DSys *, int) = nullptr;            // plain FP64 or FP32-screened kernels
     void (*loop_k)(const DSys *, double, int) = nullptr;
+    int helpers = 0;                               // helper blocks of the eager advance (0: none)
+    Adv *adv = nullptr;                            // their per-system protocol words (in the arena)
     double prep_ms = 0, run_ms = 0;
     // energies / replica exchange scratch (one block: num, T, E, kin, warn, stop, rng, stats)
     unsigned char *aux = nullptr;
@@ -437,6 +439,9 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             put(c, (double *)d.pair_step_acc, s.pair_step_acc, (size_t)m.n_pair_steps);
         }
     }
+    // the helper protocol words of every system, contiguous (cleared before each launch)
+    h->adv = cv.take<Adv>((size_t)h->n_systems);
+    for (int k = 0; k < h->n_systems; k++) h->hs[k].adv = h->adv + k;
     return cv.off;
 }
 
@@ -527,6 +532,11 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         d.cut_key = host_tkey(cut);
         f32_bracket(SDMD_ZERO, d.zero32);
         for (int q = 0; q < 3; q++) f32_bracket(s.box[q], d.box32 + 2 * q);
+        {   // |x| bound for the eager records' rounding margin: 4 times the largest box edge
+            float b[2];
+            f32_bracket(4.0 * std::max(s.box[0], std::max(s.box[1], s.box[2])), b);
+            d.xmax32 = b[1];
+        }
     }
     const bool scr = h->opts.screen == SDMD_SCREEN_FP32;
     h->smem = scr ? screen_smem_bytes(nbcap_max) : fp64_smem_bytes(nbcap_max);
@@ -541,6 +551,9 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
                                                      s.n_con_steps, s.n_conn));
     }
     h->staged = (h->smem + st_max <= 192 * 1024) ? 1 : 0;
+    // helper blocks read and write the state in global memory: asking for them
+    // explicitly keeps the systems unstaged
+    if (scr && h->opts.advance == SDMD_ADVANCE_EAGER && h->opts.helper_blocks > 0) h->staged = 0;
     h->smem_loop = h->staged ? h->smem + st_max : h->smem;
     h->threads = h->opts.threads_per_system > 0 ? h->opts.threads_per_system : 128;
     if (h->threads < 32 || h->threads > 1024 || (h->threads & 31)) { delete h; return SDMD_EINVAL; }
@@ -611,6 +624,26 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
             return r;
         }
         if ((long)full * sms < n_systems && capped > full) h->loop_k = loop_kernel_screen_r128;
+    }
+    // Eager advance on the screened path: for a few large systems, helper blocks on
+    // the SMs the systems leave free advance every atom the pop does not involve
+    // (one cooperative launch; the blocks must all be resident at once).
+    if (scr && h->opts.advance == SDMD_ADVANCE_EAGER && !h->staged && h->opts.helper_blocks >= 0) {
+        int32_t nmax = 0;
+        for (auto &m : h->meta) nmax = std::max(nmax, m.n);
+        int coop = 0, per_sm = 0;
+        if ((r = cuda_fail(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->opts.device))) ||
+            (r = cuda_fail(cudaFuncSetAttribute(loop_kernel_screen_coop, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                (int)h->smem_loop))) ||
+            (r = cuda_fail(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, loop_kernel_screen_coop, h->threads,
+                                                                         h->smem_loop)))) {
+            sdmd_gpu_destroy(h);
+            return r;
+        }
+        const int room = per_sm * h->sms - n_systems;
+        int want = h->opts.helper_blocks;
+        if (want == 0) want = (n_systems * 2 <= h->sms && nmax >= 2048) ? room : 0;
+        if (coop && want > 0 && room > 0) h->helpers = std::min(want, room);
     }
     if (h->opts.advance == SDMD_ADVANCE_LAZY) lazy_enter_kernel<<<n_systems, 128, 0, h->stream>>>(h->ds);
     if ((r = cuda_fail(cudaStreamSynchronize(h->stream)))) { sdmd_gpu_destroy(h); return r; }
@@ -709,7 +742,17 @@ static int run_rounds(sdmd_gpu *h, int64_t want, double t_end) {
     for (int round = 0; round < 1 << 20; round++) {
         launch_samples(h, want);
         CK(cudaEventRecord(h->l0, h->stream));
-        h->loop_k<<<h->n_systems, h->threads, h->smem_loop, h->stream>>>(h->ds, t_end, h->staged);
+        if (h->helpers > 0) {   // the systems' blocks and their helper blocks, all resident at once
+            CK(cudaMemsetAsync(h->adv, 0, sizeof(Adv) * (size_t)h->n_systems, h->stream));
+            const DSys *ds = h->ds;
+            double te = t_end;
+            int nc = h->n_systems;
+            void *args[] = {(void *)&ds, (void *)&te, (void *)&nc};
+            CK(cudaLaunchCooperativeKernel((const void *)loop_kernel_screen_coop, dim3(nc + h->helpers),
+                                           dim3(h->threads), args, h->smem_loop, h->stream));
+        } else {
+            h->loop_k<<<h->n_systems, h->threads, h->smem_loop, h->stream>>>(h->ds, t_end, h->staged);
+        }
         CK(cudaEventRecord(h->l1, h->stream));
         samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
         CK(cudaGetLastError());
@@ -1020,6 +1063,21 @@ extern "C" int sdmd_gpu_prepare_noalloc(sdmd_gpu *h, int32_t full_predict) {
     if (e.code) {
         h->err = e;
         return e.code;
+    }
+    return SDMD_OK;
+}
+
+extern "C" int sdmd_gpu_launch_info(sdmd_gpu *h, int32_t *threads, int32_t *helper_blocks, int32_t *staged,
+                                    int32_t *loop_kernel) {
+    if (!h) return SDMD_EINVAL;
+    if (threads) *threads = h->threads;
+    if (helper_blocks) *helper_blocks = h->helpers;
+    if (staged) *staged = h->staged;
+    if (loop_kernel) {
+        if (h->helpers > 0) *loop_kernel = SDMD_LOOP_SCREEN_HELPERS;
+        else if (h->loop_k == loop_kernel_screen_r128) *loop_kernel = SDMD_LOOP_SCREEN_R128;
+        else if (h->loop_k == loop_kernel_screen) *loop_kernel = SDMD_LOOP_SCREEN;
+        else *loop_kernel = SDMD_LOOP_FP64;
     }
     return SDMD_OK;
 }

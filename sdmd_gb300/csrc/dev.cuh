@@ -33,6 +33,40 @@ struct DScal {
     double stop_time;        // > 0: stop after the first executed event with time >= stop_time
 };
 
+// Eager advance by helper blocks (large systems, one cooperative launch).  The
+// system's own block publishes each pop (seq, dt, target, partner) with a release
+// store; the helper blocks advance every other atom (UpdateData / TimeForward,
+// src/ToolFunctions.c:23-36) and count their completions in `done` with release
+// adds.  The two groups of fields sit on separate 128-byte lines.
+constexpr unsigned long long ADV_STOP = ~0ull;
+struct __align__(128) Adv {
+    unsigned long long seq;   // pops published so far; ADV_STOP ends the helpers
+    double dt;
+    int32_t t, p;
+    int32_t herr;             // set by a helper whose wait for the next pop ran out
+    int32_t pad0[25];
+    unsigned long long done;  // helper completions, all pops together
+    int32_t pad1[30];
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_release_add(unsigned long long *p, unsigned long long v) {
+    asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+constexpr unsigned long long ADV_WAIT_NS = 2000000000ull;   // 2 s without progress ends a wait
+
 // one system's device arrays (all 1-based per-atom arrays, entry 0 unused)
 struct DSys {
     int32_t n, ncell;
@@ -113,14 +147,27 @@ struct DSys {
     // i's constraint list (first occurrence), -1 for none; con_ok[i] = 0 when a
     // partner lies outside the window (the list is then searched)
     const int8_t *con_win, *con_ok;
-    // lazy mode, screened path: per atom a 64-byte record of outward-rounded FP32
-    // intervals -- {x, y}, {z, vx}, {vy, vz}, {tloc - T0, packed cell} -- so that a
-    // candidate's position interval costs FP32 work only; valid while shadow_ok.
-    // [nlo, nhi] holds now - T0 for the event being predicted.
+    // screened path: per atom a 64-byte record of outward-rounded FP32 intervals --
+    // {x, y}, {z, vx}, {vy, vz}, {tr - T0, packed cell} -- so that a candidate's
+    // position interval costs FP32 work only; valid while shadow_ok.  tr is the
+    // time the record's position belongs to: tloc in lazy mode, the clock value of
+    // the pop that wrote the record in eager mode.  [nlo, nhi] holds now - T0 for
+    // the event being predicted.
     float4 *shr;
     double T0;
     int32_t shadow_ok;
     float nlo, nhi;
+    // eager mode: the record bounds x(tr) + v (now - tr), while the position the
+    // reference's step-by-step advance reaches differs from it by the rounding of
+    // the pops since tr.  Per axis that is at most mxa + mxb |v| (see loop_body);
+    // xmax32 bounds |x| for every atom (4 times the largest box edge).
+    float mxa, mxb, xmax32;
+    float T0f;                // an upper bound of T0 as a float (eager mode)
+    // eager mode with helper blocks: adv_on in the block's copy while they run,
+    // adv_h of them advance this system, adv_seq pops published so far
+    Adv *adv;
+    int32_t adv_on, adv_h;
+    unsigned long long adv_seq;
 };
 
 // position component of atom j at the current time (lazy mode extrapolates)

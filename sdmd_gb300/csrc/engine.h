@@ -7,6 +7,7 @@
 namespace sdmd {
 struct DSys;
 struct DScal;
+struct Adv;
 
 // exact FP64 path (loop_fp64.cu)
 size_t fp64_smem_bytes(int nbcap);
@@ -20,6 +21,9 @@ size_t screen_smem_bytes(int nbcap);
 __global__ void sweep_kernel_screen(const DSys *systems, int full);
 __global__ void loop_kernel_screen(const DSys *systems, double t_end_override, int staged);
 __global__ void loop_kernel_screen_r128(const DSys *systems, double t_end_override, int staged);
+// the screened loop with helper blocks for the eager advance (cooperative launch:
+// blocks 0 .. n_chain-1 run the systems, the rest advance their atoms)
+__global__ void loop_kernel_screen_coop(const DSys *systems, double t_end_override, int n_chain);
 
 // parallel full-rebuild sweep of the screened path (sweep_par.cuh)
 size_t verify_smem_bytes(int nbcap, int warps);

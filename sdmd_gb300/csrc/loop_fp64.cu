@@ -39,6 +39,76 @@ __device__ inline void set_err(Blk &B, int code, int atom) {
     if (B.err == 0) { B.err = code; B.err_atom = atom; }
 }
 
+// Helper-block side of the eager advance: wait for the next published pop, then
+// x += v dt and t -= dt (UpdateData / TimeForward, src/ToolFunctions.c:23-36) for
+// this block's slice of atoms, except the pop's target and partner, which the
+// system's own block advances itself.  Every wait is bounded.
+__device__ __noinline__ void helper_body(const DSys *systems, int n_systems) {
+    const int b = blockIdx.x - n_systems, nh = gridDim.x - n_systems;
+    const int s = b % n_systems, h = b / n_systems;
+    const int H = (nh - s + n_systems - 1) / n_systems;    // helpers of system s
+    const DSys &G = systems[s];
+    const int n = G.n;
+    const int a0 = 1 + (int)((long long)h * n / H), a1 = 1 + (int)((long long)(h + 1) * n / H);
+    double *x = G.x, *y = G.y, *z = G.z, *et = G.ev_time;
+    const double *vx = G.vx, *vy = G.vy, *vz = G.vz;
+    Adv *A = G.adv;
+    __shared__ double s_dt;
+    __shared__ int32_t s_t, s_p, s_go;
+    unsigned long long seen = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            unsigned long long q;
+            const unsigned long long t0 = gtimer();
+            int go = 1;
+            while ((q = ld_acquire(&A->seq)) == seen) {
+                if (gtimer() - t0 > ADV_WAIT_NS) { atomicExch(&A->herr, 1); go = 0; break; }
+                __nanosleep(100);
+            }
+            if (go && q == ADV_STOP) go = 0;
+            if (go) {
+                seen = q;
+                s_dt = *(volatile double *)&A->dt;
+                s_t = *(volatile int32_t *)&A->t;
+                s_p = *(volatile int32_t *)&A->p;
+            }
+            s_go = go;
+        }
+        __syncthreads();
+        if (!s_go) break;
+        const double dt = s_dt;
+        const int t = s_t, p = s_p;
+        for (int i = a0 + threadIdx.x; i < a1; i += blockDim.x) {
+            if (i == t || i == p) continue;
+            x[i] += vx[i] * dt;
+            y[i] += vy[i] * dt;
+            z[i] += vz[i] * dt;
+            et[i] -= dt;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) red_release_add(&A->done, 1ull);
+    }
+}
+
+// the system's block: publish this pop to the helpers
+__device__ __forceinline__ void adv_publish(DSys &S, int t, int p, double dt) {
+    Adv *A = S.adv;
+    *(volatile double *)&A->dt = dt;
+    *(volatile int32_t *)&A->t = t;
+    *(volatile int32_t *)&A->p = p;
+    S.adv_seq++;
+    st_release(&A->seq, S.adv_seq);
+}
+// the system's block: wait until every helper advanced the last published pop
+__device__ __noinline__ void adv_wait(const DSys &S, Blk &B) {
+    const unsigned long long want = S.adv_seq * (unsigned long long)S.adv_h;
+    const unsigned long long t0 = gtimer();
+    while (ld_acquire(&S.adv->done) < want) {
+        if (gtimer() - t0 > ADV_WAIT_NS) { set_err(B, SDMD_ETIMEOUT, 0); return; }
+        __nanosleep(20);
+    }
+}
+
 // lazy mode: bring the target t and the partner p (when > 0) to the current time
 // before they change, x += v * (now - tloc) per axis.  Lanes 0..5 of warp 0 take
 // one (atom, axis) each: the six independent FP64 chains share warp-instructions.
@@ -903,22 +973,36 @@ __global__ void sweep_kernel_screen(const DSys *systems, int full) {
 // The event loop (src/SGThread.c:75-151)
 template <bool SCR>
 __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_override, int staged, DSys &S, DSys &G,
-                                          Blk &B, DScal &C, PairScal &PS) {
-    if (threadIdx.x == 0) { S = systems[blockIdx.x]; G = S; }
+                                          Blk &B, DScal &C, PairScal &PS, int n_chain = 0) {
+    if (threadIdx.x == 0) {
+        S = systems[blockIdx.x];
+        G = S;
+        // a launch of n_chain system blocks plus helper blocks (helper_body): the
+        // helpers numbered b = s, s + n_chain, ... advance system s's other atoms
+        const int nh = n_chain > 0 ? (int)gridDim.x - n_chain : 0;
+        S.adv_h = nh > 0 ? (nh - (int)blockIdx.x + n_chain - 1) / n_chain : 0;
+        S.adv_on = S.adv_h > 0 && !S.lazy && S.adv != nullptr;
+        S.adv_seq = 0;
+    }
     const int tid = threadIdx.x, T = blockDim.x;
     __shared__ int32_t sh_t, sh_p, sh_exec, sh_go;
     __shared__ double sh_dt;
     __shared__ int32_t rec_partner, rec_type, rec_sub;
     __shared__ int32_t sh_move[3], sh_cells_ok, sh_rebase;
     // the records' epoch T0 moves to the current time every 4N pops, so that the
-    // interval of now - T0 stays about one mean free flight wide
-    int64_t rebase_at = C.pops + 4 * (int64_t)S.n;
+    // interval of now - T0 stays about one mean free flight wide (thread 0's copies)
+    int64_t rebase_at = 0, rec_pop0 = 0;
     if (tid == 0) {
         B.err = 0; B.warn = 0; C = *S.sc;
         if (!C.cbt_built && !C.err) { C.err = SDMD_EINVAL; C.err_atom = 0; *S.sc = C; }   // prepare() first
+        rebase_at = C.pops + 4 * (int64_t)S.n;
+        rec_pop0 = C.pops;
     }
     __syncthreads();
-    if (C.err) return;
+    if (C.err) {
+        if (tid == 0 && S.adv_h > 0) st_release(&S.adv->seq, ADV_STOP);
+        return;
+    }
     Shm M;
     ShmS MS;
     if constexpr (SCR) carve_screen(MS, S.nbcap); else carve(M, S.nbcap);
@@ -931,8 +1015,12 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
         __syncthreads();
         if (tid == 0) sh_cells_ok = B.err == 0;
         stage_rp(S);
-        if (S.lazy && S.shr) {   // interval records of every atom for this launch (epoch T0 = now)
-            if (tid == 0) S.T0 = C.time;
+        if (S.shr) {   // interval records of every atom for this launch (epoch T0 = now)
+            if (tid == 0) {
+                S.T0 = C.time;
+                S.T0f = __double2float_ru(C.time);
+                if (!S.lazy) S.now = C.time;   // eager: the records hold the positions at the clock's value
+            }
             __syncthreads();
             for (int k = 1 + tid; k <= S.n; k += T)
                 for (int w = 0; w < 4; w++) shadow_word(S, k, w);
@@ -969,6 +1057,15 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
                     }
                 } else {
                     sh_dt = tev;
+                    sh_rebase = 0;
+                    // eager: records are rewritten from the positions before this pop's
+                    // advance, which belong to the clock's current value
+                    if (S.shadow_ok && C.pops >= rebase_at) {
+                        S.T0 = C.time; S.T0f = __double2float_ru(C.time); S.now = C.time;
+                        rebase_at = C.pops + 4 * (int64_t)S.n; rec_pop0 = C.pops; sh_rebase = 1;
+                    }
+                    // the helpers start on this pop at once (after the records, when they are rebuilt)
+                    if (S.adv_on && !sh_rebase) adv_publish(S, t, rp > 0 ? rp : 0, tev);
                 }
                 sh_p = rp > 0 ? rp : 0;
             }
@@ -976,32 +1073,65 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
         __syncthreads();
         if (!sh_go) break;
         if constexpr (SCR) {
-            if (S.lazy && S.shadow_ok && sh_rebase) {   // every record against the new epoch
+            if (S.shadow_ok && sh_rebase) {   // every record against the new epoch
                 for (int k = 1 + tid; k <= S.n; k += T)
                     for (int w = 0; w < 4; w++) shadow_word(S, k, w);
                 __syncthreads();
+                if (tid == 0 && S.adv_on) adv_publish(S, sh_t, sh_p, sh_dt);
             }
         }
         const double dt = sh_dt;
-        if (!S.lazy) {
-            for (int i = 1 + tid; i <= S.n; i += T) {      // UpdateData + TimeForward
-                S.x[i] += S.vx[i] * dt;
-                S.y[i] += S.vy[i] * dt;
-                S.z[i] += S.vz[i] * dt;
-                S.ev_time[i] -= dt;
-            }
-            __syncthreads();
-        }
         const int t = sh_t, p = sh_p;
+        if (!S.lazy) {
+            if (S.adv_on) {   // the helpers advance the rest; lanes 0-7 take t's and p's x, y, z, time
+                if (tid < 8) {
+                    const int a = tid < 4 ? t : p, d = tid & 3;
+                    if (a > 0) {
+                        if (d == 3) S.ev_time[a] -= dt;
+                        else {
+                            double *X = d == 0 ? S.x : (d == 1 ? S.y : S.z);
+                            const double *V = d == 0 ? S.vx : (d == 1 ? S.vy : S.vz);
+                            X[a] += V[a] * dt;
+                        }
+                    }
+                }
+                if (tid < 32) __syncwarp();
+            } else {
+                for (int i = 1 + tid; i <= S.n; i += T) {      // UpdateData + TimeForward
+                    S.x[i] += S.vx[i] * dt;
+                    S.y[i] += S.vy[i] * dt;
+                    S.z[i] += S.vz[i] * dt;
+                    S.ev_time[i] -= dt;
+                }
+                __syncthreads();
+            }
+        }
         sync_pair_warp0(S, t, p);
         if (tid == 0) {
             if (S.lazy) C.time = S.now;
-            else C.time += dt;
+            else {
+                C.time += dt;
+                S.now = C.time;
+                if (S.shadow_ok) {
+                    // A record written at the clock value tr bounds x(tr) + v (now - tr).
+                    // The reference's position is x(tr) advanced by m separately rounded
+                    // steps x += v dt_k, and its clock also rounds at every step, so the
+                    // two differ by at most 2u m (|v| |now| + max|x|) per axis
+                    // (u = 2^-53), for the m <= pops - rec_pop0 + 1 pops since tr.
+                    shadow_now(S);
+                    const float m = (float)(C.pops - rec_pop0 + 1);
+                    const float c = __fmul_ru(m, 0x1p-51f);
+                    S.mxa = __fmul_ru(c, S.xmax32);
+                    S.mxb = __fmul_ru(c, __fadd_ru(S.nhi, S.T0f));
+                }
+            }
             int hazard = p > 0 && S.ev_pcounter[t] < S.ev_counter[p];   // HazardCheck
             sh_exec = !hazard;
             sh_move[0] = 0;
             if (!hazard) {
                 C.c.frame++;
+                // an HB event rescans the target's neighbourhood: every atom must be current
+                if (S.adv_on && S.ev_type[t] == SDMD_EV_HB) adv_wait(S, B);
                 do_event(S, C, t, p, B, SCR ? sh_move : nullptr);
                 S.ev_counter[t]++;
                 if (p) S.ev_counter[p]++;
@@ -1045,6 +1175,7 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
         }
         __syncthreads();
     }
+    if (tid == 0 && S.adv_h > 0) st_release(&S.adv->seq, ADV_STOP);   // the helpers stop
     if constexpr (SCR) {
         __syncthreads();
         if (sh_cells_ok) cells_to_list(S);
@@ -1085,6 +1216,18 @@ __global__ void __launch_bounds__(256, 2) loop_kernel_screen_r128(const DSys *sy
     __shared__ DScal C;
     __shared__ PairScal PS;
     loop_body<true>(systems, t_end_override, staged, S, G, B, C, PS);
+}
+
+__global__ void loop_kernel_screen_coop(const DSys *systems, double t_end_override, int n_chain) {
+    __shared__ DSys S, G;
+    __shared__ Blk B;
+    __shared__ DScal C;
+    __shared__ PairScal PS;
+    if ((int)blockIdx.x >= n_chain) {
+        helper_body(systems, n_chain);
+        return;
+    }
+    loop_body<true>(systems, t_end_override, 0, S, G, B, C, PS, n_chain);
 }
 
 size_t screen_smem_bytes(int nbcap) { return screen_smem_bytes_dev(nbcap); }

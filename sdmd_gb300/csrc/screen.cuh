@@ -125,7 +125,7 @@ __device__ __forceinline__ void shadow_word(const DSys &S, int k, int w) {
         case 2: r = make_float4(__double2float_rd(S.vy[k]), __double2float_ru(S.vy[k]),
                                 __double2float_rd(S.vz[k]), __double2float_ru(S.vz[k])); break;
         default: {
-            const double d = S.tloc[k] - S.T0;
+            const double d = (S.lazy ? S.tloc[k] : S.now) - S.T0;
             r = make_float4(f_dn(__double2float_rd(d)), f_up(__double2float_ru(d)),
                             __int_as_float(S.cx[k] | S.cy[k] << 10 | S.cz[k] << 20), 0.f);
         }
@@ -149,6 +149,14 @@ __device__ __forceinline__ void atom_piv(const DSys &S, int j, PIv &P) {
     P.x[0] = iadd(ivc(a.x, a.y), imul(P.v[0], dt));
     P.x[1] = iadd(ivc(a.z, a.w), imul(P.v[1], dt));
     P.x[2] = iadd(ivc(b.x, b.y), imul(P.v[2], dt));
+    if (!S.lazy) {   // eager: widen by the rounding of the step-by-step advance since tr
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            const float vm = fmaxf(fabsf(P.v[d].lo), fabsf(P.v[d].hi));
+            const float mx = __fmaf_ru(S.mxb, vm, S.mxa);
+            P.x[d] = ivc(__fsub_rd(P.x[d].lo, mx), __fadd_ru(P.x[d].hi, mx));
+        }
+    }
     const int cp = __float_as_int(e.z);
     P.c[0] = cp & 1023; P.c[1] = (cp >> 10) & 1023; P.c[2] = cp >> 20;
 }
@@ -1161,6 +1169,10 @@ __device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
             PS.over[a] = base > RC;
         }
     }
+    // Eager mode with helper blocks: from here on exact positions and event times
+    // of other atoms are read (refine, folds, tree repair); the screen above used
+    // the records only.
+    if (S.adv_on && tid == 0) adv_wait(S, B);
     __syncthreads();
     // 6. exact FP64 for the refined entries, packed into lanes; one warp per kind
     {

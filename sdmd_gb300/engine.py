@@ -21,7 +21,10 @@ SCREEN_FP64, SCREEN_FP32 = 0, 1
 ABI_FUNCS = ["sdmd_gpu_abi_version", "sdmd_gpu_device_count", "sdmd_gpu_strerror", "sdmd_gpu_create",
              "sdmd_gpu_destroy", "sdmd_gpu_prepare", "sdmd_gpu_run", "sdmd_gpu_download", "sdmd_gpu_trace",
              "sdmd_gpu_last_ms", "sdmd_gpu_last_error", "sdmd_rng_seed", "sdmd_rng_next", "sdmd_rng_skip",
-             "sdmd_gpu_prepare_noalloc", "sdmd_gpu_last_run_stats", "sdmd_gpu_energies", "sdmd_gpu_run_remd"]
+             "sdmd_gpu_prepare_noalloc", "sdmd_gpu_last_run_stats", "sdmd_gpu_energies", "sdmd_gpu_run_remd",
+             "sdmd_gpu_launch_info"]
+LOOP_KERNELS = {0: "loop_kernel_fp64", 1: "loop_kernel_screen", 2: "loop_kernel_screen_r128",
+                3: "loop_kernel_screen_coop"}
 
 _lib = None
 
@@ -66,6 +69,7 @@ def lib():
         L.sdmd_gpu_last_run_stats.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_double)]
         L.sdmd_gpu_energies.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.sdmd_gpu_run_remd.argtypes = [C.c_void_p, C.c_int64, C.c_double, P(sdmd_remd)]
+        L.sdmd_gpu_launch_info.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32), P(C.c_int32)]
         L.sdmd_rng_seed.argtypes = [P(sdmd_rng), C.c_uint32]
         L.sdmd_rng_seed.restype = None
         L.sdmd_rng_next.argtypes = [P(sdmd_rng)]
@@ -92,11 +96,14 @@ def device_count():
 class Engine:
     """A handle over a batch of systems (sdmd_gb300.system.System objects)."""
 
-    def __init__(self, systems, advance=ADVANCE_EAGER, screen=SCREEN_FP64, threads=0, trace=0, device=0):
+    def __init__(self, systems, advance=ADVANCE_EAGER, screen=SCREEN_FP64, threads=0, trace=0, device=0, helpers=0):
+        """helpers: blocks of the eager advance on the screened path (sdmd_opts.helper_blocks:
+        0 automatic, -1 off, k > 0 exactly k)."""
         self.systems = list(systems)
         self.structs = (sdmd_system * len(self.systems))(*[s.struct() for s in self.systems])
         o = sdmd_opts()
         o.advance, o.screen, o.threads_per_system, o.device, o.trace_capacity = advance, screen, threads, device, trace
+        o.helper_blocks = helpers
         self.opts = o
         h = C.c_void_p()
         rc = lib().sdmd_gpu_create(self.structs, len(self.systems), C.byref(o), C.byref(h))
@@ -170,6 +177,13 @@ class Engine:
         out_rng = np.array([x.rng.tab[i] for i in range(31)] + [x.rng.front, x.rng.rear], np.int32)
         return {"num": num, "T": T, "E": E, "rng": out_rng, "attempted": x.attempted, "accepted": x.accepted,
                 "done": x.exchanges_done}
+
+    def launch_info(self):
+        """dict(threads, helper_blocks, staged, loop_kernel) of the handle's event-loop launch."""
+        v = [C.c_int32(0) for _ in range(4)]
+        self._check(lib().sdmd_gpu_launch_info(self.h, *[C.byref(x) for x in v]), "sdmd_gpu_launch_info")
+        return {"threads": v[0].value, "helper_blocks": v[1].value, "staged": bool(v[2].value),
+                "loop_kernel": LOOP_KERNELS.get(v[3].value, str(v[3].value))}
 
     def last_run_stats(self):
         """(kernels launched, event-loop kernels launched, event-loop kernel ms) of the last run."""

@@ -89,7 +89,8 @@ assert TRACE_DTYPE.itemsize == C.sizeof(sdmd_trace_rec)
 
 class sdmd_opts(C.Structure):
     _fields_ = [("advance", C.c_int32), ("screen", C.c_int32), ("threads_per_system", C.c_int32),
-                ("device", C.c_int32), ("trace_capacity", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("device", C.c_int32), ("trace_capacity", C.c_int32), ("helper_blocks", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class sdmd_error_info(C.Structure):

@@ -118,3 +118,59 @@ def test_emulated_directed_rounding_brackets_the_value():
     lo, hi = rd(x), ru(x)
     assert (lo.astype(np.float64) <= x).all() and (x <= hi.astype(np.float64)).all()
     assert (hi.astype(np.float64) - lo.astype(np.float64) <= np.abs(x) * 2 ** -22).all()
+
+
+def fma_ru(a, b, c):
+    """fmaf(a, b, c) rounded up, for floats: a*b is exact in FP64, then the sum."""
+    p = a.astype(np.float64) * b.astype(np.float64)
+    s, e = two_sum(p, c.astype(np.float64))
+    f = ru(s)
+    return np.where((f.astype(np.float64) == s) & (e > 0), np.nextafter(f, F32(np.inf)), f)
+
+
+def mul_ru(a, b):
+    return ru(a.astype(np.float64) * b.astype(np.float64))
+
+
+def eager_margin(m, xmax32, nhi, T0f, v_lo, v_hi):
+    """The device's per-axis widening in eager mode (loop_body, atom_piv): with
+    c = m 2^-51, mx = c max|x| + c (now - T0 + T0) |v|, all rounded up."""
+    c = mul_ru(m.astype(F32), np.full_like(m, 2.0 ** -51, dtype=F32))
+    mxa = mul_ru(c, np.full_like(c, xmax32))
+    mxb = mul_ru(c, add_ru(nhi, T0f))
+    vm = np.maximum(np.abs(v_lo), np.abs(v_hi))
+    return fma_ru(mxb, vm, mxa)
+
+
+def test_eager_records_contain_the_stepwise_position():
+    """Eager mode: the record holds x(tr), v and tr - T0, where tr is the clock
+    value of the pop that wrote it.  The reference then advances x += v dt_k at
+    every pop and its clock t += dt_k, each step rounded.  The record's interval,
+    widened by the rounding margin of the m pops since tr, must contain that
+    step-by-step position."""
+    rng = np.random.default_rng(77)
+    n = 20_000
+    box = 440.0
+    xmax32 = ru(np.array([4.0 * box]))[0]
+    for m_steps, dt_scale, t0_scale in ((1, 1e-3, 1.0), (40, 1e-4, 1e3), (400, 1e-5, 10.0), (2000, 1e-6, 1e4)):
+        x = rng.uniform(-1.0, box + 1.0, n)
+        v = rng.normal(0.0, 2.0, n) * 10.0 ** rng.integers(-3, 1, n)
+        T0 = rng.uniform(0.0, t0_scale, n)
+        t = T0 + rng.uniform(0.0, 1.0, n) * dt_scale * m_steps   # the clock when the record was written
+        tr = t.copy()
+        xs = x.copy()
+        for _ in range(m_steps):                                 # UpdateData / the clock, step by step
+            dt = rng.exponential(dt_scale, n)
+            xs = xs + v * dt
+            t = t + dt
+        lo, hi = record_interval(x, v, tr, T0, t)                # tr plays tloc's part
+        dn = t - T0
+        nhi = f_up(ru(dn))
+        T0f = ru(T0)
+        vl, vh = rd(v), ru(v)
+        mx = eager_margin(np.full(n, m_steps, np.float64), xmax32, nhi, T0f, vl, vh)
+        lo, hi = sub_rd(lo, mx), add_ru(hi, mx)
+        inside = (lo.astype(np.float64) <= xs) & (xs <= hi.astype(np.float64))
+        assert inside.all(), (m_steps, np.nonzero(~inside)[0][:5])
+        # the margin stays far below the float resolution of the position
+        assert np.median(mx.astype(np.float64) / (np.abs(x) + 1.0)) < 1e-9 * max(m_steps, 1)
