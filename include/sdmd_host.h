@@ -66,6 +66,54 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
                       int errlen);
 void sdmd_free_text(char *p);
 
+/* ---- the reference's command line (InputData, src/Initialization.c:63-256) ----
+ * Flags are read exactly as the reference reads them; arguments that are not
+ * flags are skipped.  -i / -o must name existing directories.  Returns SDMD_OK,
+ * or SDMD_EINVAL with a message in errbuf.  `help` is set for -h / -help. */
+enum { SDMD_OUT_SAVED = 0, SDMD_OUT_TRJ, SDMD_OUT_POT, SDMD_OUT_KIN, SDMD_OUT_TEM, SDMD_OUT_CNT, SDMD_OUT_HBN,
+       SDMD_OUT_XYZ, SDMD_OUT_PDB, SDMD_OUT_LOG, SDMD_OUT_SYS, SDMD_CLI_NOUT };
+#define SDMD_CLI_NCHARGE 9   /* -arg -asp -glu -his -lys -ter -AlC -AlP -COM */
+typedef struct sdmd_cli {
+    char    datadir[1024];             /* -i */
+    char    savedir[1024];             /* -o */
+    char    coordinate_file[256];      /* -f (default coordinate.gro) */
+    char    saved_in[256];             /* -si (default savedData.dat; savedData<suffix>.dat with -REMD) */
+    char    out_name[SDMD_CLI_NOUT][256];  /* -so -trj -pot -kin -tem -cnt -HBn -xyz -pdb -lgf -sys names */
+    int32_t out_on[SDMD_CLI_NOUT];     /* optional outputs switched on (-pot -kin -tem -HBn -xyz / -pdb) */
+    double  box[3];                    /* -box x y z */
+    int32_t box_given;
+    double  wall_dyn_size, wall_dyn_rate;   /* -Wsz, -Wrt */
+    int32_t pre_bonds;                 /* -pre */
+    int32_t charge[SDMD_CLI_NCHARGE];  /* charge-model selections */
+    int32_t charge_no_pbc;             /* -npC */
+    int32_t remd;                      /* -REMD server port T num [rate] [suffix] */
+    char    remd_server[256];
+    int32_t remd_port, remd_num, remd_rate;
+    double  remd_T;
+    char    remd_suffix[64];
+    int32_t visual;                    /* -visual (the OpenGL viewer is not part of this engine) */
+    int32_t help;
+} sdmd_cli;
+int sdmd_parse_args(int argc, const char *const *argv, sdmd_cli *out, char *errbuf, int errlen);
+
+/* ---- REMDConfig.txt as the sREMD launcher reads it (src/REMDExec.c:79-110) ----
+ * A comment line, "ReplicaNum = n", "Temperatures = T1 .. Tn" (K, exactly n),
+ * "SocketPort = p", "ExchangeRate = r".  T[k] is the reduced temperature replica k
+ * runs at: T_kelvin[k] * 0.0019872041 printed with "%lf" and read back, as the
+ * launcher hands it over; num[k] = k + 1 is its ladder index and exchange_time
+ * the replica's exchange period (atoi of r), the sdmd_remd fields
+ * (include/sdmd_gpu.h) of an on-device replica exchange. */
+#define SDMD_REMD_MAX_REPLICAS 1024
+typedef struct sdmd_remd_config {
+    int32_t n_replicas;
+    int32_t port;                      /* SocketPort (no socket is used here) */
+    double  exchange_time;
+    double  T_kelvin[SDMD_REMD_MAX_REPLICAS];
+    double  T[SDMD_REMD_MAX_REPLICAS];
+    int32_t num[SDMD_REMD_MAX_REPLICAS];
+} sdmd_remd_config;
+int sdmd_read_remd_config(const char *path, sdmd_remd_config *out, char *errbuf, int errlen);
+
 sdmd_system *sdmd_host_view(sdmd_host_system *h);
 void sdmd_host_free(sdmd_host_system *h);
 

@@ -148,3 +148,50 @@ def generate_gro(datadir, sequences, box, wall=0, margin=5.0, seed=1, ff="Ding")
         return C.string_at(out).decode()
     finally:
         L.sdmd_free_text(out)
+
+
+# ---- the reference's command line and REMD configuration (host/cli.c) ----------
+NOUT, NCHARGE, REMD_MAX = 11, 9, 1024
+OUT_NAMES = ["saved", "trj", "pot", "kin", "tem", "cnt", "HBn", "xyz", "pdb", "log", "sys"]
+
+
+class sdmd_cli(C.Structure):
+    _fields_ = [("datadir", C.c_char * 1024), ("savedir", C.c_char * 1024), ("coordinate_file", C.c_char * 256),
+                ("saved_in", C.c_char * 256), ("out_name", (C.c_char * 256) * NOUT), ("out_on", C.c_int32 * NOUT),
+                ("box", C.c_double * 3), ("box_given", C.c_int32), ("wall_dyn_size", C.c_double),
+                ("wall_dyn_rate", C.c_double), ("pre_bonds", C.c_int32), ("charge", C.c_int32 * NCHARGE),
+                ("charge_no_pbc", C.c_int32), ("remd", C.c_int32), ("remd_server", C.c_char * 256),
+                ("remd_port", C.c_int32), ("remd_num", C.c_int32), ("remd_rate", C.c_int32), ("remd_T", C.c_double),
+                ("remd_suffix", C.c_char * 64), ("visual", C.c_int32), ("help", C.c_int32)]
+
+
+class sdmd_remd_config(C.Structure):
+    _fields_ = [("n_replicas", C.c_int32), ("port", C.c_int32), ("exchange_time", C.c_double),
+                ("T_kelvin", C.c_double * REMD_MAX), ("T", C.c_double * REMD_MAX), ("num", C.c_int32 * REMD_MAX)]
+
+
+def parse_args(argv):
+    """sdmd_parse_args over a list of strings (argv[0] is the program name)."""
+    L = lib()
+    L.sdmd_parse_args.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.POINTER(sdmd_cli), C.c_char_p, C.c_int]
+    arr = (C.c_char_p * len(argv))(*[a.encode() for a in argv])
+    out = sdmd_cli()
+    err = C.create_string_buffer(512)
+    rc = L.sdmd_parse_args(len(argv), arr, C.byref(out), err, 512)
+    if rc:
+        raise ValueError(err.value.decode())
+    return out
+
+
+def read_remd_config(path):
+    """sdmd_read_remd_config: dict(n, port, exchange_time, T_kelvin, T, num)."""
+    L = lib()
+    L.sdmd_read_remd_config.argtypes = [C.c_char_p, C.POINTER(sdmd_remd_config), C.c_char_p, C.c_int]
+    cfg = sdmd_remd_config()
+    err = C.create_string_buffer(512)
+    rc = L.sdmd_read_remd_config(str(path).encode(), C.byref(cfg), err, 512)
+    if rc:
+        raise ValueError(err.value.decode())
+    n = cfg.n_replicas
+    return {"n": n, "port": cfg.port, "exchange_time": cfg.exchange_time, "T_kelvin": list(cfg.T_kelvin[:n]),
+            "T": np.array(cfg.T[:n]), "num": np.array(cfg.num[:n], np.int32)}
