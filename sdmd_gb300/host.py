@@ -97,9 +97,14 @@ def _copy_out(view, names_ptr, res_ptr):
                     n_bonds=s.n_bonds, n_cons=s.n_cons, n_con_steps=s.n_con_steps, n_conn=s.n_conn,
                     n_pair_steps=s.n_pair_steps)
     out.pull_scalars(s)
-    out.names = C.string_at(names_ptr, 8 * (n + 1))
-    out.resnames = C.string_at(res_ptr, 8 * (n + 1))
+    out.names = C.string_at(names_ptr, 8 * (n + 1)) if names_ptr else None
+    out.resnames = C.string_at(res_ptr, 8 * (n + 1)) if res_ptr else None
     return out
+
+
+def system_from_struct(ptr):
+    """A System holding copies of the arrays an sdmd_system (POINTER) points to."""
+    return _copy_out(ptr, None, None)
 
 
 def build_system(datadir, coord_file=None, gro_text=None, params=None, param_path=None, seed=DEBUG_RANDOM_SEED,
