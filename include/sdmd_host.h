@@ -114,6 +114,38 @@ typedef struct sdmd_remd_config {
 } sdmd_remd_config;
 int sdmd_read_remd_config(const char *path, sdmd_remd_config *out, char *errbuf, int errlen);
 
+/* ---- the reference's checkpoint, savedData.dat (SaveDAT, src/DataSave.c:512-585;
+ * ReadBreakPoint, src/Initialization.c:360-509) -------------------------------
+ * sdmd_saved_read     reads a file into memory, every record kept;
+ * sdmd_saved_apply    writes the state a continue run starts from into a system
+ *                     built from the same inputs (sdmd_build_system): positions,
+ *                     velocities, cells, types, HB state, stored events (the
+ *                     engine's continue mode keeps them), cell list, clock and
+ *                     event counters; rand() restarts from the saved seed and the
+ *                     unsaved counters from zero, as ReadBreakPoint does.  names8
+ *                     (may be NULL) are the system's atom names, checked against
+ *                     the file's;
+ * sdmd_saved_write    writes a system's state in the file's layout, with the
+ *                     static records (atom properties, residue and peptide
+ *                     tables, the connection map's bond bits, parameters, seed)
+ *                     of a file read before -- the reference reads it back with
+ *                     ReadBreakPoint. */
+typedef struct sdmd_saved sdmd_saved;
+typedef struct sdmd_saved_header {
+    int32_t  atomnum, cellnum[3];
+    int64_t  frame;
+    double   timestep, currenttime, temperature, outputrate, box[3];
+    uint32_t seed;
+    int32_t  remd_flag;
+    double   remd_T;
+    char     method[20];
+} sdmd_saved_header;
+int  sdmd_saved_read(const char *path, sdmd_saved **out, char *errbuf, int errlen);
+int  sdmd_saved_info(const sdmd_saved *s, sdmd_saved_header *out);
+int  sdmd_saved_apply(const sdmd_saved *s, sdmd_system *sys, const char *names8, char *errbuf, int errlen);
+int  sdmd_saved_write(const char *path, const sdmd_saved *tpl, const sdmd_system *sys, char *errbuf, int errlen);
+void sdmd_saved_free(sdmd_saved *s);
+
 sdmd_system *sdmd_host_view(sdmd_host_system *h);
 void sdmd_host_free(sdmd_host_system *h);
 
