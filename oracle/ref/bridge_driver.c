@@ -4,7 +4,10 @@
  * (oracle/ref/Makefile).  It exposes the reference's own set-up and loop so a
  * test can hand state to the bridge and back:
  *
- *   bd_init(argc, argv)  InputData + Prepare()'s set-up (src/SGThread.c:21-46)
+ *   bd_init(argc, argv)  InputData + Prepare()'s set-up (src/SGThread.c:21-46);
+ *                        for a continue run (parameter.txt "continue") InputData
+ *                        reads savedData.dat with ReadBreakPoint
+ *   bd_save()            the reference's own checkpoint writer (SaveData(savedData))
  *   bd_sweep()           Predict over 1..N and CreateCBT (src/SGThread.c:47-62)
  *   bd_tree()            CreateCBT only (continue mode, src/SGThread.c:54-62)
  *   bd_run(n)            SingleThreadRun's loop (src/SGThread.c:75-151) for n
@@ -20,10 +23,10 @@ int sdmd_ref_rand(void) { return rand(); }
 
 int bd_init(int argc, const char **argv) {
     InputData(argc, argv);
-    if (strcmp("new", neworcontinue)) return 2;
     InitializeFiles(NULL, fileList);
     atomList.ptr = (struct AtomStr **)calloc(atomnum + 1, sizeof(struct AtomStr *));
     for (int i = 1; i <= atomnum; i++) atomList.ptr[i] = &atom[i];
+    if (strcmp("new", neworcontinue)) return strcmp("continue", neworcontinue) ? 2 : 0;
     SDEnergyMin(20000, &atomList);
     PBC("full", NULL, &atomList);
     LinkList("full", NULL, NULL, &atomList);
@@ -39,6 +42,8 @@ void bd_sweep(void) {
 }
 
 void bd_tree(void) { CreateCBT(); }
+
+void bd_save(void) { SaveData(savedData, fileList); }
 
 long bd_run(long n_events) {
     int renewList[256] = {0};

@@ -63,6 +63,8 @@ _Static_assert(sizeof(sv_pep) == 24, "PepStr layout");
 _Static_assert(sizeof(sv_remd) == 128, "REMDStr layout");
 _Static_assert(sizeof(long) == 8, "LP64");
 
+void sdmd_host_seed_rng(sdmd_rng *r, uint32_t seed);   /* sysbuild.c: srand(seed)'s stream */
+
 #define HB_CONNECT 0x04         /* connection-map bits (src/DMD.h:59-63) */
 #define NEIGHBOR_CONNECT 0x08
 
@@ -194,7 +196,7 @@ int sdmd_saved_apply(const sdmd_saved *sv, sdmd_system *s, const char *names8, c
     s->time = sv->currenttime;
     /* ReadBreakPoint restarts rand() from the saved seed (src/Initialization.c:472-473);
        the counters it does not store start again at zero */
-    sdmd_rng_seed(&s->rng, sv->seed);
+    sdmd_host_seed_rng(&s->rng, sv->seed);
     memset(&s->counters, 0, sizeof s->counters);
     s->counters.frame = sv->frame;
     s->counters.collision = sv->ev[0]; s->counters.hb = sv->ev[1]; s->counters.bond = sv->ev[2];

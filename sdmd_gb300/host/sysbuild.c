@@ -105,6 +105,8 @@ static void rng_seed(sdmd_rng *r, uint32_t seed) {
     r->front = 3; r->rear = 0;
     for (int k = 0; k < 310; k++) rng_next(r);
 }
+/* the seeded stream for the other host-side files (savedata.c) */
+__attribute__((visibility("hidden"))) void sdmd_host_seed_rng(sdmd_rng *r, uint32_t seed) { rng_seed(r, seed); }
 static int32_t rnd(B *b) { return rng_next(&b->rng); }
 static double random01(B *b) { return 0 + (double)rnd(b) / ((double)2147483647 / (1 - 0)); }
 /* Maxwell_Boltzmann_Distribution (src/ToolFunctions.c:544-569) with libm log,

@@ -110,7 +110,20 @@ def in_child(target, *args):
     q = ctx.Queue()
     p = ctx.Process(target=target, args=(*args, q))
     p.start()
-    out = q.get(timeout=600)
+    import queue
+    out = None
+    for _ in range(600):   # the reference exits the process on its own errors: notice that
+        try:
+            out = q.get(timeout=1)
+            break
+        except queue.Empty:
+            if not p.is_alive():
+                break
+    if out is None:
+        try:
+            out = q.get(timeout=2)
+        except queue.Empty:
+            out = ("error", f"child ended with exit code {p.exitcode} and no result")
     p.join(timeout=60)
     assert out[0] == "ok", out
     return out[1:]
