@@ -39,6 +39,9 @@ struct sdmd_gpu {
     void (*sweep_k)(const DSys *, int) = nullptr;            // plain FP64 or FP32-screened kernels
     void (*loop_k)(const DSys *, double, int) = nullptr;
     int helpers = 0;                               // helper blocks of the eager advance (0: none)
+    std::vector<int> pair_src;                     // system whose (identical) pair tables system k shares
+    size_t dyn_begin = 0, dyn_end = 0;             // the dynamic arrays' block in the arena
+    DScal *sc_all = nullptr;                       // the systems' scalar blocks, contiguous
     Adv *adv = nullptr;                            // their per-system protocol words (in the arena)
     double prep_ms = 0, run_ms = 0;
     // energies / replica exchange scratch (one block: num, T, E, kin, warn, stop, rng, stats)
@@ -222,7 +225,7 @@ constexpr int kSweepBlocksPerSM = 8;   // parallel sweep: blocks in flight per S
 
 // brackets of every FP64 threshold the prediction compares against, computed with
 // the same FP64 operations as the device (d + ZERO, d - ZERO, dmin - ZERO, dmax + ZERO)
-static void build_screen32(const sdmd_system &s, Screen32 &o) {
+static void build_screen32(const sdmd_system &s, Screen32 &o, bool with_pairs) {
     const size_t NT3 = (size_t)SDMD_NTABLES * SDMD_NTYPES * SDMD_NTYPES;
     auto entry = [](double dmin, double dmax, float *e) {
         f32_bracket(dmin - SDMD_ZERO, e + 0);
@@ -235,10 +238,12 @@ static void build_screen32(const sdmd_system &s, Screen32 &o) {
         f32_bracket(d - SDMD_ZERO, e + 2);
         f32_bracket(d, e + 4);
     };
-    o.pair_thr.assign(NT3 * 8, 0.f);
-    for (size_t k = 0; k < NT3; k++) entry(s.pair_dmin[k], s.pair_dmax[k], &o.pair_thr[8 * k]);
-    o.pair_step.assign(((size_t)s.n_pair_steps + 1) * 6, 0.f);
-    for (int k = 0; k < s.n_pair_steps; k++) step(s.pair_step_d[k], &o.pair_step[6 * (size_t)k]);
+    if (with_pairs) {
+        o.pair_thr.assign(NT3 * 8, 0.f);
+        for (size_t k = 0; k < NT3; k++) entry(s.pair_dmin[k], s.pair_dmax[k], &o.pair_thr[8 * k]);
+        o.pair_step.assign(((size_t)s.n_pair_steps + 1) * 6, 0.f);
+        for (int k = 0; k < s.n_pair_steps; k++) step(s.pair_step_d[k], &o.pair_step[6 * (size_t)k]);
+    }
     o.con_thr.assign(((size_t)s.n_cons + 1) * 8, 0.f);
     for (int k = 0; k < s.n_cons; k++) entry(s.con_dmin[k], s.con_dmax[k], &o.con_thr[8 * (size_t)k]);
     o.con_step.assign(((size_t)s.n_con_steps + 1) * 6, 0.f);
@@ -248,15 +253,17 @@ static void build_screen32(const sdmd_system &s, Screen32 &o) {
         f32_bracket(s.bond_dmin[k], &o.bond[4 * (size_t)k]);
         f32_bracket(s.bond_dmax[k], &o.bond[4 * (size_t)k + 2]);
     }
-    o.pair_key.assign(NT3 * 2, 0);
-    for (size_t k = 0; k < NT3; k++) {
-        o.pair_key[2 * k] = host_tkey(s.pair_dmin[k] - SDMD_ZERO);
-        o.pair_key[2 * k + 1] = host_tkey(s.pair_dmax[k] + SDMD_ZERO);
-    }
-    o.pair_stepkey.assign(((size_t)s.n_pair_steps + 1) * 2, 0);
-    for (int k = 0; k < s.n_pair_steps; k++) {
-        o.pair_stepkey[2 * (size_t)k] = host_tkey(s.pair_step_d[k] + SDMD_ZERO);
-        o.pair_stepkey[2 * (size_t)k + 1] = host_tkey(s.pair_step_d[k] - SDMD_ZERO);
+    if (with_pairs) {
+        o.pair_key.assign(NT3 * 2, 0);
+        for (size_t k = 0; k < NT3; k++) {
+            o.pair_key[2 * k] = host_tkey(s.pair_dmin[k] - SDMD_ZERO);
+            o.pair_key[2 * k + 1] = host_tkey(s.pair_dmax[k] + SDMD_ZERO);
+        }
+        o.pair_stepkey.assign(((size_t)s.n_pair_steps + 1) * 2, 0);
+        for (int k = 0; k < s.n_pair_steps; k++) {
+            o.pair_stepkey[2 * (size_t)k] = host_tkey(s.pair_step_d[k] + SDMD_ZERO);
+            o.pair_stepkey[2 * (size_t)k + 1] = host_tkey(s.pair_step_d[k] - SDMD_ZERO);
+        }
     }
     o.con_key.assign(((size_t)s.n_cons + 1) * 2, 0);
     for (int k = 0; k < s.n_cons; k++) {
@@ -273,8 +280,8 @@ static void build_screen32(const sdmd_system &s, Screen32 &o) {
     // RightPair: the first of (t1,t2), (t1',t2), (t1,t2'), (t1',t2') with dmin > 0, ' = AtomTypeChange(., 0)
     auto unhb = [](int t) { return t == 3 ? 1 : t == 4 ? 2 : t == 27 ? 26 : t; };
     auto idx0 = [](int a, int b) { return a * SDMD_NTYPES + b; };
-    o.rp_idx.assign((size_t)SDMD_NTYPES * SDMD_NTYPES, -1);
-    for (int t1 = 0; t1 < SDMD_NTYPES; t1++)
+    if (with_pairs) o.rp_idx.assign((size_t)SDMD_NTYPES * SDMD_NTYPES, -1);
+    for (int t1 = 0; with_pairs && t1 < SDMD_NTYPES; t1++)
         for (int t2 = 0; t2 < SDMD_NTYPES; t2++) {
             const int a = unhb(t1), b = unhb(t2);
             const int cand[4] = {idx0(t1, t2), idx0(a, t2), idx0(t1, b), idx0(a, b)};
@@ -324,16 +331,23 @@ template <class T> static void put(std::vector<std::pair<void *, std::pair<const
     if (count && src) cp.push_back({(void *)dst, {(const void *)src, count * sizeof(T)}});
 }
 
+// The arena holds, in this order: every system's static arrays (topology, tables
+// and the host-derived screen tables; identical pair tables are stored once and
+// shared), every system's dynamic arrays (the state sdmd_gpu_create uploads and
+// sdmd_gpu_download returns), then the per-system scalar blocks and the
+// device-only scratch.  Upload and download are then one copy each.
 static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
                      std::vector<std::pair<void *, std::pair<const void *, size_t>>> *copies,
                      const std::vector<Screen32> *s32 = nullptr) {
     Carver cv{base, 0};
     const int trace_cap = h->opts.trace_capacity > 0 ? h->opts.trace_capacity : 0;
+    const size_t NT3 = (size_t)SDMD_NTABLES * SDMD_NTYPES * SDMD_NTYPES;
+    // ---- static arrays ----
     for (int k = 0; k < h->n_systems; k++) {
         const sdmd_system &s = sys[k];
         const SysMeta &m = h->meta[k];
         DSys &d = h->hs[k];
-        size_t N1 = (size_t)m.n + 1, NT3 = (size_t)SDMD_NTABLES * SDMD_NTYPES * SDMD_NTYPES;
+        const size_t N1 = (size_t)m.n + 1;
         d.mass = cv.take<double>(N1);
         d.protein = cv.take<int32_t>(N1); d.aanum = cv.take<int32_t>(N1); d.aatype = cv.take<int32_t>(N1);
         d.hb_neighbor = cv.take<int32_t>(N1); d.hb_role = cv.take<int32_t>(N1); d.name_code = cv.take<int32_t>(N1);
@@ -346,69 +360,51 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
         d.con_step_acc = cv.take<double>(m.n_con_steps + 1);
         d.conn_off = cv.take<int32_t>(N1 + 1); d.conn_j = cv.take<int32_t>(m.n_conn + 1);
         d.conn_bits = cv.take<int32_t>(m.n_conn + 1);
-        d.pair_dmin = cv.take<double>(NT3); d.pair_dmax = cv.take<double>(NT3);
-        d.pair_step_off = cv.take<int32_t>(NT3); d.pair_step_n = cv.take<int32_t>(NT3);
-        d.pair_step_d = cv.take<double>(m.n_pair_steps + 1); d.pair_step_e = cv.take<double>(m.n_pair_steps + 1);
-        d.pair_step_acc = cv.take<double>(m.n_pair_steps + 1);
-        d.x = cv.take<double>(N1); d.y = cv.take<double>(N1); d.z = cv.take<double>(N1);
-        d.vx = cv.take<double>(N1); d.vy = cv.take<double>(N1); d.vz = cv.take<double>(N1);
-        d.cx = cv.take<int32_t>(N1); d.cy = cv.take<int32_t>(N1); d.cz = cv.take<int32_t>(N1);
-        d.type = cv.take<int32_t>(N1); d.hb_bond = cv.take<int32_t>(N1); d.hb_itype = cv.take<int32_t>(N1);
-        d.nb_partner = cv.take<int32_t>(4 * N1); d.nb_status = cv.take<int32_t>(N1); d.nb_pnum = cv.take<int32_t>(N1);
-        d.ev_time = cv.take<double>(N1); d.ev_partner = cv.take<int32_t>(N1);
-        d.ev_counter = cv.take<int64_t>(N1); d.ev_pcounter = cv.take<int64_t>(N1);
-        d.ev_potential = cv.take<double>(N1); d.ev_type = cv.take<int32_t>(N1); d.ev_sub = cv.take<int32_t>(N1);
-        d.cell_list = cv.take<int32_t>(N1 + m.ncell);
-        d.cbt_node = cv.take<int32_t>(2 * N1 + 2); d.cbt_leaf = cv.take<int32_t>(N1 + 1);
-        d.sc = cv.take<DScal>(1);
-        d.trace = cv.take<sdmd_trace_rec>(trace_cap > 0 ? trace_cap : 1);
-        d.trace_cap = trace_cap;
-        d.smp_cap = s.thermostat ? h->smp_cap_of[k] : 0;
-        size_t sc_ = d.smp_cap > 0 ? (size_t)d.smp_cap : 1;
-        d.smp = cv.take<double>(sc_);
-        d.smp_raw = cv.take<int32_t>(3 * sc_);
-        d.smp_cum = cv.take<int64_t>(sc_);
-        d.tloc = cv.take<double>(N1);
-        d.lazy = h->opts.advance == SDMD_ADVANCE_LAZY ? 1 : 0;
-        d.pair_thr32 = cv.take<float>(NT3 * 8);
-        d.pair_step32 = cv.take<float>(((size_t)m.n_pair_steps + 1) * 6);
+        const int src = h->pair_src[k];
+        const bool own_pairs = src == k;
+        if (own_pairs) {
+            d.pair_dmin = cv.take<double>(NT3); d.pair_dmax = cv.take<double>(NT3);
+            d.pair_step_off = cv.take<int32_t>(NT3); d.pair_step_n = cv.take<int32_t>(NT3);
+            d.pair_step_d = cv.take<double>(m.n_pair_steps + 1); d.pair_step_e = cv.take<double>(m.n_pair_steps + 1);
+            d.pair_step_acc = cv.take<double>(m.n_pair_steps + 1);
+            d.pair_thr32 = cv.take<float>(NT3 * 8);
+            d.pair_step32 = cv.take<float>(((size_t)m.n_pair_steps + 1) * 6);
+            d.pair_key = cv.take<long long>(NT3 * 2);
+            d.pair_stepkey = cv.take<long long>(((size_t)m.n_pair_steps + 1) * 2);
+            d.rp_idx = cv.take<int16_t>((size_t)SDMD_NTYPES * SDMD_NTYPES);
+        } else {   // the same tables as system src: share its device copies
+            const DSys &o = h->hs[src];
+            d.pair_dmin = o.pair_dmin; d.pair_dmax = o.pair_dmax;
+            d.pair_step_off = o.pair_step_off; d.pair_step_n = o.pair_step_n;
+            d.pair_step_d = o.pair_step_d; d.pair_step_e = o.pair_step_e; d.pair_step_acc = o.pair_step_acc;
+            d.pair_thr32 = o.pair_thr32; d.pair_step32 = o.pair_step32;
+            d.pair_key = o.pair_key; d.pair_stepkey = o.pair_stepkey; d.rp_idx = o.rp_idx;
+        }
         d.con_thr32 = cv.take<float>(((size_t)m.n_cons + 1) * 8);
         d.con_step32 = cv.take<float>(((size_t)m.n_con_steps + 1) * 6);
         d.bond32 = cv.take<float>(((size_t)m.n_bonds + 1) * 4);
-        d.pair_key = cv.take<long long>(NT3 * 2);
-        d.pair_stepkey = cv.take<long long>(((size_t)m.n_pair_steps + 1) * 2);
         d.con_key = cv.take<long long>(((size_t)m.n_cons + 1) * 2);
         d.con_stepkey = cv.take<long long>(((size_t)m.n_con_steps + 1) * 2);
         d.conn_win = cv.take<int32_t>(N1 * kConnWin);
         d.cbt_leaf0 = cv.take<int32_t>(N1 + 1);
-        d.rp_idx = cv.take<int16_t>((size_t)SDMD_NTYPES * SDMD_NTYPES);
         d.con_win = cv.take<int8_t>(N1 * 128);
         d.con_ok = cv.take<int8_t>(N1);
-        if (h->opts.screen == SDMD_SCREEN_FP32) {
-            d.sw_hbit = cv.take<int32_t>(N1);
-            d.sw_flag = cv.take<int32_t>(N1);
-            d.sw_warn = cv.take<int32_t>(N1);
-            // the records pack a cell index in 10 bits per axis
-            d.shr = s.cellnum[0] <= 1024 && s.cellnum[1] <= 1024 && s.cellnum[2] <= 1024 ? cv.take<float4>(N1 * 4)
-                                                                                        : nullptr;
-            d.maxc = std::min<int32_t>(kMaxPerCell, m.n);
-            d.cell_cnt = cv.take<int32_t>((size_t)m.ncell + 1);
-            d.cell_arr = cv.take<int32_t>(((size_t)m.ncell + 1) * d.maxc);
-        }
         if (copies && s32) {
             const Screen32 &q = (*s32)[k];
-            put(*copies, (float *)d.pair_thr32, q.pair_thr.data(), q.pair_thr.size());
-            put(*copies, (float *)d.pair_step32, q.pair_step.data(), q.pair_step.size());
+            if (own_pairs) {
+                put(*copies, (float *)d.pair_thr32, q.pair_thr.data(), q.pair_thr.size());
+                put(*copies, (float *)d.pair_step32, q.pair_step.data(), q.pair_step.size());
+                put(*copies, (long long *)d.pair_key, q.pair_key.data(), q.pair_key.size());
+                put(*copies, (long long *)d.pair_stepkey, q.pair_stepkey.data(), q.pair_stepkey.size());
+                put(*copies, (int16_t *)d.rp_idx, q.rp_idx.data(), q.rp_idx.size());
+            }
             put(*copies, (float *)d.con_thr32, q.con_thr.data(), q.con_thr.size());
             put(*copies, (float *)d.con_step32, q.con_step.data(), q.con_step.size());
             put(*copies, (float *)d.bond32, q.bond.data(), q.bond.size());
-            put(*copies, (long long *)d.pair_key, q.pair_key.data(), q.pair_key.size());
-            put(*copies, (long long *)d.pair_stepkey, q.pair_stepkey.data(), q.pair_stepkey.size());
             put(*copies, (long long *)d.con_key, q.con_key.data(), q.con_key.size());
             put(*copies, (long long *)d.con_stepkey, q.con_stepkey.data(), q.con_stepkey.size());
             put(*copies, (int32_t *)d.conn_win, q.conn_win.data(), q.conn_win.size());
             put(*copies, (int32_t *)d.cbt_leaf0, q.leaf0.data(), q.leaf0.size());
-            put(*copies, (int16_t *)d.rp_idx, q.rp_idx.data(), q.rp_idx.size());
             put(*copies, (int8_t *)d.con_win, q.con_win.data(), q.con_win.size());
             put(*copies, (int8_t *)d.con_ok, q.con_ok.data(), q.con_ok.size());
         }
@@ -431,12 +427,63 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             put(c, (double *)d.con_step_acc, s.con_step_acc, (size_t)m.n_con_steps);
             put(c, (int32_t *)d.conn_off, s.conn_off, N1 + 1); put(c, (int32_t *)d.conn_j, s.conn_j, (size_t)m.n_conn);
             put(c, (int32_t *)d.conn_bits, s.conn_bits, (size_t)m.n_conn);
-            put(c, (double *)d.pair_dmin, s.pair_dmin, NT3); put(c, (double *)d.pair_dmax, s.pair_dmax, NT3);
-            put(c, (int32_t *)d.pair_step_off, s.pair_step_off, NT3);
-            put(c, (int32_t *)d.pair_step_n, s.pair_step_n, NT3);
-            put(c, (double *)d.pair_step_d, s.pair_step_d, (size_t)m.n_pair_steps);
-            put(c, (double *)d.pair_step_e, s.pair_step_e, (size_t)m.n_pair_steps);
-            put(c, (double *)d.pair_step_acc, s.pair_step_acc, (size_t)m.n_pair_steps);
+            if (own_pairs) {
+                put(c, (double *)d.pair_dmin, s.pair_dmin, NT3); put(c, (double *)d.pair_dmax, s.pair_dmax, NT3);
+                put(c, (int32_t *)d.pair_step_off, s.pair_step_off, NT3);
+                put(c, (int32_t *)d.pair_step_n, s.pair_step_n, NT3);
+                put(c, (double *)d.pair_step_d, s.pair_step_d, (size_t)m.n_pair_steps);
+                put(c, (double *)d.pair_step_e, s.pair_step_e, (size_t)m.n_pair_steps);
+                put(c, (double *)d.pair_step_acc, s.pair_step_acc, (size_t)m.n_pair_steps);
+            }
+        }
+    }
+    // ---- dynamic arrays: one contiguous block for all systems ----
+    cv.off = (cv.off + 255) & ~size_t(255);
+    h->dyn_begin = cv.off;
+    for (int k = 0; k < h->n_systems; k++) {
+        const SysMeta &m = h->meta[k];
+        DSys &d = h->hs[k];
+        const size_t N1 = (size_t)m.n + 1;
+        d.x = cv.take<double>(N1); d.y = cv.take<double>(N1); d.z = cv.take<double>(N1);
+        d.vx = cv.take<double>(N1); d.vy = cv.take<double>(N1); d.vz = cv.take<double>(N1);
+        d.cx = cv.take<int32_t>(N1); d.cy = cv.take<int32_t>(N1); d.cz = cv.take<int32_t>(N1);
+        d.type = cv.take<int32_t>(N1); d.hb_bond = cv.take<int32_t>(N1); d.hb_itype = cv.take<int32_t>(N1);
+        d.nb_partner = cv.take<int32_t>(4 * N1); d.nb_status = cv.take<int32_t>(N1); d.nb_pnum = cv.take<int32_t>(N1);
+        d.ev_time = cv.take<double>(N1); d.ev_partner = cv.take<int32_t>(N1);
+        d.ev_counter = cv.take<int64_t>(N1); d.ev_pcounter = cv.take<int64_t>(N1);
+        d.ev_potential = cv.take<double>(N1); d.ev_type = cv.take<int32_t>(N1); d.ev_sub = cv.take<int32_t>(N1);
+        d.cell_list = cv.take<int32_t>(N1 + m.ncell);
+    }
+    h->dyn_end = cv.off;
+    // ---- scalar blocks of all systems (one copy each way), then device-only scratch ----
+    DScal *scs = cv.take<DScal>((size_t)h->n_systems);
+    h->sc_all = scs;
+    for (int k = 0; k < h->n_systems; k++) h->hs[k].sc = scs + k;
+    for (int k = 0; k < h->n_systems; k++) {
+        const sdmd_system &s = sys[k];
+        const SysMeta &m = h->meta[k];
+        DSys &d = h->hs[k];
+        const size_t N1 = (size_t)m.n + 1;
+        d.cbt_node = cv.take<int32_t>(2 * N1 + 2); d.cbt_leaf = cv.take<int32_t>(N1 + 1);
+        d.trace = cv.take<sdmd_trace_rec>(trace_cap > 0 ? trace_cap : 1);
+        d.trace_cap = trace_cap;
+        d.smp_cap = s.thermostat ? h->smp_cap_of[k] : 0;
+        size_t sc_ = d.smp_cap > 0 ? (size_t)d.smp_cap : 1;
+        d.smp = cv.take<double>(sc_);
+        d.smp_raw = cv.take<int32_t>(3 * sc_);
+        d.smp_cum = cv.take<int64_t>(sc_);
+        d.tloc = cv.take<double>(N1);
+        d.lazy = h->opts.advance == SDMD_ADVANCE_LAZY ? 1 : 0;
+        if (h->opts.screen == SDMD_SCREEN_FP32) {
+            d.sw_hbit = cv.take<int32_t>(N1);
+            d.sw_flag = cv.take<int32_t>(N1);
+            d.sw_warn = cv.take<int32_t>(N1);
+            // the records pack a cell index in 10 bits per axis
+            d.shr = s.cellnum[0] <= 1024 && s.cellnum[1] <= 1024 && s.cellnum[2] <= 1024 ? cv.take<float4>(N1 * 4)
+                                                                                        : nullptr;
+            d.maxc = std::min<int32_t>(kMaxPerCell, m.n);
+            d.cell_cnt = cv.take<int32_t>((size_t)m.ncell + 1);
+            d.cell_arr = cv.take<int32_t>(((size_t)m.ncell + 1) * d.maxc);
         }
     }
     // the helper protocol words of every system, contiguous (cleared before each launch)
@@ -558,6 +605,26 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     h->threads = h->opts.threads_per_system > 0 ? h->opts.threads_per_system : 128;
     if (h->threads < 32 || h->threads > 1024 || (h->threads & 31)) { delete h; return SDMD_EINVAL; }
     if (h->smem > 227 * 1024) { delete h; return SDMD_ECAPACITY; }
+    // systems whose pair tables are identical (the same force field) share one device copy
+    h->pair_src.assign(n_systems, 0);
+    {
+        std::vector<int> distinct;
+        auto same = [](const sdmd_system &a, const sdmd_system &b) {
+            const size_t NT3 = (size_t)SDMD_NTABLES * SDMD_NTYPES * SDMD_NTYPES, ns = (size_t)a.n_pair_steps;
+            if (a.n_pair_steps != b.n_pair_steps) return false;
+            auto eq = [](const void *x, const void *y, size_t bytes) { return x == y || !memcmp(x, y, bytes); };
+            return eq(a.pair_dmin, b.pair_dmin, NT3 * 8) && eq(a.pair_dmax, b.pair_dmax, NT3 * 8) &&
+                   eq(a.pair_step_off, b.pair_step_off, NT3 * 4) && eq(a.pair_step_n, b.pair_step_n, NT3 * 4) &&
+                   eq(a.pair_step_d, b.pair_step_d, ns * 8) && eq(a.pair_step_e, b.pair_step_e, ns * 8) &&
+                   eq(a.pair_step_acc, b.pair_step_acc, ns * 8);
+        };
+        for (int k = 0; k < n_systems; k++) {
+            h->pair_src[k] = k;
+            for (int j : distinct)
+                if (same(systems[j], systems[k])) { h->pair_src[k] = j; break; }
+            if (h->pair_src[k] == k && distinct.size() < 16) distinct.push_back(k);
+        }
+    }
     h->arena_bytes = layout(h, systems, nullptr, nullptr) + 256;
     if ((r = cuda_fail(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->opts.device))) ||
         (r = cuda_fail(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking))) ||
@@ -580,19 +647,23 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     h->esmem = energy_smem_bytes(nbcap_max);
     std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
     std::vector<Screen32> s32(n_systems);
-    for (int k = 0; k < n_systems; k++) build_screen32(systems[k], s32[k]);
+    for (int k = 0; k < n_systems; k++) build_screen32(systems[k], s32[k], h->pair_src[k] == k);
     layout(h, systems, h->arena, &copies, &s32);
-    for (auto &c : copies) cudaMemcpyAsync(c.first, c.second.first, c.second.second, cudaMemcpyHostToDevice, h->stream);
+    // one staging image of the static and dynamic blocks, one copy to the device
+    std::vector<unsigned char> staging(h->dyn_end);
+    for (auto &c : copies)
+        memcpy(staging.data() + ((unsigned char *)c.first - h->arena), c.second.first, c.second.second);
     std::vector<DScal> sc(n_systems);
     for (int k = 0; k < n_systems; k++) {
         const sdmd_system &s = systems[k];
         for_dynamic(h, k, s, [&](void *dv, void *hp, size_t bytes) {
-            cudaMemcpyAsync(dv, hp, bytes, cudaMemcpyHostToDevice, h->stream);
+            memcpy(staging.data() + ((unsigned char *)dv - h->arena), hp, bytes);
         });
         memset(&sc[k], 0, sizeof(DScal));
         sc[k].time = s.time; sc[k].rng = s.rng; sc[k].c = s.counters;
-        cudaMemcpyAsync(h->hs[k].sc, &sc[k], sizeof(DScal), cudaMemcpyHostToDevice, h->stream);
     }
+    cudaMemcpyAsync(h->arena, staging.data(), h->dyn_end, cudaMemcpyHostToDevice, h->stream);
+    cudaMemcpyAsync(h->sc_all, sc.data(), sizeof(DScal) * n_systems, cudaMemcpyHostToDevice, h->stream);
     cudaMemcpyAsync(h->ds, h->hs.data(), sizeof(DSys) * n_systems, cudaMemcpyHostToDevice, h->stream);
     // the dynamic shared-memory limit must cover dynamic + static usage: always set it
     if ((r = cuda_fail(cudaFuncSetAttribute(h->sweep_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -654,8 +725,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
 // copy every system's scalar block back and report the first device error
 static int collect_errors(sdmd_gpu *h) {
     std::vector<DScal> sc(h->n_systems);
-    for (int k = 0; k < h->n_systems; k++)
-        CK(cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(sc.data(), h->sc_all, sizeof(DScal) * h->n_systems, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     for (int k = 0; k < h->n_systems; k++) {
         if (sc[k].err) {
@@ -758,8 +828,7 @@ static int run_rounds(sdmd_gpu *h, int64_t want, double t_end) {
         CK(cudaGetLastError());
         h->launches += 4;
         h->loop_launches += 1;
-        for (int k = 0; k < h->n_systems; k++)
-            CK(cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(sc.data(), h->sc_all, sizeof(DScal) * h->n_systems, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
         float lms = 0;
         cudaEventElapsedTime(&lms, h->l0, h->l1);
@@ -775,13 +844,12 @@ extern "C" int sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_sy
     if (!h || !systems || n_systems != h->n_systems) return SDMD_EINVAL;
     CK(cudaSetDevice(h->opts.device));
     std::vector<DScal> sc(n_systems);
-    for (int k = 0; k < n_systems; k++) {
+    for (int k = 0; k < n_systems; k++)
         if (systems[k].n_atoms != h->meta[k].n) return SDMD_EINVAL;
-        for_dynamic(h, k, systems[k], [&](void *dv, void *hp, size_t bytes) {
-            cudaMemcpyAsync(hp, dv, bytes, cudaMemcpyDeviceToHost, h->stream);
-        });
-        cudaMemcpyAsync(&sc[k], h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost, h->stream);
-    }
+    // the dynamic block of every system in one copy, then scattered into the caller's arrays
+    std::vector<unsigned char> dyn(h->dyn_end - h->dyn_begin);
+    CK(cudaMemcpyAsync(dyn.data(), h->arena + h->dyn_begin, dyn.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(sc.data(), h->sc_all, sizeof(DScal) * n_systems, cudaMemcpyDeviceToHost, h->stream));
     std::vector<std::vector<double>> tl(n_systems);
     if (h->opts.advance == SDMD_ADVANCE_LAZY)
         for (int k = 0; k < n_systems; k++) {
@@ -789,6 +857,10 @@ extern "C" int sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_sy
             cudaMemcpyAsync(tl[k].data(), h->hs[k].tloc, tl[k].size() * 8, cudaMemcpyDeviceToHost, h->stream);
         }
     CK(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < n_systems; k++)
+        for_dynamic(h, k, systems[k], [&](void *dv, void *hp, size_t bytes) {
+            memcpy(hp, dyn.data() + ((unsigned char *)dv - (h->arena + h->dyn_begin)), bytes);
+        });
     for (int k = 0; k < n_systems; k++) {
         sdmd_system &s = systems[k];
         s.time = sc[k].time;
@@ -851,12 +923,12 @@ extern "C" int sdmd_gpu_run_remd(sdmd_gpu *h, int64_t n_exchanges, double t_end,
     CK(cudaSetDevice(h->opts.device));
     const int n = h->n_systems;
     std::vector<double> rate(n, 0);
+    std::vector<DScal> scs(n);
     if (!(x->every_events > 0)) {   // REMDRun: rate = ((int)(currenttime / outputRate) + 1) * outputRate
-        for (int k = 0; k < n; k++) {
-            DScal c;
-            CK(cudaMemcpy(&c, h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost));
-            rate[k] = (double)((long long)(c.time / x->every_time) + 1) * x->every_time;
-        }
+        CK(cudaMemcpyAsync(scs.data(), h->sc_all, sizeof(DScal) * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        for (int k = 0; k < n; k++)
+            rate[k] = (double)((long long)(scs[k].time / x->every_time) + 1) * x->every_time;
     }
     int64_t stats[2] = {x->attempted, x->accepted};
     CK(cudaMemcpyAsync(h->x_num, x->num, sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream));
@@ -878,11 +950,10 @@ extern "C" int sdmd_gpu_run_remd(sdmd_gpu *h, int64_t n_exchanges, double t_end,
         if ((r = collect_errors(h))) return r;
         // every replica must have reached its exchange point (not the end of the run)
         bool reached = true;
-        for (int k = 0; k < n; k++) {
-            DScal c;
-            CK(cudaMemcpy(&c, h->hs[k].sc, sizeof(DScal), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpyAsync(scs.data(), h->sc_all, sizeof(DScal) * n, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        for (const DScal &c : scs)
             if (x->every_events > 0 ? c.c.frame < c.target_frame : !c.at_stop) reached = false;
-        }
         if (!reached) break;
         energy_kernel<<<n, 32, h->esmem, h->stream>>>(h->ds, h->x_E, h->x_kin, h->x_warn);
         remd_exchange_kernel<<<1, 1, 0, h->stream>>>(h->ds, n, h->x_num, h->x_T, h->x_E, h->x_warn, h->x_rng,
