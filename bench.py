@@ -249,6 +249,8 @@ def run_ours(args, D):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")   # > 129 MB L2
 
     systems = build_workload(args.workload, D.rank)
+    if args.systems:   # the first K systems of the batch (small profiling cases)
+        systems = systems[:args.systems]
     cfg = run_config(args, systems, D.world)
     E = args.events_per_step
     adv = ADVANCE_LAZY if args.advance == "lazy" else ADVANCE_EAGER
@@ -501,6 +503,8 @@ def run_reference(args, D):
     B.build_host()
     import multiprocessing as mp
     systems = build_workload(args.workload, 0)   # built (and cached) once, before the workers load it
+    if args.systems:
+        systems = systems[:args.systems]
     cfg = run_config(args, systems, 1)
     if args.workload == "c3":
         cfg["reference_note"] = "exchange rounds not replayed: the replicas run E events per step"
@@ -557,6 +561,7 @@ def main():
     ap.add_argument("--workload", default="c4", choices=sorted(WORKLOADS))
     ap.add_argument("--events-per-step", type=int, default=None, help="executed events per system per step")
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--systems", type=int, default=0, help="run only the first K systems of the batch")
     ap.add_argument("--advance", choices=["eager", "lazy"], default="eager")
     ap.add_argument("--screen", choices=["fp32", "fp64"], default="fp32")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
