@@ -143,6 +143,8 @@ WORKLOADS = {
           "1e4 events per replica",
     "c4": "C4: 512 single random-sequence chains of 5-60 residues, box edge 40 A * (N/59)^(1/3) (floor 27 A), "
           "Andersen NVT 280-400 K",
+    "c5": "C5: 8 replicas of 400 random-sequence 10-mers (~42k atoms) in a smooth cylindrical wall of radius "
+          "60 A with a 120 A periodic axis (compressed rigid-chain packing), Andersen NVT 310 K",
 }
 
 
@@ -151,7 +153,8 @@ def build_workload(name, rank):
     if name not in WORKLOADS:
         raise SystemExit(f"unknown workload {name}")
     make = {"c1": lambda: [W.c1(seed=1 + rank)], "c2": lambda: [W.c2(seed=1 + rank)],
-            "c3": lambda: W.c3(seed=1 + rank), "c4": lambda: W.c4(seed=1 + rank)}[name]
+            "c3": lambda: W.c3(seed=1 + rank), "c4": lambda: W.c4(seed=1 + rank),
+            "c5": lambda: W.c5(seed=1 + rank)}[name]
     return make()
 
 

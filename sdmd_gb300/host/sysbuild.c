@@ -1136,44 +1136,6 @@ static double dist3(const double *a, const double *c) {
     return sqrt(d0 * d0 + d1 * d1 + d2 * d2);
 }
 
-/* push/pull the pair (i, j) toward distance `target` */
-static void move_pair(double *pi, double *pj, double target, double w) {
-    double d[3] = {pj[0] - pi[0], pj[1] - pi[1], pj[2] - pi[2]};
-    double l = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    if (l < 1e-9) { d[0] = 1e-3; d[1] = 0.7e-3; d[2] = 0.3e-3; l = sqrt(1e-6 + 0.49e-6 + 0.09e-6); }
-    double f = w * 0.5 * (l - target) / l;
-    for (int k = 0; k < 3; k++) { pi[k] += f * d[k]; pj[k] -= f * d[k]; }
-}
-
-/* largest violation of the model's real bounds (with the 1e-4 A text margin) */
-static double chain_violation(B *b) {
-    int N = b->n;
-    double worst = 0;
-    for (int i = 1; i <= N; i++) {
-        hatom *a = &b->atom[i];
-        for (int q = 0; q < a->nbond; q++) {
-            double lo = sqrt(a->bond[q].dmin), hi = sqrt(a->bond[q].dmax), d = dist3(a->pos, b->atom[a->bond[q].j].pos);
-            double v = d < lo + 0.0004 ? lo + 0.0004 - d : (d > hi - 0.0004 ? d - hi + 0.0004 : 0);
-            if (v > worst) worst = v;
-        }
-        for (int q = 0; q < a->ncon; q++) {
-            double lo = sqrt(a->con[q].dmin), hi = sqrt(a->con[q].dmax), d = dist3(a->pos, b->atom[a->con[q].j].pos);
-            double v = d < lo + 0.0004 ? lo + 0.0004 - d : (d > hi - 0.0004 ? d - hi + 0.0004 : 0);
-            if (v > worst) worst = v;
-        }
-        for (int j = i + 1; j <= N; j++) {
-            int bits = conn_get(&b->atom[i], j) | conn_get(&b->atom[j], i);
-            if (bits & (BOND_C | CONSTR_C)) continue;
-            int t1 = b->atom[i].type, t2 = b->atom[j].type;
-            if (t1 > t2) { int z = t1; t1 = t2; t2 = z; }
-            double dmin = sqrt(b->coll[t1][t2].dmin);
-            double d = dist3(b->atom[i].pos, b->atom[j].pos);
-            if (dmin > 0 && dmin + 0.002 - d > worst) worst = dmin + 0.002 - d;
-        }
-    }
-    return worst;
-}
-
 static void move4(double *pi, double *pj, double target, double w) {
     double d[4] = {pj[0] - pi[0], pj[1] - pi[1], pj[2] - pi[2], pj[3] - pi[3]};
     double l = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + d[3] * d[3]);
@@ -1490,6 +1452,244 @@ static void *gen_worker(void *arg) {
     return NULL;
 }
 
+/* ---- compressive packing of a dense cylinder ------------------------------------
+ * The chains of a dense confined workload are placed overlap-free in a longer
+ * cylinder (axis x, periodic; radius D/2 about y = z = D/2), then the axis
+ * shrinks to its target length by at most 1 % a step, each chain's centre moving
+ * with it.  After each step the chains, kept rigid, are pushed apart: every pair
+ * of atoms of two chains closer than its hard-core distance (plus a margin), and
+ * every atom past the wall margin, gives its chain a push and a turn, and the
+ * pushes repeat until no such contact is left.  Each chain keeps the geometry it
+ * was built with. */
+typedef struct { double c[3], R[9], body_r2; int a0, a1; } rchain;
+
+static void rot_apply(const double *R, const double *v, double *o) {
+    for (int k = 0; k < 3; k++) o[k] = R[3 * k] * v[0] + R[3 * k + 1] * v[1] + R[3 * k + 2] * v[2];
+}
+
+/* R <- (rotation by the small vector w) * R, re-orthonormalised */
+static void rot_turn(double *R, const double *w) {
+    const double th = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+    if (th < 1e-15) return;
+    const double k[3] = {w[0] / th, w[1] / th, w[2] / th}, c = cos(th), s = sin(th), t = 1 - c;
+    const double Q[9] = {t * k[0] * k[0] + c, t * k[0] * k[1] - s * k[2], t * k[0] * k[2] + s * k[1],
+                         t * k[0] * k[1] + s * k[2], t * k[1] * k[1] + c, t * k[1] * k[2] - s * k[0],
+                         t * k[0] * k[2] - s * k[1], t * k[1] * k[2] + s * k[0], t * k[2] * k[2] + c};
+    double M[9];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) M[3 * i + j] = Q[3 * i] * R[j] + Q[3 * i + 1] * R[3 + j] + Q[3 * i + 2] * R[6 + j];
+    memcpy(R, M, sizeof M);
+}
+
+/* one round of pushes, shared by the host threads: each takes a fixed range of
+   atoms and sums its pushes into its own accumulators, which are added in thread
+   order, so the result does not depend on scheduling */
+typedef struct {
+    B *b; const int *owner, *head, *next, *cell; double L, D, margin, cs;
+    int i0, i1, nch; double (*acc)[7]; const rchain *ch; long contacts;
+} pushjob;
+
+static void *push_range(void *arg) {
+    pushjob *J = arg;
+    B *b = J->b;
+    const double L = J->L, D = J->D, cs = J->cs;
+    const int gx = (int)(L / cs), gy = (int)(D / cs) + 1;
+    const double rw = D / 2 - J->margin;
+    const rchain *ch = J->ch;
+    double (*acc)[7] = J->acc;
+    long contacts = 0;
+    for (int i = J->i0; i < J->i1; i++) {
+        hatom *a = &b->atom[i];
+        const int ki = J->owner[i];
+        const int c0 = J->cell[i] % gx, c1 = (J->cell[i] / gx) % gy, c2 = J->cell[i] / (gx * gy);
+        for (int dz = -1; dz <= 1; dz++) for (int dy = -1; dy <= 1; dy++) for (int dx = -1; dx <= 1; dx++) {
+            const int y = c1 + dy, z = c2 + dz;
+            if (y < 0 || z < 0 || y >= gy || z >= gy) continue;
+            const int x = (c0 + dx + gx) % gx;
+            for (int j = J->head[(z * gy + y) * gx + x]; j; j = J->next[j]) {
+                if (j <= i || J->owner[j] == ki) continue;
+                hatom *o = &b->atom[j];
+                int t1 = a->type, t2 = o->type;
+                if (t1 > t2) { int t = t1; t1 = t2; t2 = t; }
+                const double dmin2 = b->coll[t1][t2].dmin;
+                if (dmin2 <= 0) continue;
+                double v[3] = {o->pos[0] - a->pos[0], o->pos[1] - a->pos[1], o->pos[2] - a->pos[2]};
+                v[0] -= L * floor(v[0] / L + 0.5);
+                const double d2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2], dmin = sqrt(dmin2);
+                if (d2 >= (dmin + 0.01) * (dmin + 0.01)) continue;
+                contacts++;
+                const double d = sqrt(d2) > 1e-9 ? sqrt(d2) : 1e-9, f = 0.5 * (dmin + 0.03 - d) / d;
+                const double p[3] = {v[0] * f, v[1] * f, v[2] * f};   /* j's push; i gets -p */
+                const int kj = J->owner[j];
+                for (int side = 0; side < 2; side++) {
+                    const int k = side ? kj : ki;
+                    const double sg = side ? 1.0 : -1.0;
+                    const double *q = side ? o->pos : a->pos;
+                    double r[3] = {q[0] - ch[k].c[0], q[1] - ch[k].c[1], q[2] - ch[k].c[2]};
+                    r[0] -= L * floor(r[0] / L + 0.5);
+                    acc[k][0] += sg * p[0]; acc[k][1] += sg * p[1]; acc[k][2] += sg * p[2];
+                    acc[k][3] += sg * (r[1] * p[2] - r[2] * p[1]);
+                    acc[k][4] += sg * (r[2] * p[0] - r[0] * p[2]);
+                    acc[k][5] += sg * (r[0] * p[1] - r[1] * p[0]);
+                    acc[k][6] += 1;
+                }
+            }
+        }
+        const double ry = a->pos[1] - D / 2, rz = a->pos[2] - D / 2, rr = sqrt(ry * ry + rz * rz);
+        if (rr > rw - 0.005) {   /* the wall pushes the chain inward */
+            contacts++;
+            const double f = (rw - 0.02 - rr) / rr, p[3] = {0, ry * f, rz * f};
+            double r[3] = {a->pos[0] - ch[ki].c[0], a->pos[1] - ch[ki].c[1], a->pos[2] - ch[ki].c[2]};
+            r[0] -= L * floor(r[0] / L + 0.5);
+            acc[ki][1] += p[1]; acc[ki][2] += p[2];
+            acc[ki][3] += r[1] * p[2] - r[2] * p[1];
+            acc[ki][4] += r[2] * p[0] - r[0] * p[2];
+            acc[ki][5] += r[0] * p[1] - r[1] * p[0];
+            acc[ki][6] += 1;
+        }
+    }
+    J->contacts = contacts;
+    return NULL;
+}
+
+static long push_round(B *b, rchain *ch, int nch, const double *body, int *owner, double L, double D, double margin,
+                       double cs, int *head, int *next, int *cell, double (*acc)[7], int nthr) {
+    const int N = b->n;
+    for (int k = 0; k < nch; k++)   /* atom positions from the chains' rigid motions */
+        for (int i = ch[k].a0; i <= ch[k].a1; i++) {
+            double *p = b->atom[i].pos;
+            rot_apply(ch[k].R, body + 3 * i, p);
+            for (int q = 0; q < 3; q++) p[q] += ch[k].c[q];
+        }
+    const int gx = (int)(L / cs), gy = (int)(D / cs) + 1;
+    const double cx = L / gx;
+    for (long g = 0; g < (long)gx * gy * gy; g++) head[g] = 0;
+    for (int i = N; i >= 1; i--) {
+        double *p = b->atom[i].pos;
+        p[0] -= L * floor(p[0] / L);
+        int c0 = (int)(p[0] / cx), c1 = (int)(p[1] / cs), c2 = (int)(p[2] / cs);
+        c0 = c0 < 0 ? 0 : (c0 >= gx ? gx - 1 : c0);
+        c1 = c1 < 0 ? 0 : (c1 >= gy ? gy - 1 : c1);
+        c2 = c2 < 0 ? 0 : (c2 >= gy ? gy - 1 : c2);
+        cell[i] = (c2 * gy + c1) * gx + c0;
+        next[i] = head[cell[i]]; head[cell[i]] = i;
+    }
+    pushjob J[64];
+    pthread_t th[64];
+    for (int t = 0; t < nthr; t++) {
+        J[t] = (pushjob){b, owner, head, next, cell, L, D, margin, cs, 1 + (int)((long)N * t / nthr),
+                         1 + (int)((long)N * (t + 1) / nthr), nch, acc + (size_t)t * nch, ch, 0};
+        if (t > 0) pthread_create(&th[t], NULL, push_range, &J[t]);
+    }
+    push_range(&J[0]);
+    long contacts = J[0].contacts;
+    for (int t = 1; t < nthr; t++) {
+        pthread_join(th[t], NULL);
+        contacts += J[t].contacts;
+        for (int k = 0; k < nch; k++)
+            for (int q = 0; q < 7; q++) { acc[k][q] += acc[(size_t)t * nch + k][q]; acc[(size_t)t * nch + k][q] = 0; }
+    }
+    for (int k = 0; k < nch; k++) {   /* the mean push moves the chain, the mean torque turns it */
+        if (acc[k][6] > 0) {
+            const double m = 1.0 / acc[k][6];
+            for (int q = 0; q < 3; q++) ch[k].c[q] += acc[k][q] * m;
+            const double w[3] = {acc[k][3] * m / ch[k].body_r2, acc[k][4] * m / ch[k].body_r2,
+                                 acc[k][5] * m / ch[k].body_r2};
+            rot_turn(ch[k].R, w);
+        }
+        for (int q = 0; q < 7; q++) acc[k][q] = 0;
+    }
+    return contacts;
+}
+
+static int compress_cylinder(B *b, double L0, double L1, double D, double margin) {
+    const int N = b->n, nch = b->nprot;
+    rchain *ch = calloc((size_t)nch, sizeof(rchain));
+    double *body = malloc(sizeof(double) * 3 * (size_t)(N + 1));
+    int *owner = malloc(sizeof(int) * (size_t)(N + 1));
+    for (int k = 0; k < nch; k++) {   /* body frames: unwrapped about the first atom, centred */
+        rchain *c = &ch[k];
+        c->a0 = b->prot[k + 1].start_atom; c->a1 = b->prot[k + 1].end_atom;
+        const double x0 = b->atom[c->a0].pos[0];
+        double m[3] = {0, 0, 0};
+        for (int i = c->a0; i <= c->a1; i++) {
+            double *p = body + 3 * i;
+            double dx = b->atom[i].pos[0] - x0;
+            dx -= L0 * floor(dx / L0 + 0.5);
+            p[0] = x0 + dx; p[1] = b->atom[i].pos[1]; p[2] = b->atom[i].pos[2];
+            for (int q = 0; q < 3; q++) m[q] += p[q];
+            owner[i] = k;
+        }
+        const double n = c->a1 - c->a0 + 1;
+        double r2 = 0;
+        for (int q = 0; q < 3; q++) c->c[q] = m[q] / n;
+        for (int i = c->a0; i <= c->a1; i++)
+            for (int q = 0; q < 3; q++) { body[3 * i + q] -= c->c[q]; r2 += body[3 * i + q] * body[3 * i + q]; }
+        c->body_r2 = r2 / n + 1.0;
+        for (int q = 0; q < 9; q++) c->R[q] = q % 4 == 0;
+    }
+    const double cs = 3.4;   /* above the largest hard-core distance plus the push margin */
+    const long ncell = (long)((L0 / cs) + 2) * ((long)(D / cs) + 2) * ((long)(D / cs) + 2);
+    int *head = malloc(sizeof(int) * (size_t)ncell), *next = malloc(sizeof(int) * (size_t)(N + 1)),
+        *cell = malloc(sizeof(int) * (size_t)(N + 1));
+    int nthr = 16;   /* a fixed partition: the packing is the same on every machine */
+    {
+        const char *e = getenv("SDMD_GEN_THREADS");
+        if (e) nthr = atoi(e) < 1 ? 1 : (atoi(e) > 64 ? 64 : atoi(e));
+    }
+    double (*acc)[7] = calloc((size_t)nch * nthr, sizeof(double[7]));
+    double L = L0;
+    int rc = SDMD_OK;
+    /* A step whose pushes do not settle within 3000 rounds is taken back: the
+       chains return to the last settled packing, get a small random kick, and
+       the axis shrinks by half as much (the step grows again after successes). */
+    rchain *good = malloc(sizeof(rchain) * (size_t)nch);
+    memcpy(good, ch, sizeof(rchain) * (size_t)nch);
+    double Lgood = L, step = 0.01;
+    xrng kick = {0x853c49e6748fea9bULL};
+    for (;;) {
+        long contacts = 1;
+        int rounds = 0;
+        while (contacts && rounds < 3000) {
+            contacts = push_round(b, ch, nch, body, owner, L, D, margin, cs, head, next, cell, acc, nthr);
+            rounds++;
+        }
+        if (getenv("SDMD_COMPRESS_STATS")) fprintf(stderr, "L %.3f step %.5f rounds %d contacts %ld\n", L, step, rounds, contacts);
+        if (contacts) {
+            if (step < 2e-4) { rc = fail(b, "compression jammed at an axis length of %.2f A (target %.2f A)", Lgood, L1); break; }
+            memcpy(ch, good, sizeof(rchain) * (size_t)nch);
+            L = Lgood;
+            for (int k = 0; k < nch; k++) {
+                for (int q = 0; q < 3; q++) ch[k].c[q] += 0.02 * (xr_u(&kick) - 0.5);
+                const double w[3] = {0.004 * (xr_u(&kick) - 0.5), 0.004 * (xr_u(&kick) - 0.5), 0.004 * (xr_u(&kick) - 0.5)};
+                rot_turn(ch[k].R, w);
+            }
+            step *= 0.5;
+        } else {
+            memcpy(good, ch, sizeof(rchain) * (size_t)nch);
+            Lgood = L;
+            if (L <= L1) break;
+            if (rounds < 300 && step < 0.01) step = step * 1.5 < 0.01 ? step * 1.5 : 0.01;
+        }
+        const double Ln = L * (1 - step) > L1 ? L * (1 - step) : L1;
+        for (int k = 0; k < nch; k++) ch[k].c[0] *= Ln / L;
+        L = Ln;
+    }
+    free(good);
+    /* whole chains (the build's energy minimisation takes plain coordinate
+       differences), each with its centre inside the box */
+    for (int k = 0; k < nch; k++) {
+        ch[k].c[0] -= L * floor(ch[k].c[0] / L);
+        for (int i = ch[k].a0; i <= ch[k].a1; i++) {
+            double *p = b->atom[i].pos;
+            rot_apply(ch[k].R, body + 3 * i, p);
+            for (int q = 0; q < 3; q++) p[q] += ch[k].c[q];
+        }
+    }
+    free(ch); free(body); free(owner); free(head); free(next); free(cell); free(acc);
+    return rc;
+}
+
 int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const char *const *sequences,
                       const double box[3], int wall, double margin, uint64_t seed, char **gro_out, char *err,
                       int errlen) {
@@ -1500,14 +1700,15 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
     int nall = 0, capall = 0;
     char (*an)[8] = NULL, (*rn)[8] = NULL;
     int *rid = NULL;
-    /* grid of placed atoms for overlap rejection (4 A cells) */
-    const double G = 4.0;
+    /* grid of placed atoms for overlap rejection (4 A cells); atoms of different
+       chains stay 4 A apart, or 3.3 A in a cylinder (above every hard-core
+       distance of the model's pair tables for peptide atoms, 3.28 A), where the density needs it */
+    const double G = 4.0, clear2 = wall == SDMD_WALL_CYLINDER ? 3.3 * 3.3 : 16.0;
+    /* the box the chains are placed in: the target box, or for a dense cylinder a
+       longer one that the compression below brings to the target length */
+    double bx[3] = {box[0], box[1], box[2]};
     int gn[3];
-    for (int d = 0; d < 3; d++) gn[d] = (int)(box[d] / G) + 1;
-    long ng = (long)gn[0] * gn[1] * gn[2];
-    int *head = malloc(sizeof(int) * ng);
-    for (long q = 0; q < ng; q++) head[q] = -1;
-    int *next = NULL;
+    int *head = NULL, *next = NULL;
     /* chains are independent: relax them on all host threads, then place them in order */
     /* residue templates, learned serially from short context chains with a fixed seed */
     templcache *shared = calloc(1, sizeof(templcache));
@@ -1544,6 +1745,20 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
     for (int q = 0; q < nthr; q++) pthread_join(th[q], NULL);
     pthread_mutex_destroy(&J.mu);
     free(shared);
+    if (wall == SDMD_WALL_CYLINDER && !J.failed) {
+        /* Overlap-free insertion of rigid chains stalls near 70 A^3 per atom in the
+           cylinder; above 110 A^3 per atom it succeeds quickly.  Denser targets are
+           placed in a cylinder stretched to that density and compressed. */
+        long atoms = 0;
+        for (int c = 0; c < n_chains; c++) atoms += J.n[c];
+        const double ra = box[1] / 2 - margin, vol = M_PI * ra * ra * box[0];
+        const double stretch = 110.0 * (double)atoms / vol;
+        if (stretch > 1) bx[0] = box[0] * stretch;
+    }
+    for (int d = 0; d < 3; d++) gn[d] = (int)(bx[d] / G) + 1;
+    long ng = (long)gn[0] * gn[1] * gn[2];
+    head = malloc(sizeof(int) * ng);
+    for (long q = 0; q < ng; q++) head[q] = -1;
     for (int c = 0; c < n_chains; c++) {
         int n = J.n[c]; double *xyz = J.xyz[c]; char (*nm)[8] = J.nm[c], (*rs)[8] = J.rs[c]; int *ri = J.ri[c];
         if (J.failed) {
@@ -1559,33 +1774,72 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
         for (int i = 1; i <= n; i++) for (int d = 0; d < 3; d++) xyz[3 * i + d] -= cm[d];
         int ok = 0;
         double *tr = malloc(sizeof(double) * 3 * (n + 1));
+        /* inside a cylinder the chains lie along its (periodic) x axis: their longest
+           extent (the principal axis of their positions) is turned onto x first, and
+           each attempt turns them about x by a random angle */
+        double A[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+        if (wall == SDMD_WALL_CYLINDER) {
+            double Cv[9] = {0};
+            for (int i = 1; i <= n; i++)
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) Cv[3 * a + b] += xyz[3 * i + a] * xyz[3 * i + b];
+            double e[3] = {1, 0.5, 0.25};
+            for (int it = 0; it < 200; it++) {   /* power iteration: the largest-variance direction */
+                double f[3];
+                for (int a = 0; a < 3; a++) f[a] = Cv[3 * a] * e[0] + Cv[3 * a + 1] * e[1] + Cv[3 * a + 2] * e[2];
+                double nf = sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+                if (!(nf > 0)) break;
+                for (int a = 0; a < 3; a++) e[a] = f[a] / nf;
+            }
+            /* rows of A: e, and two unit vectors orthogonal to it */
+            double u[3] = {fabs(e[0]) < 0.9 ? 1.0 : 0.0, fabs(e[0]) < 0.9 ? 0.0 : 1.0, 0.0};
+            double w[3] = {e[1] * u[2] - e[2] * u[1], e[2] * u[0] - e[0] * u[2], e[0] * u[1] - e[1] * u[0]};
+            double nw = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            for (int a = 0; a < 3; a++) w[a] /= nw;
+            double v[3] = {w[1] * e[2] - w[2] * e[1], w[2] * e[0] - w[0] * e[2], w[0] * e[1] - w[1] * e[0]};
+            for (int a = 0; a < 3; a++) { A[a] = e[a]; A[3 + a] = v[a]; A[6 + a] = w[a]; }
+        }
         for (int attempt = 0; attempt < 20000 && !ok; attempt++) {
-            /* uniform rotation from a random unit quaternion */
-            double u1 = xr_u(&rng), u2 = xr_u(&rng), u3 = xr_u(&rng);
-            double qa = sqrt(1 - u1) * sin(2 * M_PI * u2), qb = sqrt(1 - u1) * cos(2 * M_PI * u2);
-            double qc = sqrt(u1) * sin(2 * M_PI * u3), qd = sqrt(u1) * cos(2 * M_PI * u3);
-            double R[9] = {1 - 2 * (qc * qc + qd * qd), 2 * (qb * qc - qa * qd), 2 * (qb * qd + qa * qc),
-                           2 * (qb * qc + qa * qd), 1 - 2 * (qb * qb + qd * qd), 2 * (qc * qd - qa * qb),
-                           2 * (qb * qd - qa * qc), 2 * (qc * qd + qa * qb), 1 - 2 * (qb * qb + qc * qc)};
-            double t[3] = {xr_u(&rng) * box[0], xr_u(&rng) * box[1], xr_u(&rng) * box[2]};
+            double R[9];
+            double t[3] = {xr_u(&rng) * bx[0], xr_u(&rng) * bx[1], xr_u(&rng) * bx[2]};
+            if (wall == SDMD_WALL_CYLINDER) {   /* R = (turn about x by phi) * A */
+                const double ph = 2 * M_PI * xr_u(&rng), c = cos(ph), sn = sin(ph);
+                const double Rx[9] = {1, 0, 0, 0, c, -sn, 0, sn, c};
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++)
+                        R[3 * a + b] = Rx[3 * a] * A[b] + Rx[3 * a + 1] * A[3 + b] + Rx[3 * a + 2] * A[6 + b];
+                /* the centre within the cylinder's cross-section, uniform over the disc */
+                const double rr = (bx[1] / 2 - margin) * sqrt(xr_u(&rng)), th = 2 * M_PI * xr_u(&rng);
+                t[1] = bx[1] / 2 + rr * cos(th);
+                t[2] = bx[2] / 2 + rr * sin(th);
+            } else {   /* uniform rotation from a random unit quaternion */
+                double u1 = xr_u(&rng), u2 = xr_u(&rng), u3 = xr_u(&rng);
+                double qa = sqrt(1 - u1) * sin(2 * M_PI * u2), qb = sqrt(1 - u1) * cos(2 * M_PI * u2);
+                double qc = sqrt(u1) * sin(2 * M_PI * u3), qd = sqrt(u1) * cos(2 * M_PI * u3);
+                const double Q[9] = {1 - 2 * (qc * qc + qd * qd), 2 * (qb * qc - qa * qd), 2 * (qb * qd + qa * qc),
+                                     2 * (qb * qc + qa * qd), 1 - 2 * (qb * qb + qd * qd), 2 * (qc * qd - qa * qb),
+                                     2 * (qb * qd - qa * qc), 2 * (qc * qd + qa * qb), 1 - 2 * (qb * qb + qc * qc)};
+                memcpy(R, Q, sizeof R);
+            }
             ok = 1;
             for (int i = 1; i <= n && ok; i++) {
                 const double *p = xyz + 3 * i;
                 for (int d = 0; d < 3; d++) tr[3 * i + d] = R[3 * d] * p[0] + R[3 * d + 1] * p[1] + R[3 * d + 2] * p[2] + t[d];
-                const double *q = tr + 3 * i;
+                double *q = tr + 3 * i;
                 if (wall == SDMD_WALL_CYLINDER) {
-                    double ry = q[1] - box[1] / 2, rz = q[2] - box[2] / 2;
-                    if (sqrt(ry * ry + rz * rz) > box[1] / 2 - margin) { ok = 0; break; }
-                    if (q[0] < 0 || q[0] >= box[0]) { ok = 0; break; }
+                    double ry = q[1] - bx[1] / 2, rz = q[2] - bx[2] / 2;
+                    if (sqrt(ry * ry + rz * rz) > bx[1] / 2 - margin) { ok = 0; break; }
+                    q[0] = fmod(q[0], bx[0]);   /* the axis is periodic */
+                    if (q[0] < 0) q[0] += bx[0];
                 } else {
                     /* periodic box: the build wraps every atom once (PBC "full"), so stay
                        within one box length of the primary cell */
-                    for (int d = 0; d < 3; d++) if (q[d] < -box[d] || q[d] >= 2 * box[d]) ok = 0;
+                    for (int d = 0; d < 3; d++) if (q[d] < -bx[d] || q[d] >= 2 * bx[d]) ok = 0;
                 }
                 if (!ok) break;
                 int gc[3];
                 for (int d = 0; d < 3; d++) {
-                    double w = fmod(q[d], box[d]); if (w < 0) w += box[d];
+                    double w = fmod(q[d], bx[d]); if (w < 0) w += bx[d];
                     gc[d] = (int)(w / G); if (gc[d] >= gn[d]) gc[d] = gn[d] - 1; if (gc[d] < 0) gc[d] = 0;
                 }
                 for (int dz = -1; dz <= 1 && ok; dz++) for (int dy = -1; dy <= 1 && ok; dy++) for (int dx = -1; dx <= 1 && ok; dx++) {
@@ -1595,10 +1849,10 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
                         double dd = 0;
                         for (int d = 0; d < 3; d++) {   /* minimum image */
                             double v = q[d] - all[3 * a + d];
-                            v -= box[d] * floor(v / box[d] + 0.5);
+                            v -= bx[d] * floor(v / bx[d] + 0.5);
                             dd += v * v;
                         }
-                        if (dd < 16.0) { ok = 0; break; }
+                        if (dd < clear2) { ok = 0; break; }
                     }
                 }
             }
@@ -1623,7 +1877,7 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
             const double *q = all + 3 * a;
             int gc[3];
             for (int d = 0; d < 3; d++) {
-                double w = fmod(q[d], box[d]); if (w < 0) w += box[d];
+                double w = fmod(q[d], bx[d]); if (w < 0) w += bx[d];
                 gc[d] = (int)(w / G); if (gc[d] >= gn[d]) gc[d] = gn[d] - 1; if (gc[d] < 0) gc[d] = 0;
             }
             long cell = ((long)gc[2] * gn[1] + gc[1]) * gn[0] + gc[0];
@@ -1632,16 +1886,46 @@ int sdmd_generate_gro(const char *datadir, const char *ff, int n_chains, const c
         total += n;
         free(tr); free(xyz); free(nm); free(rs); free(ri);
     }
+    free(J.n); free(J.xyz); free(J.nm); free(J.rs); free(J.ri);
+    free(head); free(next);
     /* residue numbers restart at 1 for every chain: the reader starts a new
        protein when the residue number decreases (src/Initialization.c:946) */
-    sb_printf(&out, "generated peptides\n%d\n", total);
-    for (int a = 0; a < nall; a++) {
-        sb_printf(&out, "%5d%-5s%5s%5d%10.5f%10.5f%10.5f\n", rid[a] % 100000, rn[a], an[a], (a + 1) % 100000,
-                  all[3 * a] / 10, all[3 * a + 1] / 10, all[3 * a + 2] / 10);
+    for (int pass = 0; pass < 2; pass++) {
+        const double *bb = pass == 0 ? bx : box;
+        sb_printf(&out, "generated peptides\n%d\n", total);
+        for (int a = 0; a < nall; a++) {
+            sb_printf(&out, "%5d%-5s%5s%5d%10.5f%10.5f%10.5f\n", rid[a] % 100000, rn[a], an[a], (a + 1) % 100000,
+                      all[3 * a] / 10, all[3 * a + 1] / 10, all[3 * a + 2] / 10);
+        }
+        sb_printf(&out, "%10.5f%10.5f%10.5f\n", bb[0] / 10, bb[1] / 10, bb[2] / 10);
+        if (pass == 1 || bx[0] <= box[0]) break;
+        /* the stretched placement, read back with the model's bounds, compressed to
+           the target length, and written again */
+        B b;
+        memset(&b, 0, sizeof b);
+        sdmd_params p;
+        memset(&p, 0, sizeof p);
+        snprintf(p.continue_mode, 20, "new"); snprintf(p.force_field, 20, "%s", ff);
+        b.p = &p; b.err = err; b.errlen = errlen;
+        snprintf(b.datadir, sizeof b.datadir, "%s", datadir);
+        snprintf(b.ff, sizeof b.ff, "%s", ff);
+        cur c;
+        cur_text(out.s, &c);
+        int r = read_gro(&b, &c);
+        free(c.buf);
+        if (!r) r = read_model(&b);
+        if (!r) r = read_tables(&b);
+        if (!r && b.n != nall) r = fail(&b, "generated system has %d atoms, expected %d", b.n, nall);
+        if (!r) r = compress_cylinder(&b, bx[0], box[0], box[1], margin);
+        if (!r) for (int a = 0; a < nall; a++) memcpy(all + 3 * a, b.atom[a + 1].pos, sizeof(double) * 3);
+        free_builder(&b);
+        out.n = 0;
+        if (r) {
+            free(all); free(an); free(rn); free(rid); free(out.s);
+            return r;
+        }
     }
-    sb_printf(&out, "%10.5f%10.5f%10.5f\n", box[0] / 10, box[1] / 10, box[2] / 10);
-    free(J.n); free(J.xyz); free(J.nm); free(J.rs); free(J.ri);
-    free(head); free(all); free(an); free(rn); free(rid); free(next);
+    free(all); free(an); free(rn); free(rid);
     *gro_out = out.s;
     return SDMD_OK;
 }

@@ -13,11 +13,13 @@ and the force-field tables of Library_Ding.  No public dataset is involved.
   C4  512 single chains of 5-60 residues, box edge scaled to C1's density,
       temperatures 280-400 K
 
-Not generated here: 8 replicas of 400 ten-residue chains in a cylinder of radius
-60 A (axis x, 120 A periodic), NVT 310 K.  Their 0.031 atoms per A^3 is beyond
-what overlap-free random insertion of extended chains reaches; building it would
-need a compressive equilibration.  The wall code such a system runs is covered by
-the cylinder-wall golden case instead.
+  C5  8 replicas of 400 random-sequence 10-mers (about 42k atoms) in a smooth
+      cylindrical wall of radius 60 A (axis x, 120 A periodic), Andersen NVT
+      310 K.  Overlap-free insertion stalls far below this density (0.031 atoms
+      per A^3), so the chains are placed in a longer cylinder and compressed to
+      the target length as rigid bodies (the host generator's compressive
+      packing); the replicas share that start and differ in their thermostat
+      random streams.
 """
 import json
 import os
@@ -63,9 +65,22 @@ def cached(key, make):
     return s
 
 
-def _datadir(param_kw):
+def _datadir(param_kw, wall_atom=None):
+    """A run directory: parameter.txt and the force-field library.  With
+    `wall_atom`, the library's Wall.txt names that atom type instead: the shipped
+    one names PHO, which the reference's atom model table lacks (src/Models.c
+    129-206), so ReadWall would stop."""
     d = tempfile.mkdtemp(prefix="sdmd_wl_")
-    os.symlink(os.path.join(DATA, "Library_Ding"), os.path.join(d, "Library_Ding"))
+    lib = os.path.join(DATA, "Library_Ding")
+    if wall_atom is None:
+        os.symlink(lib, os.path.join(d, "Library_Ding"))
+    else:
+        os.makedirs(os.path.join(d, "Library_Ding"))
+        for e in os.listdir(lib):
+            if e != "Wall.txt":
+                os.symlink(os.path.join(lib, e), os.path.join(d, "Library_Ding", e))
+        with open(os.path.join(d, "Library_Ding", "Wall.txt"), "w") as f:
+            f.write(f"Wall\n   ATOM {wall_atom:<7s} {wall_atom:<4s} 12.0  N N\n")
     with open(os.path.join(d, "parameter.txt"), "w") as f:
         f.write(params_text(**param_kw))
     return d
@@ -154,6 +169,29 @@ def c4(n_systems=512, lo=5, hi=60, seed=1, t_lo=280.0, t_hi=400.0, rng_seed0=500
             for _ in pool.imap_unordered(_c4_touch, missing):
                 pass
     return [_c4_one(sp) for sp in specs]
+
+
+def c5(n_replicas=8, n_chains=400, length=10, seed=1, temperature_k=310.0, radius=60.0, axis=120.0,
+       margin=4.0, rng_seed=1575263273):
+    """n_replicas copies of one packing of n_chains random-sequence chains inside a
+    smooth cylindrical wall (radius `radius`, periodic axis x of length `axis`),
+    atoms at least `margin` from the wall; replica k's thermostat stream is
+    glibc srand(2000 + k).  The wall atom is a CA (the cylinder-wall golden case's
+    choice)."""
+    def make():
+        d = _datadir(dict(temp=round(temperature_k * BOLTZMANN, 4), thermostat="Andersen", time=1e9,
+                          wall_exist="smooth", wall_type="cylinder"), wall_atom="CA")
+        gro = generate_gro(d, random_sequences(n_chains, length, seed), (axis, 2 * radius, 2 * radius), wall=2,
+                           margin=margin, seed=seed)
+        return build_system(d, gro_text=gro, seed=rng_seed)
+
+    base = cached(f"c5_{n_chains}_{length}_{seed}_{temperature_k}_{radius}_{axis}_{margin}_{rng_seed}", make)
+    out = []
+    for k in range(n_replicas):
+        s = base.copy()
+        s.rng = glibc_rng_state(2000 + k)
+        out.append(s)
+    return out
 
 
 def _c4_touch(spec):

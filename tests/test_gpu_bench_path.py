@@ -10,8 +10,8 @@ These tests hold that path to the reference's own golden traces (targets,
 partners, types and sub-types of every pop, event times, velocities and the
 state at every checkpoint -- zero difference, which meets any relative
 tolerance), with and without helper blocks, and to the oracle on the full-size
-systems of the benchmark: the 42k-atom full-rebuild-sweep system and a subset of
-the uneven batch.
+systems of the benchmark: the 42k-atom full-rebuild-sweep system, a subset of
+the uneven batch, and the dense confined batch's shape at a smaller size.
 """
 import numpy as np
 import pytest
@@ -164,3 +164,25 @@ def test_uneven_batch_subset_matches_oracle(engine_mod):
         o = oracle_run(s, 3000)
         assert_state_equal(r.a, o.a)
         assert r.counters == o.counters and r.time == o.time
+
+
+def test_dense_cylinder_batch_matches_oracle(engine_mod):
+    """The dense confined workload's shape at a size the oracle runs in seconds: two
+    replicas of 18 random-sequence 10-mers packed near its density (compressed
+    rigid-chain packing) inside a smooth cylindrical wall of radius 30 A with a
+    27 A periodic axis, differing in their thermostat streams.  With helper
+    blocks advancing the atoms a pop does not involve, each replica equals its own
+    oracle run after 5000 events, wall collisions included."""
+    from sdmd_gb300 import workloads as W
+    systems = W.c5(n_replicas=2, n_chains=18, radius=30.0, axis=27.0)
+    refs = [s.copy() for s in systems]
+    with bench_engine(engine_mod, systems, helpers=6) as e:
+        e.prepare(full=True)
+        e.run(5000)
+        e.download()
+    for s, r in zip(refs, systems):
+        o = oracle_run(s, 5000)
+        assert_state_equal(r.a, o.a)
+        assert r.counters == o.counters and r.time == o.time
+    assert all(s.counters["wall"] > 0 for s in systems)
+    assert not np.array_equal(systems[0].a["x"], systems[1].a["x"])
