@@ -547,6 +547,25 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     h->meta.resize(n_systems);
     int nbcap_max = 0;
     h->smp_cap_of.resize(n_systems);
+    // Neighbour capacity of a system: 4x its fullest 27-cell neighbourhood at upload
+    // (room for density fluctuations during a run), less for dense systems whose
+    // buffers would not fit one CTA's shared memory: 3x, 2x, then 1.5x.  A gather
+    // that overflows at run time stops the run with SDMD_ECAPACITY.
+    const bool scr0 = h->opts.screen == SDMD_SCREEN_FP32;
+    std::vector<int> occ_of(n_systems);
+    for (int k = 0; k < n_systems; k++) occ_of[k] = max_neighbourhood(systems[k]);
+    auto cap_of = [&](int k, int num, int den) {
+        const sdmd_system &s = systems[k];
+        return s.n_atoms <= 2048 ? s.n_atoms : std::min(s.n_atoms, std::max(512, num * occ_of[k] / den + 64));
+    };
+    int head_num = 4, head_den = 1;
+    static const int heads[4][2] = {{4, 1}, {3, 1}, {2, 1}, {3, 2}};
+    for (const auto &f : heads) {
+        head_num = f[0]; head_den = f[1];
+        int mx = 0;
+        for (int k = 0; k < n_systems; k++) mx = std::max(mx, cap_of(k, head_num, head_den));
+        if ((scr0 ? screen_smem_bytes(mx) : fp64_smem_bytes(mx)) <= 227 * 1024) break;
+    }
     for (int k = 0; k < n_systems; k++) {
         long per = (1L << 23) / n_systems;
         per = per < 4096 ? 4096 : per > 65536 ? 65536 : per;
@@ -557,8 +576,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         m.ncell = s.cellnum[0] * s.cellnum[1] * s.cellnum[2];
         m.n_bonds = s.n_bonds; m.n_cons = s.n_cons; m.n_con_steps = s.n_con_steps; m.n_conn = s.n_conn;
         m.n_pair_steps = s.n_pair_steps;
-        int occ = max_neighbourhood(s);
-        m.nbcap = s.n_atoms <= 2048 ? s.n_atoms : std::min(s.n_atoms, std::max(512, 4 * occ + 64));
+        m.nbcap = cap_of(k, head_num, head_den);
         nbcap_max = std::max(nbcap_max, m.nbcap);
         DSys &d = h->hs[k];
         memset(&d, 0, sizeof(d));
