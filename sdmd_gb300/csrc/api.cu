@@ -9,6 +9,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "dev.cuh"
@@ -155,6 +158,68 @@ static int validate(const sdmd_system &s) {
 }
 
 // largest 27-cell neighbourhood population at upload time
+// ---- host staging for the one-copy upload and download ---------------------------
+// A pinned host buffer, kept for the process and grown on demand: handles are
+// created and destroyed repeatedly by drivers that hand a batch back and forth
+// (and by the benchmark's end-to-end loop), and a pinned source lets the copy
+// run at the link's rate.  One user at a time (the lock is held from filling the
+// buffer until its copy has completed).
+struct PinnedStage {
+    std::mutex mu;
+    unsigned char *p = nullptr;
+    size_t bytes = 0;
+    unsigned char *get(size_t need) {   // with mu held
+        if (need <= bytes) return p;
+        if (p) cudaFreeHost(p);
+        p = nullptr; bytes = 0;
+        const size_t want = need + need / 8;
+        if (cudaHostAlloc((void **)&p, want, cudaHostAllocPortable) != cudaSuccess) { cudaGetLastError(); p = nullptr; return nullptr; }
+        bytes = want;
+        return p;
+    }
+};
+static PinnedStage g_up, g_down;
+
+// fn(k) for k = 0..n-1 on up to 8 host threads, in contiguous ranges (per-system
+// host work of large batches; each k writes only its own outputs)
+template <class F> static void parallel_for(int n, F fn) {
+    const int nt = n < 16 ? 1 : (int)std::min<unsigned>({8u, (unsigned)n / 8, std::max(1u, std::thread::hardware_concurrency())});
+    if (nt <= 1) {
+        for (int k = 0; k < n; k++) fn(k);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t++)
+        th.emplace_back([&fn, a = (int)((long)n * t / nt), b = (int)((long)n * (t + 1) / nt)] {
+            for (int k = a; k < b; k++) fn(k);
+        });
+    for (auto &x : th) x.join();
+}
+
+// memcpy of many (dst, src, bytes) pieces on up to 8 host threads (large batches)
+struct Piece { void *dst; const void *src; size_t bytes; };
+static void copy_pieces(const std::vector<Piece> &v) {
+    size_t total = 0;
+    for (auto &c : v) total += c.bytes;
+    const int nt = total < (32u << 20) ? 1 : (int)std::min<unsigned>(8u, std::max(1u, std::thread::hardware_concurrency()));
+    if (nt == 1) {
+        for (auto &c : v) memcpy(c.dst, c.src, c.bytes);
+        return;
+    }
+    // contiguous runs of pieces with about equal bytes per thread
+    std::vector<size_t> cut{0};
+    size_t acc = 0, per = total / nt + 1;
+    for (size_t i = 0; i < v.size(); i++) {
+        acc += v[i].bytes;
+        if (acc >= per * cut.size() && cut.size() < (size_t)nt) cut.push_back(i + 1);
+    }
+    cut.push_back(v.size());
+    std::vector<std::thread> th;
+    for (size_t t = 0; t + 1 < cut.size(); t++)
+        th.emplace_back([&v, a = cut[t], b = cut[t + 1]] { for (size_t i = a; i < b; i++) memcpy(v[i].dst, v[i].src, v[i].bytes); });
+    for (auto &x : th) x.join();
+}
+
 static int max_neighbourhood(const sdmd_system &s) {
     int N = s.n_atoms, cn0 = s.cellnum[0], cn1 = s.cellnum[1], cn2 = s.cellnum[2];
     long ncell = (long)cn0 * cn1 * cn2;
@@ -526,9 +591,11 @@ extern "C" void sdmd_gpu_destroy(sdmd_gpu *h) {
 extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, const sdmd_opts *opts, sdmd_gpu **out) {
     if (!systems || n_systems <= 0 || !out) return SDMD_EINVAL;
     *out = nullptr;
-    for (int k = 0; k < n_systems; k++) {
-        int r = validate(systems[k]);
-        if (r) return r;
+    {
+        std::vector<int> bad(n_systems);
+        parallel_for(n_systems, [&](int k) { bad[k] = validate(systems[k]); });
+        for (int k = 0; k < n_systems; k++)
+            if (bad[k]) return bad[k];
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SDMD_ENODEV;
@@ -553,7 +620,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     // that overflows at run time stops the run with SDMD_ECAPACITY.
     const bool scr0 = h->opts.screen == SDMD_SCREEN_FP32;
     std::vector<int> occ_of(n_systems);
-    for (int k = 0; k < n_systems; k++) occ_of[k] = max_neighbourhood(systems[k]);
+    parallel_for(n_systems, [&](int k) { occ_of[k] = max_neighbourhood(systems[k]); });
     auto cap_of = [&](int k, int num, int den) {
         const sdmd_system &s = systems[k];
         return s.n_atoms <= 2048 ? s.n_atoms : std::min(s.n_atoms, std::max(512, num * occ_of[k] / den + 64));
@@ -636,8 +703,13 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
                    eq(a.pair_step_d, b.pair_step_d, ns * 8) && eq(a.pair_step_e, b.pair_step_e, ns * 8) &&
                    eq(a.pair_step_acc, b.pair_step_acc, ns * 8);
         };
+        // the comparison with system 0 (the common case: one force field) on all
+        // host threads, the rest in order
+        std::vector<char> like0(n_systems, 0);
+        parallel_for(n_systems - 1, [&](int k) { like0[k + 1] = same(systems[0], systems[k + 1]); });
         for (int k = 0; k < n_systems; k++) {
             h->pair_src[k] = k;
+            if (like0[k]) { h->pair_src[k] = 0; continue; }
             for (int j : distinct)
                 if (same(systems[j], systems[k])) { h->pair_src[k] = j; break; }
             if (h->pair_src[k] == k && distinct.size() < 16) distinct.push_back(k);
@@ -665,22 +737,41 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     h->esmem = energy_smem_bytes(nbcap_max);
     std::vector<std::pair<void *, std::pair<const void *, size_t>>> copies;
     std::vector<Screen32> s32(n_systems);
-    for (int k = 0; k < n_systems; k++) build_screen32(systems[k], s32[k], h->pair_src[k] == k);
+    parallel_for(n_systems, [&](int k) { build_screen32(systems[k], s32[k], h->pair_src[k] == k); });
     layout(h, systems, h->arena, &copies, &s32);
-    // one staging image of the static and dynamic blocks, one copy to the device
-    std::vector<unsigned char> staging(h->dyn_end);
-    for (auto &c : copies)
-        memcpy(staging.data() + ((unsigned char *)c.first - h->arena), c.second.first, c.second.second);
+    // one staging image of the static and dynamic blocks, one copy to the device;
+    // the bytes no piece covers (alignment gaps) are zero, as the arena's memset left them
+    std::vector<Piece> pieces;
+    pieces.reserve(copies.size() + 64 * (size_t)n_systems);
+    for (auto &c : copies) pieces.push_back({(void *)((unsigned char *)c.first - h->arena), c.second.first, c.second.second});
     std::vector<DScal> sc(n_systems);
     for (int k = 0; k < n_systems; k++) {
         const sdmd_system &s = systems[k];
         for_dynamic(h, k, s, [&](void *dv, void *hp, size_t bytes) {
-            memcpy(staging.data() + ((unsigned char *)dv - h->arena), hp, bytes);
+            pieces.push_back({(void *)((unsigned char *)dv - h->arena), hp, bytes});
         });
         memset(&sc[k], 0, sizeof(DScal));
         sc[k].time = s.time; sc[k].rng = s.rng; sc[k].c = s.counters;
     }
-    cudaMemcpyAsync(h->arena, staging.data(), h->dyn_end, cudaMemcpyHostToDevice, h->stream);
+    std::sort(pieces.begin(), pieces.end(), [](const Piece &a, const Piece &b) { return a.dst < b.dst; });
+    std::unique_lock<std::mutex> up_lock(g_up.mu);
+    std::vector<unsigned char> pageable;
+    unsigned char *stage = g_up.get(h->dyn_end);
+    if (!stage) { pageable.resize(h->dyn_end); stage = pageable.data(); }   // pinned memory unavailable
+    {
+        size_t at = 0;   // zero the gaps, then fill the pieces
+        for (auto &c : pieces) {
+            const size_t off = (size_t)c.dst;
+            if (off > at) memset(stage + at, 0, off - at);
+            at = std::max(at, off + c.bytes);
+            c.dst = stage + off;
+        }
+        if (h->dyn_end > at) memset(stage + at, 0, h->dyn_end - at);
+    }
+    copy_pieces(pieces);
+    cudaMemcpyAsync(h->arena, stage, h->dyn_end, cudaMemcpyHostToDevice, h->stream);
+    if ((r = cuda_fail(cudaStreamSynchronize(h->stream)))) { up_lock.unlock(); sdmd_gpu_destroy(h); return r; }
+    up_lock.unlock();
     cudaMemcpyAsync(h->sc_all, sc.data(), sizeof(DScal) * n_systems, cudaMemcpyHostToDevice, h->stream);
     cudaMemcpyAsync(h->ds, h->hs.data(), sizeof(DSys) * n_systems, cudaMemcpyHostToDevice, h->stream);
     // the dynamic shared-memory limit must cover dynamic + static usage: always set it
@@ -865,8 +956,12 @@ extern "C" int sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_sy
     for (int k = 0; k < n_systems; k++)
         if (systems[k].n_atoms != h->meta[k].n) return SDMD_EINVAL;
     // the dynamic block of every system in one copy, then scattered into the caller's arrays
-    std::vector<unsigned char> dyn(h->dyn_end - h->dyn_begin);
-    CK(cudaMemcpyAsync(dyn.data(), h->arena + h->dyn_begin, dyn.size(), cudaMemcpyDeviceToHost, h->stream));
+    std::unique_lock<std::mutex> down_lock(g_down.mu);
+    const size_t dyn_bytes = h->dyn_end - h->dyn_begin;
+    std::vector<unsigned char> pageable;
+    unsigned char *dyn = g_down.get(dyn_bytes);
+    if (!dyn) { pageable.resize(dyn_bytes); dyn = pageable.data(); }   // pinned memory unavailable
+    CK(cudaMemcpyAsync(dyn, h->arena + h->dyn_begin, dyn_bytes, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaMemcpyAsync(sc.data(), h->sc_all, sizeof(DScal) * n_systems, cudaMemcpyDeviceToHost, h->stream));
     std::vector<std::vector<double>> tl(n_systems);
     if (h->opts.advance == SDMD_ADVANCE_LAZY)
@@ -875,10 +970,15 @@ extern "C" int sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_sy
             cudaMemcpyAsync(tl[k].data(), h->hs[k].tloc, tl[k].size() * 8, cudaMemcpyDeviceToHost, h->stream);
         }
     CK(cudaStreamSynchronize(h->stream));
-    for (int k = 0; k < n_systems; k++)
-        for_dynamic(h, k, systems[k], [&](void *dv, void *hp, size_t bytes) {
-            memcpy(hp, dyn.data() + ((unsigned char *)dv - (h->arena + h->dyn_begin)), bytes);
-        });
+    {
+        std::vector<Piece> pieces;
+        for (int k = 0; k < n_systems; k++)
+            for_dynamic(h, k, systems[k], [&](void *dv, void *hp, size_t bytes) {
+                pieces.push_back({hp, dyn + ((unsigned char *)dv - (h->arena + h->dyn_begin)), bytes});
+            });
+        copy_pieces(pieces);
+    }
+    down_lock.unlock();
     for (int k = 0; k < n_systems; k++) {
         sdmd_system &s = systems[k];
         s.time = sc[k].time;

@@ -126,6 +126,15 @@ def glibc_rng_state(seed, skip=0):
     return np.concatenate([tab, np.array([f, b], np.int32)])
 
 
+# (name, dtype, pointer slot) of every array field of sdmd_system
+_ARRAY_SLOTS = [(name, dt, getattr(sdmd_system, name).offset // C.sizeof(C.c_void_p))
+                for name, dt in STATIC_ARRAYS + DYNAMIC_ARRAYS]
+assert all(getattr(sdmd_system, n).offset % C.sizeof(C.c_void_p) == 0 for n, _, _ in _ARRAY_SLOTS)
+assert C.sizeof(C.c_void_p) == 8 and C.sizeof(sdmd_system) % 8 == 0
+_SLOT_INDEX = np.array([slot for _, _, slot in _ARRAY_SLOTS], np.intp)
+assert C.sizeof(sdmd_rng) == 33 * 4
+
+
 class System:
     """Arrays of one system plus its ctypes view.  Construct with `from_arrays`."""
 
@@ -136,6 +145,8 @@ class System:
         self.counters = {}
         self.time = 0.0
         self._struct = None
+        self._ptr_arrays = None   # the arrays whose addresses _ptrs holds
+        self._ptrs = None
 
     @property
     def n(self):
@@ -152,7 +163,9 @@ class System:
 
     def struct(self):
         """ctypes sdmd_system viewing this object's arrays (rebuilt each call; the
-        scalars are copied in, the arrays are shared)."""
+        scalars are copied in, the arrays are shared).  The array pointers are
+        written as integers into the struct's pointer slots, and the RNG state is
+        one 33-word copy: a batch of hundreds of systems is marshalled in a few ms."""
         s = sdmd_system()
         for k, v in self.scal.items():
             if isinstance(v, (list, tuple, np.ndarray)):
@@ -161,15 +174,20 @@ class System:
                     arr[i] = x
             else:
                 setattr(s, k, v)
-        for name, dt in STATIC_ARRAYS + DYNAMIC_ARRAYS:
-            arr = self.a[name]
-            assert arr.dtype == dt and arr.flags.c_contiguous, name
-            setattr(s, name, arr.ctypes.data_as(_PTR[dt]))
+        arrs = [self.a[name] for name, _, _ in _ARRAY_SLOTS]
+        held = self._ptr_arrays
+        if held is None or any(a is not b for a, b in zip(arrs, held)):
+            # arrays replaced since the last call: check them and take their addresses
+            # (the list keeps those very arrays alive, so the addresses stay theirs)
+            for (name, dt, _), arr in zip(_ARRAY_SLOTS, arrs):
+                if arr.dtype != dt or not arr.flags.c_contiguous:
+                    raise ValueError(f"array {name}: need C-contiguous {np.dtype(dt).name}")
+            self._ptrs = np.array([arr.__array_interface__["data"][0] for arr in arrs], np.uint64)
+            self._ptr_arrays = arrs
+        np.frombuffer(s, np.uint64, C.sizeof(sdmd_system) // 8)[_SLOT_INDEX] = self._ptrs
         s.time = self.time
-        for i in range(31):
-            s.rng.tab[i] = int(self.rng[i])
-        s.rng.front = int(self.rng[31])
-        s.rng.rear = int(self.rng[32])
+        rng = np.ascontiguousarray(self.rng, np.int32)
+        C.memmove(C.addressof(s.rng), rng.ctypes.data, 33 * 4)
         for k, v in self.counters.items():
             setattr(s.counters, k, int(v))
         self._struct = s

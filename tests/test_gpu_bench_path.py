@@ -170,18 +170,19 @@ def test_dense_cylinder_batch_matches_oracle(engine_mod):
     """The dense confined workload's shape at a size the oracle runs in seconds: two
     replicas of 18 random-sequence 10-mers packed near its density (compressed
     rigid-chain packing) inside a smooth cylindrical wall of radius 30 A with a
-    27 A periodic axis, differing in their thermostat streams.  With helper
-    blocks advancing the atoms a pop does not involve, each replica equals its own
-    oracle run after 5000 events, wall collisions included."""
+    27 A periodic axis, differing in their thermostat streams; atoms start 3.4 A
+    from the wall (above every wall hard core, 3.27 A), so that wall collisions come
+    early.  With helper blocks advancing the atoms a pop does not involve, each
+    replica equals its own oracle run after 8000 events, wall collisions included."""
     from sdmd_gb300 import workloads as W
-    systems = W.c5(n_replicas=2, n_chains=18, radius=30.0, axis=27.0)
+    systems = W.c5(n_replicas=2, n_chains=18, radius=30.0, axis=27.0, margin=3.4)
     refs = [s.copy() for s in systems]
     with bench_engine(engine_mod, systems, helpers=6) as e:
         e.prepare(full=True)
-        e.run(5000)
+        e.run(8000)
         e.download()
     for s, r in zip(refs, systems):
-        o = oracle_run(s, 5000)
+        o = oracle_run(s, 8000)
         assert_state_equal(r.a, o.a)
         assert r.counters == o.counters and r.time == o.time
     assert all(s.counters["wall"] > 0 for s in systems)
