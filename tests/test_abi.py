@@ -64,3 +64,26 @@ def test_host_rng_helpers_match_glibc(gpu_lib):
     engine.lib().sdmd_rng_seed(C.byref(r), 1575263273)
     libc.srand(1575263273)
     assert [engine.lib().sdmd_rng_next(C.byref(r)) for _ in range(5000)] == [libc.rand() for _ in range(5000)]
+
+
+def test_struct_views_the_current_arrays():
+    """System.struct() writes every array's address into the sdmd_system it hands
+    to the C ABI, reuses them while the arrays are the same objects, and takes
+    the new ones when an array is replaced; scalars and the RNG ring are copied."""
+    from sdmd_gb300.system import STATIC_ARRAYS, DYNAMIC_ARRAYS, from_fixture
+    from tests.conftest import load_golden
+    s = from_fixture(load_golden("ala10_nvt"), "pre")
+    addr = lambda p: C.cast(p, C.c_void_p).value
+    st = s.struct()
+    for name, _ in STATIC_ARRAYS + DYNAMIC_ARRAYS:
+        assert addr(getattr(st, name)) == s.a[name].ctypes.data, name
+    assert [st.rng.tab[i] for i in range(31)] + [st.rng.front, st.rng.rear] == [int(v) for v in s.rng]
+    assert st.n_atoms == s.n and st.time == s.time
+    s.a["vx"] = s.a["vx"].copy()                      # a replaced array is seen at once
+    s.rng[3] += 1
+    st = s.struct()
+    assert addr(st.vx) == s.a["vx"].ctypes.data
+    assert st.rng.tab[3] == int(s.rng[3])
+    with pytest.raises(ValueError):
+        s.a["x"] = s.a["x"][::2]                      # a strided view is refused
+        s.struct()
