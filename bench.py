@@ -199,6 +199,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def autotune_candidates(systems):
+    """CTA sizes the autotuner tries: up to 512 threads for large systems (which run
+    with helper blocks), 128-256 for a single small one, 64-256 for batches."""
+    if min(s.n for s in systems) >= 2048:
+        return (128, 256, 512)
+    return (128, 256) if len(systems) == 1 else (64, 128, 256)
+
+
 def load_traffic():
     p = os.path.join(REPO, "profiles", "traffic.json")
     try:
@@ -263,7 +271,7 @@ def run_ours(args, D):
         threads = args.threads
     else:   # CTA size from the autotuner (short runs on copies of the workload)
         threads, tuned = autotune_threads(systems, advance=adv, screen=scr, device=D.local,
-                                          candidates=(128, 256) if len(systems) == 1 else (64, 128, 256))
+                                          candidates=autotune_candidates(systems))
     eng = Engine(systems, threads=threads, device=D.local, advance=adv, screen=scr)
     eng.prepare(full=True)
     sweep_ms = eng.last_ms()[0]

@@ -170,7 +170,8 @@ enum { SDMD_SCREEN_FP64 = 0,     /* every candidate root in FP64 */
 typedef struct sdmd_opts {
     int32_t advance;               /* SDMD_ADVANCE_* */
     int32_t screen;                /* SDMD_SCREEN_* */
-    int32_t threads_per_system;    /* 32 (one warp) .. 256; 0 = autotuned */
+    int32_t threads_per_system;    /* 32 (one warp) .. 256, or up to 512 for systems that run with
+                                      helper blocks (eager advance, FP32 screen); 0 = 128 */
     int32_t device;                /* CUDA device ordinal */
     int32_t trace_capacity;        /* records kept by sdmd_gpu_run when tracing (0 = off) */
     /* eager advance on the FP32 screened path: blocks on other SMs that advance
@@ -255,7 +256,8 @@ int  sdmd_gpu_last_run_stats(sdmd_gpu *h, int64_t *launches, int64_t *loop_launc
 /* How the handle launches its event loop: threads per system block, helper blocks
  * of the eager advance (0: none), whether whole systems are staged in shared
  * memory, and which loop kernel runs (SDMD_LOOP_*).  Any pointer may be NULL. */
-enum { SDMD_LOOP_FP64 = 0, SDMD_LOOP_SCREEN = 1, SDMD_LOOP_SCREEN_R128 = 2, SDMD_LOOP_SCREEN_HELPERS = 3 };
+enum { SDMD_LOOP_FP64 = 0, SDMD_LOOP_SCREEN = 1, SDMD_LOOP_SCREEN_R128 = 2, SDMD_LOOP_SCREEN_HELPERS = 3,
+       SDMD_LOOP_SCREEN_HELPERS_512 = 4 };
 int  sdmd_gpu_launch_info(sdmd_gpu *h, int32_t *threads, int32_t *helper_blocks, int32_t *staged,
                           int32_t *loop_kernel);
 

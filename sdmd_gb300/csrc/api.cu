@@ -42,6 +42,8 @@ struct sdmd_gpu {
     void (*sweep_k)(const DSys *, int) = nullptr;            // plain FP64 or FP32-screened kernels
     void (*loop_k)(const DSys *, double, int) = nullptr;
     int helpers = 0;                               // helper blocks of the eager advance (0: none)
+    const void *coop_k = nullptr;                  // the cooperative loop build for this block size
+    int sweep_threads = 128;                       // block size of the per-system sweep kernels (<= 256)
     std::vector<int> pair_src;                     // system whose (identical) pair tables system k shares
     size_t dyn_begin = 0, dyn_end = 0;             // the dynamic arrays' block in the arena
     DScal *sc_all = nullptr;                       // the systems' scalar blocks, contiguous
@@ -689,6 +691,8 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
     h->smem_loop = h->staged ? h->smem + st_max : h->smem;
     h->threads = h->opts.threads_per_system > 0 ? h->opts.threads_per_system : 128;
     if (h->threads < 32 || h->threads > 1024 || (h->threads & 31)) { delete h; return SDMD_EINVAL; }
+    if (h->threads > 512) { delete h; return SDMD_EUNSUPPORTED; }
+    h->sweep_threads = std::min(h->threads, 256);
     if (h->smem > 227 * 1024) { delete h; return SDMD_ECAPACITY; }
     // systems whose pair tables are identical (the same force field) share one device copy
     h->pair_src.assign(n_systems, 0);
@@ -812,10 +816,12 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         int32_t nmax = 0;
         for (auto &m : h->meta) nmax = std::max(nmax, m.n);
         int coop = 0, per_sm = 0;
+        // blocks of more than 256 threads: the 128-register build of the same launch
+        h->coop_k = h->threads > 256 ? (const void *)loop_kernel_screen_coop512 : (const void *)loop_kernel_screen_coop;
         if ((r = cuda_fail(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, h->opts.device))) ||
-            (r = cuda_fail(cudaFuncSetAttribute(loop_kernel_screen_coop, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            (r = cuda_fail(cudaFuncSetAttribute(h->coop_k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                 (int)h->smem_loop))) ||
-            (r = cuda_fail(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, loop_kernel_screen_coop, h->threads,
+            (r = cuda_fail(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, h->coop_k, h->threads,
                                                                          h->smem_loop)))) {
             sdmd_gpu_destroy(h);
             return r;
@@ -825,6 +831,8 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         if (want == 0) want = (n_systems * 2 <= h->sms && nmax >= 2048) ? room : 0;
         if (coop && want > 0 && room > 0) h->helpers = std::min(want, room);
     }
+    // blocks of more than 256 threads exist only as the cooperative loop with helpers
+    if (h->threads > 256 && h->helpers == 0) { sdmd_gpu_destroy(h); return SDMD_EUNSUPPORTED; }
     if (h->opts.advance == SDMD_ADVANCE_LAZY) lazy_enter_kernel<<<n_systems, 128, 0, h->stream>>>(h->ds);
     if ((r = cuda_fail(cudaStreamSynchronize(h->stream)))) { sdmd_gpu_destroy(h); return r; }
     *out = h;
@@ -880,9 +888,9 @@ extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
             sweep_predict_kernel<<<dim3(px, ns), 64, h->smem, h->stream>>>(h->ds);
             sweep_verify_kernel<<<dim3(vx, ns), 128, h->vsmem, h->stream>>>(h->ds);
         }
-        sweep_fix_kernel<<<ns, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+        sweep_fix_kernel<<<ns, h->sweep_threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
     } else {
-        h->sweep_k<<<h->n_systems, h->threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
+        h->sweep_k<<<h->n_systems, h->sweep_threads, h->smem, h->stream>>>(h->ds, full_predict ? 1 : 0);
     }
     if (full_predict) samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(h->ds, h->n_systems);
     CK(cudaGetLastError());
@@ -927,7 +935,7 @@ static int run_rounds(sdmd_gpu *h, int64_t want, double t_end) {
             double te = t_end;
             int nc = h->n_systems;
             void *args[] = {(void *)&ds, (void *)&te, (void *)&nc};
-            CK(cudaLaunchCooperativeKernel((const void *)loop_kernel_screen_coop, dim3(nc + h->helpers),
+            CK(cudaLaunchCooperativeKernel(h->coop_k, dim3(nc + h->helpers),
                                            dim3(h->threads), args, h->smem_loop, h->stream));
         } else {
             h->loop_k<<<h->n_systems, h->threads, h->smem_loop, h->stream>>>(h->ds, t_end, h->staged);
@@ -1238,7 +1246,7 @@ extern "C" int sdmd_gpu_prepare_noalloc(sdmd_gpu *h, int32_t full_predict) {
         dim3 grid((unsigned)std::max<int64_t>(1, std::min<int64_t>((want + 255) / 256, 1024)), (unsigned)h->n_systems);
         samples_values_kernel<<<grid, 256, 0, h->stream>>>(table, want);
     }
-    h->sweep_k<<<h->n_systems, h->threads, h->smem, h->stream>>>(table, full_predict ? 1 : 0);
+    h->sweep_k<<<h->n_systems, h->sweep_threads, h->smem, h->stream>>>(table, full_predict ? 1 : 0);
     if (full_predict) samples_commit_kernel<<<n_blocks(h->n_systems, 64), 64, 0, h->stream>>>(table, h->n_systems);
     noalloc_first_error_kernel<<<1, 1, 0, h->stream>>>(table, h->n_systems, first);
     CK(cudaGetLastError());
@@ -1263,7 +1271,7 @@ extern "C" int sdmd_gpu_launch_info(sdmd_gpu *h, int32_t *threads, int32_t *help
     if (helper_blocks) *helper_blocks = h->helpers;
     if (staged) *staged = h->staged;
     if (loop_kernel) {
-        if (h->helpers > 0) *loop_kernel = SDMD_LOOP_SCREEN_HELPERS;
+        if (h->helpers > 0) *loop_kernel = h->threads > 256 ? SDMD_LOOP_SCREEN_HELPERS_512 : SDMD_LOOP_SCREEN_HELPERS;
         else if (h->loop_k == loop_kernel_screen_r128) *loop_kernel = SDMD_LOOP_SCREEN_R128;
         else if (h->loop_k == loop_kernel_screen) *loop_kernel = SDMD_LOOP_SCREEN;
         else *loop_kernel = SDMD_LOOP_FP64;

@@ -24,6 +24,7 @@ __global__ void loop_kernel_screen_r128(const DSys *systems, double t_end_overri
 // the screened loop with helper blocks for the eager advance (cooperative launch:
 // blocks 0 .. n_chain-1 run the systems, the rest advance their atoms)
 __global__ void loop_kernel_screen_coop(const DSys *systems, double t_end_override, int n_chain);
+__global__ void loop_kernel_screen_coop512(const DSys *systems, double t_end_override, int n_chain);
 
 // parallel full-rebuild sweep of the screened path (sweep_par.cuh)
 size_t verify_smem_bytes(int nbcap, int warps);

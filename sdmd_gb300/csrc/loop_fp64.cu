@@ -1230,6 +1230,22 @@ __global__ void loop_kernel_screen_coop(const DSys *systems, double t_end_overri
     loop_body<true>(systems, t_end_override, 0, S, G, B, C, PS, n_chain);
 }
 
+// The same launch built for 512 threads a block (at most 128 registers a thread):
+// dense systems, whose hundreds of candidates per atom then take half the screen
+// passes.
+__global__ void __launch_bounds__(512, 1) loop_kernel_screen_coop512(const DSys *systems, double t_end_override,
+                                                                     int n_chain) {
+    __shared__ DSys S, G;
+    __shared__ Blk B;
+    __shared__ DScal C;
+    __shared__ PairScal PS;
+    if ((int)blockIdx.x >= n_chain) {
+        helper_body(systems, n_chain);
+        return;
+    }
+    loop_body<true>(systems, t_end_override, 0, S, G, B, C, PS, n_chain);
+}
+
 size_t screen_smem_bytes(int nbcap) { return screen_smem_bytes_dev(nbcap); }
 size_t verify_smem_bytes(int nbcap, int warps) { return verify_warp_bytes(nbcap) * (size_t)warps; }
 

@@ -24,7 +24,7 @@ ABI_FUNCS = ["sdmd_gpu_abi_version", "sdmd_gpu_device_count", "sdmd_gpu_strerror
              "sdmd_gpu_prepare_noalloc", "sdmd_gpu_last_run_stats", "sdmd_gpu_energies", "sdmd_gpu_run_remd",
              "sdmd_gpu_launch_info"]
 LOOP_KERNELS = {0: "loop_kernel_fp64", 1: "loop_kernel_screen", 2: "loop_kernel_screen_r128",
-                3: "loop_kernel_screen_coop"}
+                3: "loop_kernel_screen_coop", 4: "loop_kernel_screen_coop512"}
 
 _lib = None
 
@@ -33,6 +33,9 @@ class sdmd_remd(C.Structure):
     _fields_ = [("num", C.POINTER(C.c_int32)), ("T", C.POINTER(C.c_double)), ("E", C.POINTER(C.c_double)),
                 ("every_events", C.c_int64), ("every_time", C.c_double), ("rng", sdmd_rng),
                 ("attempted", C.c_int64), ("accepted", C.c_int64), ("exchanges_done", C.c_int64)]
+
+
+SDMD_EUNSUPPORTED = -17   # include/sdmd_gpu.h
 
 
 class EngineError(RuntimeError):
@@ -213,11 +216,19 @@ def autotune_threads(systems, advance=ADVANCE_EAGER, screen=SCREEN_FP64, candida
                      device=0):
     """Pick the threads per system (CTA size) that runs `events` executed events per
     system fastest on copies of `systems` (full-rebuild sweep first, one warm-up
-    run, then a timed run).  Returns (best, {threads: events/s})."""
+    run, then a timed run).  A size the handle does not support for this batch
+    (more than 256 threads without helper blocks) is skipped.  Returns
+    (best, {threads: events/s})."""
     rates = {}
     for t in candidates:
         work = [s.copy() for s in systems]
-        with Engine(work, advance=advance, screen=screen, threads=t, device=device) as e:
+        try:
+            e = Engine(work, advance=advance, screen=screen, threads=t, device=device)
+        except EngineError as err:
+            if err.code == SDMD_EUNSUPPORTED and t > 256:
+                continue
+            raise
+        with e:
             e.prepare(full=True)
             e.run(max(events // 4, 16))
             e.run(events)

@@ -166,18 +166,22 @@ def test_uneven_batch_subset_matches_oracle(engine_mod):
         assert r.counters == o.counters and r.time == o.time
 
 
-def test_dense_cylinder_batch_matches_oracle(engine_mod):
+@pytest.mark.parametrize("threads", [256, 512])
+def test_dense_cylinder_batch_matches_oracle(engine_mod, threads):
     """The dense confined workload's shape at a size the oracle runs in seconds: two
     replicas of 18 random-sequence 10-mers packed near its density (compressed
     rigid-chain packing) inside a smooth cylindrical wall of radius 30 A with a
     27 A periodic axis, differing in their thermostat streams; atoms start 3.4 A
     from the wall (above every wall hard core, 3.27 A), so that wall collisions come
     early.  With helper blocks advancing the atoms a pop does not involve, each
-    replica equals its own oracle run after 8000 events, wall collisions included."""
+    replica equals its own oracle run after 8000 events, wall collisions included,
+    with 256-thread blocks and with the 512-thread build."""
     from sdmd_gb300 import workloads as W
     systems = W.c5(n_replicas=2, n_chains=18, radius=30.0, axis=27.0, margin=3.4)
     refs = [s.copy() for s in systems]
-    with bench_engine(engine_mod, systems, helpers=6) as e:
+    with bench_engine(engine_mod, systems, helpers=6, threads=threads) as e:
+        assert e.launch_info()["loop_kernel"] == ("loop_kernel_screen_coop512" if threads > 256
+                                                   else "loop_kernel_screen_coop")
         e.prepare(full=True)
         e.run(8000)
         e.download()
