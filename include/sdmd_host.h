@@ -153,6 +153,27 @@ void sdmd_host_free(sdmd_host_system *h);
 const char *sdmd_host_atom_names(const sdmd_host_system *h);
 const char *sdmd_host_residue_names(const sdmd_host_system *h);
 
+/*
+ * The reference's text outputs, written from an engine state (SaveData,
+ * src/DataSave.c).  Each call writes one frame to `path`, appending when `append`
+ * is non-zero (the reference appends one frame per dump), in the reference's
+ * format byte for byte.  names8 / resnames8: 8-byte name records as above.
+ *   sdmd_write_gro     out_trj.gro      SaveGRO           (src/DataSave.c:616-640)
+ *   sdmd_write_pdb     out_pdb.pdb      SavePDB           (:588-613)
+ *   sdmd_write_cnt     out_cnt.txt      SaveConnectionMap (:218-233): static bond /
+ *                      constraint bits plus the formed hydrogen bonds' HB and
+ *                      neighbour bits
+ *   sdmd_write_hbn     out_HBn.txt      SaveHB            (:205-216)
+ *   sdmd_write_series  out_pot.txt, out_kin.txt, out_tem.txt: one "time value" line
+ *                      (SavePot / SaveKin / SaveTemp, :235-278); the value is the
+ *                      caller's (sdmd_gpu_energies gives CalPotenE / CalKinetE)
+ */
+int sdmd_write_gro(const char *path, int append, const sdmd_system *s, const char *names8, const char *resnames8);
+int sdmd_write_pdb(const char *path, int append, const sdmd_system *s, const char *names8, const char *resnames8);
+int sdmd_write_cnt(const char *path, int append, const sdmd_system *s);
+int sdmd_write_hbn(const char *path, int append, const sdmd_system *s);
+int sdmd_write_series(const char *path, int append, double time, double value);
+
 #ifdef __cplusplus
 }
 #endif

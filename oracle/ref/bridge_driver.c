@@ -73,6 +73,14 @@ long bd_run(long n_events) {
     return frame;
 }
 
+/* one of the reference's own writers (SaveData, src/DataSave.c:105-160) into its
+   output directory, flushed; type is the reference's enum FileType */
+void bd_save_type(int type) {
+    SaveData((enum FileType)type, fileList);
+    if (fileList[type].file) fflush(fileList[type].file);
+}
+double bd_temperature(void) { return CalSysTem(); }
+
 /* the reference's own energies of its current state (src/ToolFunctions.c:626-752) */
 double bd_potential(void) { long w = warningsum; double e = CalPotenE(); warningsum = w; return e; }
 double bd_kinetic(void) { return CalKinetE(); }

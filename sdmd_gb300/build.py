@@ -82,7 +82,7 @@ def build_host(force=False):
     if not srcs:
         return None
     deps = srcs + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")] + [
-        os.path.join(INCLUDE, "sdmd_gpu.h")]
+        os.path.join(INCLUDE, "sdmd_gpu.h"), os.path.join(INCLUDE, "sdmd_host.h")]
     if not force and _newer(HOST_LIB, deps):
         return HOST_LIB
     tmp = HOST_LIB + ".tmp"

@@ -1,0 +1,149 @@
+/*
+ * writers.c -- the reference's text outputs (SaveData, src/DataSave.c), written
+ * from an engine state (an sdmd_system as sdmd_gpu_download fills it).
+ *
+ * Each call appends one frame to the named file (or starts it, append == 0), in
+ * the reference's exact format: the trajectory (SaveGRO :616-640, SavePDB
+ * :588-613), the connection map (SaveConnectionMap :218-233), the hydrogen-bond
+ * counts (SaveHB :205-216) and the one-number-per-dump series of potential and
+ * kinetic energy and temperature (SavePot / SaveKin / SaveTemp :235-278).  The
+ * energies are the caller's (sdmd_gpu_energies computes the reference's
+ * CalPotenE / CalKinetE on the device); the writer only formats them.
+ *
+ * Atom and residue names come as 8-byte records (entry i at i*8), as
+ * sdmd_host_atom_names / sdmd_host_residue_names return them.
+ */
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "sdmd_host.h"
+
+#define BOND_CONNECT 0x01       /* connection-map bits (src/DMD.h:59-63) */
+#define CONSTRAINT_CONNECT 0x02
+#define HB_CONNECT 0x04
+#define NEIGHBOR_CONNECT 0x08
+
+static FILE *open_out(const char *path, int append) { return path ? fopen(path, append ? "a" : "w") : NULL; }
+
+static int close_out(FILE *f) { return fclose(f) == 0 ? SDMD_OK : SDMD_EINVAL; }
+
+/* a name record as the reference prints it: at most 7 characters, NUL-terminated */
+static const char *name8(const char *names, int i, char *buf) {
+    memcpy(buf, names + 8 * (size_t)i, 8);
+    buf[7] = 0;
+    return buf;
+}
+
+int sdmd_write_gro(const char *path, int append, const sdmd_system *s, const char *names8, const char *resnames8) {
+    if (!s || !names8 || !resnames8) return SDMD_EINVAL;
+    FILE *f = open_out(path, append);
+    if (!f) return SDMD_EINVAL;
+    char a[8], r[8];
+    fprintf(f, "model\n");
+    fprintf(f, "%5i\n", s->n_atoms);
+    for (int i = 1; i <= s->n_atoms; i++)
+        fprintf(f, "%5i%-5s%5s%5i%8.3f%8.3f%8.3f%10.4f%10.4f%10.4f\n", s->aanum[i], name8(resnames8, i, r),
+                name8(names8, i, a), i, s->x[i] / 10, s->y[i] / 10, s->z[i] / 10, s->vx[i], s->vy[i], s->vz[i]);
+    fprintf(f, "%10.5f%10.5f%10.5f\n", s->box[0] / 10, s->box[1] / 10, s->box[2] / 10);
+    return close_out(f);
+}
+
+int sdmd_write_pdb(const char *path, int append, const sdmd_system *s, const char *names8, const char *resnames8) {
+    if (!s || !names8 || !resnames8) return SDMD_EINVAL;
+    FILE *f = open_out(path, append);
+    if (!f) return SDMD_EINVAL;
+    char a[8], r[8];
+    fprintf(f, "TITLE     I have tried to minimize the energy!\n");
+    fprintf(f, "REMARK    THIS IS A SIMULATION BOX\n");
+    fprintf(f, "CRYST1%9.3lf%9.3lf%9.3lf  90.00  90.00  90.00 P 1           1\n", s->box[0], s->box[1], s->box[2]);
+    for (int i = 1; i <= s->n_atoms; i++) {
+        name8(names8, i, a);
+        /* the chain letter: peptide 1 is 'A' (the reference adds '0' to 'A' - '1') */
+        const char chain = (char)(s->protein[i] + 'A' - '1' + '0');
+        fprintf(f, "ATOM  %5i  %-4s%3s %c%4i    %8.3lf%8.3lf%8.3lf%6.2lf%6.2lf           %c\n", i, a,
+                name8(resnames8, i, r), chain, s->aanum[i], s->x[i], s->y[i], s->z[i], 1.0, 0.0, a[0]);
+    }
+    fprintf(f, "TER\n");
+    fprintf(f, "ENDMDL\n");
+    return close_out(f);
+}
+
+static int cmp_int(const void *a, const void *b) {
+    const int x = *(const int *)a, y = *(const int *)b;
+    return (x > y) - (x < y);
+}
+
+/* The connection map of the state: the static BOND/CONSTRAINT bits of the sparse
+   rows, and for every formed hydrogen bond i -> j (hb_bond) the bits HBEvent sets:
+   map[i][j] |= HB, map[i][nb(j)] |= NEIGHBOR, map[nb(j)][i] |= NEIGHBOR, with nb(j)
+   j's HB neighbour (src/Events.c:320-325). */
+int sdmd_write_cnt(const char *path, int append, const sdmd_system *s) {
+    if (!s) return SDMD_EINVAL;
+    const int N = s->n_atoms;
+    /* the HB-derived entries as (row, column, bits) triples */
+    int cap = 16, n_hb = 0;
+    int (*hb)[3] = malloc(sizeof(int[3]) * (size_t)cap);
+    if (!hb) return SDMD_ENOMEM;
+    for (int i = 1; i <= N; i++) {
+        const int j = s->hb_bond[i];
+        if (j <= 0 || j > N) continue;
+        const int nj = s->hb_neighbor[j];
+        if (n_hb + 3 > cap) {
+            cap *= 2;
+            int (*g)[3] = realloc(hb, sizeof(int[3]) * (size_t)cap);
+            if (!g) { free(hb); return SDMD_ENOMEM; }
+            hb = g;
+        }
+        hb[n_hb][0] = i; hb[n_hb][1] = j; hb[n_hb][2] = HB_CONNECT; n_hb++;
+        if (nj > 0 && nj <= N) {
+            hb[n_hb][0] = i; hb[n_hb][1] = nj; hb[n_hb][2] = NEIGHBOR_CONNECT; n_hb++;
+            hb[n_hb][0] = nj; hb[n_hb][1] = i; hb[n_hb][2] = NEIGHBOR_CONNECT; n_hb++;
+        }
+    }
+    FILE *f = open_out(path, append);
+    if (!f) { free(hb); return SDMD_EINVAL; }
+    int *cols = malloc(sizeof(int) * ((size_t)N + 2));
+    int32_t *bits = calloc((size_t)N + 2, sizeof(int32_t));
+    if (!cols || !bits) { fclose(f); free(hb); free(cols); free(bits); return SDMD_ENOMEM; }
+    fprintf(f, "Frame=%.2lf\n", s->time);
+    for (int i = 1; i <= N; i++) {
+        int nc = 0;
+        for (int q = s->conn_off[i]; q < s->conn_off[i + 1]; q++) {
+            const int n = s->conn_j[q];
+            if (n < 1 || n > N) continue;
+            if (!bits[n]) cols[nc++] = n;
+            bits[n] |= s->conn_bits[q] & (BOND_CONNECT | CONSTRAINT_CONNECT);
+        }
+        for (int k = 0; k < n_hb; k++) {
+            if (hb[k][0] != i) continue;
+            const int n = hb[k][1];
+            if (!bits[n]) cols[nc++] = n;
+            bits[n] |= hb[k][2];
+        }
+        qsort(cols, (size_t)nc, sizeof(int), cmp_int);
+        for (int k = 0; k < nc; k++) {
+            if (bits[cols[k]] > 0) fprintf(f, "%i %i ", cols[k], bits[cols[k]]);
+            bits[cols[k]] = 0;
+        }
+        fprintf(f, "\n");
+    }
+    free(hb); free(cols); free(bits);
+    return close_out(f);
+}
+
+int sdmd_write_hbn(const char *path, int append, const sdmd_system *s) {
+    if (!s) return SDMD_EINVAL;
+    FILE *f = open_out(path, append);
+    if (!f) return SDMD_EINVAL;
+    fprintf(f, "%5.2lf%10i%10i\n", s->time, s->counters.hb_formed, s->counters.alpha_hb_formed);
+    return close_out(f);
+}
+
+int sdmd_write_series(const char *path, int append, double time, double value) {
+    FILE *f = open_out(path, append);
+    if (!f) return SDMD_EINVAL;
+    fprintf(f, "%5.2lf    %10.4lf\n", time, value);
+    return close_out(f);
+}

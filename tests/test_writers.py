@@ -1,0 +1,91 @@
+"""The host library's output writers against the reference's own (no GPU).
+
+sdmd_write_* (sdmd_gb300/host/writers.c) write the reference's text outputs from
+an engine state.  Here the reference's unmodified sources (oracle/_ref, with the
+bridge) set up a golden case, run their own loop, and write their outputs with
+SaveData (src/DataSave.c); the bridge then fills an sdmd_system from that same
+state, and the host library's writers must produce the same bytes: the
+trajectory (.gro, .pdb), the connection map (with the hydrogen bonds the run
+formed), the HB counts and the energy / temperature series (two frames each,
+appended).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from tests.test_ref_bridge import LIB, REPO, _bridge, _fill, case_dir, in_child
+
+pytestmark = pytest.mark.skipif(not os.path.exists(LIB),
+                                reason="the reference's sources are not here (oracle/_ref not built)")
+
+TRJ, POT, KIN, TEM, CNT, HBN, PDB = 0, 1, 2, 3, 4, 5, 7   # enum FileType (src/DMD.h:212-228)
+NAMES = {TRJ: "out_trj.gro", POT: "out_pot.txt", KIN: "out_kin.txt", TEM: "out_tem.txt", CNT: "out_cnt.txt",
+         HBN: "out_HBn.txt", PDB: "out_pdb.pdb"}
+
+
+def _child_frames(case, runs, q):
+    """The reference writes one frame after each run; the state of each frame is
+    filled through the bridge and returned with the reference's energies."""
+    try:
+        work, ind, outd = case_dir(case)
+        L = _bridge(ind, outd)
+        L.bd_potential.restype = C.c_double
+        L.bd_kinetic.restype = C.c_double
+        L.bd_temperature.restype = C.c_double
+        L.bd_save_type.argtypes = [C.c_int]
+        L.bd_sweep()
+        frames = []
+        for n in runs:
+            L.bd_run(n)
+            for t in (TRJ, POT, KIN, TEM, CNT, HBN, PDB):
+                L.bd_save_type(t)
+            s = _fill(L)
+            frames.append((s.a, s.scal, s.counters, s.time, L.bd_potential(), L.bd_kinetic(), L.bd_temperature()))
+        files = {t: open(os.path.join(outd, name), "rb").read() for t, name in NAMES.items()}
+        q.put(("ok", frames, files, ind))
+    except Exception as e:
+        q.put(("error", repr(e)))
+
+
+def _host_writers():
+    from sdmd_gb300.host import lib
+    from sdmd_gb300.system import sdmd_system
+    L = lib()
+    P = C.POINTER(sdmd_system)
+    for f in ("sdmd_write_gro", "sdmd_write_pdb"):
+        getattr(L, f).argtypes = [C.c_char_p, C.c_int, P, C.c_char_p, C.c_char_p]
+    for f in ("sdmd_write_cnt", "sdmd_write_hbn"):
+        getattr(L, f).argtypes = [C.c_char_p, C.c_int, P]
+    L.sdmd_write_series.argtypes = [C.c_char_p, C.c_int, C.c_double, C.c_double]
+    return L
+
+
+@pytest.mark.parametrize("case,runs", [("ala10_nvt", (2000, 2000)), ("sheet2", (30000, 20000))])
+def test_writers_match_the_reference(case, runs, tmp_path):
+    from sdmd_gb300.host import build_system
+    from sdmd_gb300.system import System
+    frames, ref_files, ind = in_child(_child_frames, case, runs)
+    d = np.load(os.path.join(REPO, "tests", "golden", f"{case}.npz"))
+    named = build_system(ind, gro_text=bytes(d["meta/gro"]).decode(), seed=int(d["pre/seed"][0]))
+    L = _host_writers()
+    out = {t: str(tmp_path / name).encode() for t, name in NAMES.items()}
+    for k, (a, scal, counters, time, pot, kin, tem) in enumerate(frames):
+        s = System()
+        s.a, s.scal, s.counters, s.time = a, scal, counters, time
+        s.rng = np.zeros(33, np.int32)
+        st = C.byref(s.struct())
+        app = 1 if k else 0
+        assert L.sdmd_write_gro(out[TRJ], app, st, named.names, named.resnames) == 0
+        assert L.sdmd_write_pdb(out[PDB], app, st, named.names, named.resnames) == 0
+        assert L.sdmd_write_cnt(out[CNT], app, st) == 0
+        assert L.sdmd_write_hbn(out[HBN], app, st) == 0
+        for t, v in ((POT, pot), (KIN, kin), (TEM, tem)):
+            assert L.sdmd_write_series(out[t], app, time, v) == 0
+    for t, name in NAMES.items():
+        mine = open(out[t], "rb").read()
+        assert mine == ref_files[t], f"{name} differs"
+    if case == "sheet2":
+        assert frames[-1][2]["hb_formed"] > 0          # the map carries formed hydrogen bonds
+        assert b" 4 " in ref_files[CNT] or b" 5 " in ref_files[CNT] or b" 12 " in ref_files[CNT]
