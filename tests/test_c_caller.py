@@ -42,6 +42,9 @@ int main(int argc, char **argv) {
     if (rc != SDMD_OK) { printf("build failed: %s\n", err); return 1; }
     const sdmd_system *s = sdmd_host_view(h);
     printf("atoms %d x1 %a\n", s->n_atoms, s->x[1]);
+    snprintf(path, sizeof path, "%s/out_trj.gro", argv[1]);
+    rc = sdmd_write_gro(path, 0, s, sdmd_host_atom_names(h), sdmd_host_residue_names(h));
+    printf("gro %d\n", rc);
     sdmd_host_free(h);
     int32_t n = -1;
     rc = sdmd_gpu_device_count(&n);
@@ -74,3 +77,6 @@ def test_plain_c_caller(golden, tmp_path):
     atoms, x1 = lines["atoms"].split(" x1 ")
     assert int(atoms) == 59
     assert float.fromhex(x1) == float(d["pre/x"][1])   # the reference's initial state
+    assert lines["gro"] == "0"                            # the trajectory writer, from C
+    gro = (data / "out_trj.gro").read_text().splitlines()
+    assert gro[0] == "model" and int(gro[1]) == 59 and len(gro) == 62 and gro[2][10:15].strip() == "N"
