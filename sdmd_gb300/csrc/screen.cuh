@@ -233,9 +233,9 @@ __device__ __forceinline__ int conn_bits_w(const DSys &S, int i, int j) {
     return (((unsigned)w[1 + (idx >> 5)] & m) ? 1 : 0) | (((unsigned)w[5 + (idx >> 5)] & m) ? 2 : 0);
 }
 
-// ---- screen verdicts ----------------------------------------------------------
+// ---- screen outcomes -----------------------------------------------------------
 enum : int { SC_NONE = 0, SC_OFFER = 1, SC_REFINE = 2 };
-struct Verdict { int st, warn, dup; Iv t; };
+struct Outcome { int st, warn, dup; Iv t; };
 
 __device__ __forceinline__ int bsign3(Iv b) { return b.hi < 0.f ? 1 : (b.lo >= 0.f ? 0 : 2); }   // 1: b < 0
 
@@ -325,7 +325,7 @@ __device__ bool fp_screen(const DSys &S, int a1, int a2, int kind, int neg, Iv r
 }
 
 // BondTime for one bond (eval_bond's branches)
-__device__ void screen_bond(const DSys &S, int i, int q, const PIv &I, Verdict &v, int always_refine) {
+__device__ void screen_bond(const DSys &S, int i, int q, const PIv &I, Outcome &v, int always_refine) {
     v.warn = 0; v.dup = 0;
     int j = S.bond_j[q];
     if (j < S.dup_limit && S.ev_partner[j] == i && S.ev_type[j] == SDMD_EV_BOND && S.ev_pcounter[j] == S.ev_counter[i]) {
@@ -361,7 +361,7 @@ __device__ void screen_bond(const DSys &S, int i, int q, const PIv &I, Verdict &
 }
 
 // HBTime's scan over one candidate (eval_hb_scan's branches), kinematics given
-__device__ void screen_hbs_k(const DSys &S, int i, int j, const KIv &k, Verdict &v) {
+__device__ void screen_hbs_k(const DSys &S, int i, int j, const KIv &k, Outcome &v) {
     v.st = SC_REFINE;
     if (k.r2.lo > S.cut32[1]) { v.st = SC_NONE; return; }
     if (!(k.r2.hi <= S.cut32[0])) return;
@@ -385,13 +385,13 @@ __device__ void screen_hbs_k(const DSys &S, int i, int j, const KIv &k, Verdict 
     if (t.lo > 0.f) { v.st = SC_OFFER; v.t = t; v.warn = o.warn; }
 }
 
-// One 27-cell candidate j of atom i: the collision verdict (CollisionTime) and,
-// when the atom scans for hydrogen bonds (hb), the HB-scan verdict, sharing one
+// One 27-cell candidate j of atom i: the collision outcome (CollisionTime) and,
+// when the atom scans for hydrogen bonds (hb), the HB-scan outcome, sharing one
 // evaluation of the pair's kinematics.  `always` forces "refine" (the partner's
 // view of the target, whose event is only known after the target's fold).  Every
 // field of j is loaded at once; A holds atom i's own fields.
 __device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, const AtomI &A, bool hb, int always,
-                            Verdict &vc, Verdict &vh) {
+                            Outcome &vc, Outcome &vh) {
     vc.warn = 0; vc.dup = 0; vc.st = SC_NONE;
     vh.warn = 0; vh.dup = 0; vh.st = SC_NONE;
     if (j == i) return;
@@ -432,7 +432,7 @@ __device__ void screen_cell(const DSys &S, int i, int j, const PIv &I, const Ato
     KIv k; kin_iv(S, I, J, k);
     if (need_h) screen_hbs_k(S, i, j, k, vh);
     if (!need_c) return;
-    Verdict &v = vc;
+    Outcome &v = vc;
     if (k.r2.lo > S.cut32[1]) return;                  // certainly beyond the scan radius
     v.st = SC_REFINE;
     if (!(k.r2.hi <= S.cut32[0])) return;
@@ -868,7 +868,7 @@ constexpr int RC = 64;            // refined candidates per atom before the plai
 struct ShmS {
     Shm F;                        // the plain path's buffers (used when more than RC candidates need FP64)
     int32_t *nbj[2];
-    uint8_t *stat[2];             // verdict | warnings << 2, per entry
+    uint8_t *stat[2];             // outcome | warnings << 2, per entry
     float *tlo[2];                // lower time bound of an offer
     int32_t *rl[2];               // refined entries in scan order
     Slots R[2];                   // their exact FP64 results
@@ -1102,7 +1102,7 @@ __device__ bool predict_two(const DSys &S, int t, int p, ShmS &M, PairScal &PS, 
             a = g < S0 ? 0 : 1; e = a ? g - S0 : g;
         }
         const int i = PS.i[a], nb = PS.nb[a], nn = PS.nn[a];
-        Verdict v[2];
+        Outcome v[2];
         int j, ne = 1;
         if (e < nb) {
             const int qb = S.bond_off[i] + e;

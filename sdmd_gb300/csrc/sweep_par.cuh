@@ -20,7 +20,7 @@
 // sequential sweep does.  The event tree is then built bottom-up over CreateCBT's
 // leaf layout (src/CBT.c:16-30): with every time fixed, CreateCBT's incremental
 // repairs leave each node the winner of its two children (ties to the right), the
-// one tree this build produces.
+// one tree the bottom-up construction produces.
 #pragma once
 
 namespace sdmd {
