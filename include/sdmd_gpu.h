@@ -211,6 +211,13 @@ int  sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict);
  * t_end), whichever comes first.  Returns after all systems stopped. */
 int  sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end);
 
+/* SingleThreadRun's dump cadence (src/SGThread.c:128-139): run every system until
+ * it executes an event at a time >= dump_time (> 0), after which the reference
+ * writes its outputs, or until one of sdmd_gpu_run's limits.  at_dump (may be
+ * NULL; n_systems entries) receives 1 for each system that stopped at such an
+ * event and 0 for the others; the host then downloads and writes. */
+int  sdmd_gpu_run_to_dump(sdmd_gpu *h, double dump_time, int64_t max_events, double t_end, int32_t *at_dump);
+
 /* Copy every system's dynamic state back into the caller's arrays. */
 int  sdmd_gpu_download(sdmd_gpu *h, sdmd_system *systems, int32_t n_systems);
 

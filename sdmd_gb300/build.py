@@ -2,6 +2,7 @@
 
   sdmd_gb300/libsdmd_gpu.so   CUDA kernels + C ABI (include/sdmd_gpu.h), sm_103a only
   sdmd_gb300/libsdmd_host.so  host-side C: system builder for the reference's inputs
+  sdmd_gb300/sdmd-gb300       the sDMD executable on the engine (app/sdmd_run.c)
 
 Translation units compile in parallel; nothing here uses cmake or torch.
 """
@@ -92,11 +93,29 @@ def build_host(force=False):
     return HOST_LIB
 
 
+APP = os.path.join(HERE, "sdmd-gb300")
+APP_SRC = os.path.join(HERE, "app", "sdmd_run.c")
+
+
+def build_app(force=False):
+    """The sDMD executable, linked with the two libraries beside it."""
+    deps = [APP_SRC, GPU_LIB, HOST_LIB, os.path.join(INCLUDE, "sdmd_gpu.h"), os.path.join(INCLUDE, "sdmd_host.h")]
+    if not force and _newer(APP, deps):
+        return APP
+    tmp = APP + ".tmp"
+    subprocess.check_call(["gcc", "-O2", "-std=gnu99", "-Wall", "-I" + INCLUDE, "-o", tmp, APP_SRC, "-L" + HERE,
+                           "-lsdmd_gpu", "-lsdmd_host", "-Wl,-rpath,$ORIGIN", "-lm"])
+    os.replace(tmp, APP)
+    return APP
+
+
 def build_all(force=False):
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         fg = ex.submit(build_gpu, force)
         fh = ex.submit(build_host, force)
-        return fg.result(), fh.result()
+        out = fg.result(), fh.result()
+    build_app(force)
+    return out
 
 
 if __name__ == "__main__":

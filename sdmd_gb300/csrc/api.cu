@@ -904,6 +904,38 @@ extern "C" int sdmd_gpu_prepare(sdmd_gpu *h, int32_t full_predict) {
 
 static int run_rounds(sdmd_gpu *h, int64_t want, double t_end);
 
+extern "C" int sdmd_gpu_run_to_dump(sdmd_gpu *h, double dump_time, int64_t max_events, double t_end,
+                                    int32_t *at_dump) {
+    if (!h || max_events < 0 || !(dump_time > 0)) return SDMD_EINVAL;
+    if (at_dump)
+        for (int k = 0; k < h->n_systems; k++) at_dump[k] = 0;
+    if (max_events == 0) return SDMD_OK;
+    CK(cudaSetDevice(h->opts.device));
+    CK(cudaEventRecord(h->e0, h->stream));
+    // every system stops after its first executed event at a time >= dump_time (the
+    // loop's stop point of the replica exchange), or at the event limit
+    const int n = h->n_systems;
+    std::vector<double> stop(n, dump_time);
+    CK(cudaMemcpyAsync(h->x_stop, stop.data(), sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    remd_round_kernel<<<n_blocks(n, 64), 64, 0, h->stream>>>(h->ds, n, max_events, h->x_stop);
+    h->launches = 1; h->loop_launches = 0; h->loop_ms = 0;
+    int r = run_rounds(h, std::min<int64_t>(4 * max_events + 64, 1 << 16), t_end);
+    if (r) return r;
+    std::vector<DScal> sc(n);
+    CK(cudaMemcpyAsync(sc.data(), h->sc_all, sizeof(DScal) * n, cudaMemcpyDeviceToHost, h->stream));
+    // the stop point off again for later runs
+    remd_round_kernel<<<n_blocks(n, 64), 64, 0, h->stream>>>(h->ds, n, 0, nullptr);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->e1, h->stream));
+    CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->run_ms = ms;
+    if (at_dump)
+        for (int k = 0; k < n; k++) at_dump[k] = sc[k].at_stop ? 1 : 0;
+    return collect_errors(h);
+}
+
 extern "C" int sdmd_gpu_run(sdmd_gpu *h, int64_t max_events, double t_end) {
     if (!h || max_events < 0) return SDMD_EINVAL;
     CK(cudaSetDevice(h->opts.device));

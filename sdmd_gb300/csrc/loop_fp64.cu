@@ -1032,7 +1032,9 @@ __device__ __forceinline__ void loop_body(const DSys *systems, double t_end_over
     const double t_end = t_end_override > 0 ? t_end_override : S.t_end;
     const int64_t stop_at = C.target_frame;
     // denied pops do not advance `frame`; bound the pops so that no input can spin forever
-    const int64_t pop_limit = C.pops + 64 * (stop_at - C.c.frame) + 1000000;
+    // (a run without an event limit, stop_at near INT64_MAX, gets 2^40 pops)
+    const int64_t left = stop_at - C.c.frame;
+    const int64_t pop_limit = C.pops + (left > (int64_t(1) << 34) ? int64_t(1) << 40 : 64 * left + 1000000);
     for (;;) {
         if (tid == 0) {
             if (C.pops >= pop_limit) set_err(B, SDMD_ETIMEOUT, 0);

@@ -1,0 +1,68 @@
+#!/usr/bin/env python3
+"""Generate tests/golden/cli_ala10/: a whole run of the reference's own sDMD
+executable, for the end-to-end comparison with the engine's executable.
+
+Needs the reference's executable built by the oracle recipe
+(oracle/ref/Makefile -> oracle/_ref/sDMD: the reference's unmodified sources,
+its own main, -DDEBUG_RANDOM for the fixed seed).  The run: the ALA x 10 chain of
+the ala10_nvt fixture, Andersen NVT, Time 40 with Dump_Rate 10, and the optional
+outputs -pot -kin -tem -HBn.  Kept: the inputs (in/parameter.txt, in/sys.gro; the
+force-field library is the package's) and the text outputs (expected/).
+
+Usage: python tests/golden/make_cli_golden.py
+"""
+import os
+import shutil
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+EXE = os.path.join(REPO, "oracle", "_ref", "sDMD")
+CASE = os.path.join(HERE, "cli_ala10")
+FLAGS = ["-pot", "-kin", "-tem", "-HBn"]
+OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt"]
+
+
+def parameters(text, time, dump):
+    lines = text.splitlines()
+    for k, line in enumerate(lines):
+        if line.startswith("Time "):
+            lines[k] = f"Time               {time}"
+        elif line.startswith("Dump_Rate"):
+            lines[k] = f"Dump_Rate          {dump}"
+    return "\n".join(lines) + "\n"
+
+
+def main():
+    if not os.path.exists(EXE):
+        raise SystemExit(f"{EXE} is missing: build it with make -C oracle/ref")
+    d = np.load(os.path.join(HERE, "ala10_nvt.npz"))
+    work = tempfile.mkdtemp(prefix="sdmd_cli_golden_")
+    ind, outd = os.path.join(work, "in"), os.path.join(work, "out")
+    os.makedirs(ind)
+    os.makedirs(outd)
+    shutil.copytree(os.path.join(REPO, "sdmd_gb300", "data", "Library_Ding"), os.path.join(ind, "Library_Ding"))
+    param = parameters(bytes(d["meta/parameter"]).decode(), 40, 10.0)
+    with open(os.path.join(ind, "parameter.txt"), "w") as f:
+        f.write(param)
+    with open(os.path.join(ind, "sys.gro"), "wb") as f:
+        f.write(bytes(d["meta/gro"]))
+    subprocess.run([EXE, "-i", ind, "-o", outd, "-f", "sys.gro", *FLAGS], check=True, stdout=subprocess.DEVNULL,
+                   timeout=600)
+    os.makedirs(os.path.join(CASE, "in"), exist_ok=True)
+    os.makedirs(os.path.join(CASE, "expected"), exist_ok=True)
+    shutil.copy(os.path.join(ind, "parameter.txt"), os.path.join(CASE, "in", "parameter.txt"))
+    shutil.copy(os.path.join(ind, "sys.gro"), os.path.join(CASE, "in", "sys.gro"))
+    for name in OUTPUTS:
+        shutil.copy(os.path.join(outd, name), os.path.join(CASE, "expected", name))
+    with open(os.path.join(CASE, "expected", "flags.txt"), "w") as f:
+        f.write(" ".join(FLAGS) + "\n")
+    shutil.rmtree(work)
+    print("wrote", CASE)
+
+
+if __name__ == "__main__":
+    main()

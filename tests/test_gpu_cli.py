@@ -1,0 +1,41 @@
+"""The engine's sDMD executable against the reference's own executable (GPU).
+
+tests/golden/cli_ala10 holds a whole run of the reference's unmodified sDMD
+(tests/golden/make_cli_golden.py: its own main and command line, the fixed
+-DDEBUG_RANDOM seed): ALA x 10 under Andersen NVT to Time 40 with Dump_Rate 10
+and -pot -kin -tem -HBn.  sdmd-gb300 runs the same command line on the same
+inputs with the same seed (SDMD_DEBUG_RANDOM), its event loop on the GPU, and
+every output file must equal the reference's byte for byte: the trajectory, the
+connection map, the energies, the temperature and the HB counts at every dump.
+"""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CASE = os.path.join(REPO, "tests", "golden", "cli_ala10")
+OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt"]
+
+
+def test_executable_writes_the_reference_outputs(tmp_path):
+    import __graft_entry__ as G
+    G.build()
+    from sdmd_gb300 import build
+    ind, outd = tmp_path / "in", tmp_path / "out"
+    shutil.copytree(os.path.join(CASE, "in"), ind)
+    shutil.copytree(os.path.join(REPO, "sdmd_gb300", "data", "Library_Ding"), ind / "Library_Ding")
+    outd.mkdir()
+    flags = open(os.path.join(CASE, "expected", "flags.txt")).read().split()
+    env = dict(os.environ, SDMD_DEBUG_RANDOM="1")
+    r = subprocess.run([build.APP, "-i", str(ind), "-o", str(outd), "-f", "sys.gro", *flags], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    assert "Finished!" in r.stdout
+    for name in OUTPUTS:
+        mine = (outd / name).read_bytes()
+        ref = open(os.path.join(CASE, "expected", name), "rb").read()
+        assert mine == ref, f"{name} differs from the reference's"
