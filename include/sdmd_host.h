@@ -144,6 +144,12 @@ int  sdmd_saved_read(const char *path, sdmd_saved **out, char *errbuf, int errle
 int  sdmd_saved_info(const sdmd_saved *s, sdmd_saved_header *out);
 int  sdmd_saved_apply(const sdmd_saved *s, sdmd_system *sys, const char *names8, char *errbuf, int errlen);
 int  sdmd_saved_write(const char *path, const sdmd_saved *tpl, const sdmd_system *sys, char *errbuf, int errlen);
+/* The template of a new run: a system sdmd_build_system built from p and seed.  Its
+   sdmd_saved_write output is the reference's savedData.dat of that run, byte for
+   byte except the atom records' two pointer fields (the reference writes its own
+   heap addresses there; ReadBreakPoint ignores them). */
+int  sdmd_saved_new(const sdmd_host_system *h, const sdmd_params *p, uint32_t seed, sdmd_saved **out, char *errbuf,
+                    int errlen);
 void sdmd_saved_free(sdmd_saved *s);
 
 sdmd_system *sdmd_host_view(sdmd_host_system *h);

@@ -12,8 +12,8 @@
  * first executed event of each Dump_Rate interval, the first event of a new run
  * included -- the reference's outputs in its formats: out_trj.gro and
  * out_cnt.txt, out_pot/kin/tem.txt, out_HBn.txt and out_pdb.pdb when their flags
- * ask for them, and savedData.dat in a continue run (its static records come from
- * the file the run continued from).  The end-of-run statistics block is the
+ * ask for them, and savedData.dat (its static records from the inputs, or from the
+ * file a continue run started from).  The end-of-run statistics block is the
  * reference's (src/DMD.c:244-265).
  *
  * The random seed is time(NULL), as the reference's release build uses, or
@@ -104,6 +104,11 @@ int main(int argc, const char *argv[]) {
     sdmd_system *sys = sdmd_host_view(hs);
     const char *names = sdmd_host_atom_names(hs), *resnames = sdmd_host_residue_names(hs);
     if (saved && sdmd_saved_apply(saved, sys, names, err, sizeof err) != SDMD_OK) {
+        fprintf(stderr, "!!ERROR!!: %s\n", err);
+        return 1;
+    }
+    /* a new run's checkpoint: its static records as the reference's set-up leaves them */
+    if (!saved && sdmd_saved_new(hs, &p, seed, &saved, err, sizeof err) != SDMD_OK) {
         fprintf(stderr, "!!ERROR!!: %s\n", err);
         return 1;
     }

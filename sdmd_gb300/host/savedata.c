@@ -21,6 +21,7 @@
 #include <string.h>
 
 #include "sdmd_host.h"
+#include "host_static.h"
 
 typedef struct { int32_t atomNum, proteinNum, aminoacidNum; } sv_seq;
 typedef struct {
@@ -99,6 +100,90 @@ void sdmd_saved_free(sdmd_saved *s) {
     if (!s) return;
     free(s->cmap); free(s->aa); free(s->pep); free(s->prop); free(s->dyn); free(s->celllist);
     free(s);
+}
+
+/* The template of a new run's checkpoint, from the system the host library built:
+   every static record as the reference's set-up leaves it (ReadCoordinate's
+   property fields, CalculateMass's residue and peptide masses, the connection
+   map's BOND / CONSTRAINT bits, zeroed padding, no pointers), the parameters, and
+   the seed; dynamic fields come from the state at each write. */
+int sdmd_saved_new(const sdmd_host_system *h, const sdmd_params *p, uint32_t seed, sdmd_saved **out, char *err,
+                   int errlen) {
+    if (!h || !p || !out) return SDMD_EINVAL;
+    const sdmd_system *sys = sdmd_host_view((sdmd_host_system *)h);
+    sdmd_host_static st;
+    sdmd_host_static_info(h, &st);
+    const int N = sys->n_atoms;
+    const size_t N1 = (size_t)N + 1;
+    sdmd_saved *s = calloc(1, sizeof *s);
+    if (!s) return SDMD_ENOMEM;
+    s->atomnum = N; s->numofprotein = st.n_prot; s->totalAminoAcids = st.n_aa;
+    s->cmap = calloc(N1 * N1, sizeof(int32_t));
+    s->aa = calloc((size_t)st.n_aa + 1, sizeof(sv_aa));
+    s->pep = calloc((size_t)st.n_prot + 1, sizeof(sv_pep));
+    s->prop = calloc(N1, sizeof(sv_property));
+    s->dyn = calloc(N1, sizeof(sv_dynamic));
+    if (!s->cmap || !s->aa || !s->pep || !s->prop || !s->dyn) { sdmd_saved_free(s); return SDMD_ENOMEM; }
+    for (int i = 0; i <= N; i++)
+        for (int q = sys->conn_off[i]; q < sys->conn_off[i + 1]; q++)
+            s->cmap[(size_t)i * N1 + sys->conn_j[q]] = sys->conn_bits[q];
+    s->timestep = p->time; s->cutoffr = p->cutoff; s->temperature = p->temperature; s->outputrate = p->dump_rate;
+    memcpy(s->method, st.method, sizeof s->method);
+    for (int d = 0; d < 3; d++) {
+        s->box[d + 1] = sys->box[d]; s->cellnum[d + 1] = sys->cellnum[d]; s->cellsize[d + 1] = sys->cellsize[d];
+    }
+    for (int k = 1; k <= st.n_aa; k++) {
+        memcpy(s->aa[k].nameofAA, st.aa_name + 8 * k, 4);
+        s->aa[k].type = st.aa_type[k]; s->aa[k].startAtomNum = st.aa_start[k]; s->aa[k].endAtomNum = st.aa_end[k];
+        s->aa[k].proteinNum = st.aa_prot[k]; s->aa[k].mass = st.aa_mass[k];
+    }
+    for (int k = 1; k <= st.n_prot; k++) {
+        s->pep[k].startAtomNum = st.pep_start[k]; s->pep[k].endAtomNum = st.pep_end[k];
+        s->pep[k].startAANum = st.pep_aa_start[k]; s->pep[k].endAANum = st.pep_aa_end[k];
+        s->pep[k].mass = st.pep_mass[k];
+    }
+    s->prop[0].mass = st.mass0[0];
+    s->prop[0].typeofAtom = st.type0[0];
+    memcpy(s->prop[0].extraProperty, st.ext, 32);
+    s->dyn[0].event.partner = SDMD_INVALID;   /* atom 0's event as initialised */
+    s->dyn[0].event.time = SDMD_INFINIT;
+    for (int i = 1; i <= N; i++) {
+        sv_property *P = &s->prop[i];
+        memcpy(P->name, st.names + 8 * (size_t)i, 8);
+        P->name[7] = 0;
+        memcpy(P->extraProperty, st.ext + 32 * (size_t)i, 32);
+        memcpy(P->nameofAA, st.resnames + 8 * (size_t)i, 8);
+        P->nameofAA[7] = 0;
+        P->num = i; P->typeofAtom = sys->type[i]; P->typeofAA = sys->aatype[i]; P->mass = sys->mass[i];
+        P->sequence.atomNum = i; P->sequence.proteinNum = sys->protein[i]; P->sequence.aminoacidNum = sys->aanum[i];
+        s->dyn[i].HB.neighbor = sys->hb_neighbor[i];
+        s->dyn[i].HB.role = (char)sys->hb_role[i];
+        /* InitializeCharge (src/Initialization.c:2092-2099) without charge-model
+           flags: "+" / "-" atoms of ARG, ASP, GLU, HIS and LYS */
+        const int res = sys->aatype[i];
+        if (res == 2 || res == 4 || res == 7 || res == 9 || res == 12) {
+            if (!strcmp(P->extraProperty[0], "+")) P->charge = 1;
+            else if (!strcmp(P->extraProperty[0], "-")) P->charge = -1;
+        }
+    }
+    /* ... and the termini (:2101-2116): each peptide's first atom of type 18 and last
+       of type 26 */
+    for (int k = 1; k <= st.n_prot; k++) {
+        for (int n = st.pep_start[k]; n <= st.pep_end[k]; n++)
+            if (sys->type[n] == 18) { s->prop[n].charge = 1; break; }
+        for (int n = st.pep_end[k]; n >= st.pep_start[k]; n--)
+            if (sys->type[n] == 26) { s->prop[n].charge = -1; break; }
+    }
+    s->cellnum[0] = N + sys->cellnum[0] * sys->cellnum[1] * sys->cellnum[2] + 1;   /* src/Initialization.c:1068 */
+    s->seed = seed;
+    /* REMDInfo's initializer (src/DMD.c:126-132): a run without -REMD */
+    s->remd.REMD_PortNum = -1;
+    s->remd.REMD_OutputRate = 1000;
+    s->remd.REMD_Temperature.num = -1;
+    s->remd.REMD_Temperature.T = -1;
+    *out = s;
+    (void)err; (void)errlen;
+    return SDMD_OK;
 }
 
 #define RD(ptr, size, n) (fread((ptr), (size), (size_t)(n), f) == (size_t)(n))

@@ -8,6 +8,7 @@
  * reference's head-insertion order, which decides the scan order of BondTime.
  */
 #include "sdmd_host.h"
+#include "host_static.h"
 
 #include <ctype.h>
 #include <math.h>
@@ -55,6 +56,13 @@ struct sdmd_host_system {
         *cell_list;
     int64_t *ev_counter, *ev_pcounter;
     char *names, *resnames;
+    /* the checkpoint's static records (host_static.h) */
+    char *ext;
+    int32_t n_aa, n_prot;
+    char *aa_name;
+    int32_t *aa_type, *aa_start, *aa_end, *aa_prot, *pep_start, *pep_end, *pep_aa_start, *pep_aa_end;
+    double *aa_mass, *pep_mass;
+    char method[20];
 };
 
 typedef struct {
@@ -955,6 +963,35 @@ static int export_system(B *b, sdmd_host_system **out) {
     }
     h->conn_off[N + 1] = kn; h->bond_off[N + 1] = kb; h->con_off[N + 1] = kc;
     s->n_conn = kn;
+    /* the checkpoint's static records: extra properties, and the residue and peptide
+       tables with CalculateMass's masses (a hydrogen counts 1, src/Initialization.c
+       1547-1570) */
+    h->ext = zalloc(32 * N1);
+    for (int i = 0; i <= N; i++) {   /* atom 0 too: it can pick up a residue's extra properties */
+        memcpy(h->ext + 32 * i, b->atom[i].ext0, strnlen(b->atom[i].ext0, 15));
+        memcpy(h->ext + 32 * i + 16, b->atom[i].ext1, strnlen(b->atom[i].ext1, 15));
+    }
+    h->n_aa = b->naa; h->n_prot = b->nprot;
+    const size_t na1 = (size_t)b->naa + 1, np1 = (size_t)b->nprot + 1;
+    h->aa_name = zalloc(8 * na1);
+    h->aa_type = zalloc(4 * na1); h->aa_start = zalloc(4 * na1); h->aa_end = zalloc(4 * na1); h->aa_prot = zalloc(4 * na1);
+    h->aa_mass = zalloc(8 * na1);
+    for (int k = 1; k <= b->naa; k++) {
+        memcpy(h->aa_name + 8 * k, b->aa[k].name, strnlen(b->aa[k].name, 4));
+        h->aa_type[k] = b->aa[k].type; h->aa_start[k] = b->aa[k].start; h->aa_end[k] = b->aa[k].end;
+        h->aa_prot[k] = b->aa[k].protein;
+        for (int n = b->aa[k].start; n <= b->aa[k].end; n++)
+            h->aa_mass[k] += strncmp(b->atom[n].name, "H", 1) == 0 ? 1 : b->atom[n].mass;
+    }
+    h->pep_start = zalloc(4 * np1); h->pep_end = zalloc(4 * np1); h->pep_aa_start = zalloc(4 * np1);
+    h->pep_aa_end = zalloc(4 * np1); h->pep_mass = zalloc(8 * np1);
+    for (int k = 1; k <= b->nprot; k++) {
+        h->pep_start[k] = b->prot[k].start_atom; h->pep_end[k] = b->prot[k].end_atom;
+        h->pep_aa_start[k] = b->prot[k].start_aa; h->pep_aa_end[k] = b->prot[k].end_aa;
+        for (int n = b->prot[k].start_atom; n <= b->prot[k].end_atom; n++)
+            h->pep_mass[k] += strncmp(b->atom[n].name, "H", 1) == 0 ? 1 : b->atom[n].mass;
+    }
+    memcpy(h->method, p->force_field, strnlen(p->force_field, sizeof h->method - 1));
     memcpy(h->con_step_d, b->conpool.d, sizeof(double) * ns);
     memcpy(h->con_step_e, b->conpool.e, sizeof(double) * ns);
     memcpy(h->con_step_acc, b->conpool.acc, sizeof(double) * ns);
@@ -1077,6 +1114,17 @@ sdmd_system *sdmd_host_view(sdmd_host_system *h) { return h ? &h->sys : NULL; }
 const char *sdmd_host_atom_names(const sdmd_host_system *h) { return h ? h->names : NULL; }
 const char *sdmd_host_residue_names(const sdmd_host_system *h) { return h ? h->resnames : NULL; }
 
+void sdmd_host_static_info(const sdmd_host_system *h, sdmd_host_static *o) {
+    o->n_aa = h->n_aa; o->n_prot = h->n_prot;
+    o->names = h->names; o->resnames = h->resnames; o->ext = h->ext;
+    o->aa_name = h->aa_name; o->aa_type = h->aa_type; o->aa_start = h->aa_start; o->aa_end = h->aa_end;
+    o->aa_prot = h->aa_prot; o->aa_mass = h->aa_mass;
+    o->pep_start = h->pep_start; o->pep_end = h->pep_end; o->pep_aa_start = h->pep_aa_start;
+    o->pep_aa_end = h->pep_aa_end; o->pep_mass = h->pep_mass;
+    o->method = h->method;
+    o->mass0 = h->mass; o->type0 = h->type;
+}
+
 void sdmd_host_free(sdmd_host_system *h) {
     if (!h) return;
     void *ptrs[] = {h->mass, h->x, h->y, h->z, h->vx, h->vy, h->vz, h->ev_time, h->ev_potential, h->protein, h->aanum,
@@ -1085,7 +1133,9 @@ void sdmd_host_free(sdmd_host_system *h) {
                     h->con_dmin, h->con_dmax, h->con_step_d, h->con_step_e, h->con_step_acc, h->pair_dmin, h->pair_dmax,
                     h->pair_step_d, h->pair_step_e, h->pair_step_acc, h->pair_step_off, h->pair_step_n, h->cx, h->cy,
                     h->cz, h->type, h->hb_bond, h->hb_itype, h->nb_partner, h->nb_status, h->nb_pnum, h->ev_partner,
-                    h->ev_type, h->ev_sub, h->cell_list, h->ev_counter, h->ev_pcounter, h->names, h->resnames};
+                    h->ev_type, h->ev_sub, h->cell_list, h->ev_counter, h->ev_pcounter, h->names, h->resnames,
+                    h->ext, h->aa_name, h->aa_type, h->aa_start, h->aa_end, h->aa_prot, h->aa_mass, h->pep_start,
+                    h->pep_end, h->pep_aa_start, h->pep_aa_end, h->pep_mass};
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
     free(h);
 }

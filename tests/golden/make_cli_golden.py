@@ -7,7 +7,8 @@ Needs the reference's executable built by the oracle recipe
 its own main, -DDEBUG_RANDOM for the fixed seed).  The run: the ALA x 10 chain of
 the ala10_nvt fixture, Andersen NVT, Time 40 with Dump_Rate 10, and the optional
 outputs -pot -kin -tem -HBn.  Kept: the inputs (in/parameter.txt, in/sys.gro; the
-force-field library is the package's) and the text outputs (expected/).
+force-field library is the package's) and the outputs (expected/): the text files
+and the last checkpoint.
 
 Usage: python tests/golden/make_cli_golden.py
 """
@@ -23,7 +24,7 @@ REPO = os.path.dirname(os.path.dirname(HERE))
 EXE = os.path.join(REPO, "oracle", "_ref", "sDMD")
 CASE = os.path.join(HERE, "cli_ala10")
 FLAGS = ["-pot", "-kin", "-tem", "-HBn"]
-OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt"]
+OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt", "savedData.dat"]
 
 
 def parameters(text, time, dump):

@@ -6,7 +6,9 @@ tests/golden/cli_ala10 holds a whole run of the reference's unmodified sDMD
 and -pot -kin -tem -HBn.  sdmd-gb300 runs the same command line on the same
 inputs with the same seed (SDMD_DEBUG_RANDOM), its event loop on the GPU, and
 every output file must equal the reference's byte for byte: the trajectory, the
-connection map, the energies, the temperature and the HB counts at every dump.
+connection map, the energies, the temperature and the HB counts at every dump,
+and the last checkpoint (savedData.dat, but for the bytes the reference leaves
+undefined, as tests/test_saved_data.py compares them).
 """
 import os
 import shutil
@@ -39,3 +41,7 @@ def test_executable_writes_the_reference_outputs(tmp_path):
         mine = (outd / name).read_bytes()
         ref = open(os.path.join(CASE, "expected", name), "rb").read()
         assert mine == ref, f"{name} differs from the reference's"
+    from tests.test_saved_data import differing_defined_bytes
+    bad = differing_defined_bytes((outd / "savedData.dat").read_bytes(),
+                                  open(os.path.join(CASE, "expected", "savedData.dat"), "rb").read())
+    assert len(bad) == 0, f"savedData.dat differs at {bad[:5]}"

@@ -154,3 +154,69 @@ def test_checkpoint_read_write_continue(case, k, m, n):
     assert t1 == s2.time and all(c1[c] == s2.counters[c] for c in COUNTERS)
     for hh in (h, h2):
         host_lib().sdmd_saved_free(hh)
+
+
+def differing_defined_bytes(mine, ref):
+    """Offsets where two savedData.dat images differ, leaving out the bytes the
+    reference's SaveDAT writes without defining them: the atom records' pointer
+    fields (PropertyStr.bond / .constr: its heap addresses), residue and peptide
+    record 0 (malloc'd), the residue records' bytes past the name, and velocity[0]
+    of atoms that had a thermostat event (ThermostatEvent copies an uninitialised
+    speed[0], src/Events.c:397-418)."""
+    if len(mine) != len(ref):
+        return np.array([min(len(mine), len(ref))])
+    n_atoms, n_prot, n_aa = np.frombuffer(ref[:12], np.int32)
+    aa0 = 12 + 4 * (n_atoms + 1) ** 2 + 48 + 20 + 32
+    at = aa0 + 32 * (n_aa + 1) + 24 * (n_prot + 1)
+    mask = np.ones(len(ref), bool)
+    mask[aa0: aa0 + 32] = False
+    mask[aa0 + 32 * (n_aa + 1): aa0 + 32 * (n_aa + 1) + 24] = False
+    for k in range(n_aa + 1):
+        mask[aa0 + 32 * k + 4: aa0 + 32 * k + 8] = False
+    for i in range(n_atoms + 1):
+        mask[at + 312 * i + 120: at + 312 * i + 136] = False
+        mask[at + 312 * i + 136 + 48: at + 312 * i + 136 + 56] = False
+    a, b = np.frombuffer(mine, np.uint8), np.frombuffer(ref, np.uint8)
+    return np.nonzero((a != b) & mask)[0]
+
+
+@pytest.mark.parametrize("case,k", [("ala10_nvt", 2000), ("sheet2", 20000), ("ala10_cyl", 3000)])
+def test_new_run_template_writes_the_reference_file(case, k):
+    """A new run's checkpoint without a file to start from: sdmd_saved_new builds
+    the template from the system the host library built (same inputs and seed),
+    and writing the reference's state after K events with it gives the file the
+    reference's own SaveDAT wrote, byte for byte but for what the reference leaves
+    undefined: the atom records' two pointer fields (its heap addresses), residue
+    and peptide record 0, the residue records' bytes past the name and the unused
+    velocity[0] after a thermostat event."""
+    from sdmd_gb300.host import build_system
+    from sdmd_gb300.system import System, sdmd_system
+    work, ind, outd = case_dir(case)
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", f"{case}.npz"))
+    a_ref, c_ref, t_ref = in_child(_child_new_run_and_save, ind, outd, k)
+    ref = open(os.path.join(outd, "savedData.dat"), "rb").read()
+    seed = int(d["pre/seed"][0])
+    built = build_system(ind, gro_text=bytes(d["meta/gro"]).decode(), seed=seed)
+    # the template comes from the host library's own handle of the same build
+    from sdmd_gb300 import host as H
+    L = host_lib()
+    L.sdmd_saved_new.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_void_p), C.c_char_p, C.c_int]
+    params = H.read_parameters(os.path.join(ind, "parameter.txt"))
+    hs = C.c_void_p()
+    err = C.create_string_buffer(512)
+    assert H.lib().sdmd_build_system_gro_text(ind.encode(), bytes(d["meta/gro"]), C.byref(params), seed, 20000,
+                                               C.byref(hs), err, 512) == 0, err.value
+    tpl = C.c_void_p()
+    assert L.sdmd_saved_new(hs, C.byref(params), seed, C.byref(tpl), err, 512) == 0, err.value
+    s = System()
+    s.a, s.scal, s.counters, s.time = dict(built.a), dict(built.scal), dict(c_ref), t_ref
+    for key in DYN:
+        s.a[key] = a_ref[key]
+    s.rng = built.rng.copy()
+    path = os.path.join(work, "new_template.dat")
+    write_saved(path, tpl, s)
+    mine = open(path, "rb").read()
+    bad = differing_defined_bytes(mine, ref)
+    assert len(bad) == 0, f"{len(bad)} bytes differ, first at offset {bad[0]}"
+    L.sdmd_saved_free(tpl)
+    H.lib().sdmd_host_free(hs)
