@@ -5,7 +5,8 @@
  *
  * The reference's command line (InputData, src/Initialization.c:63-256), inputs
  * and outputs: parameter.txt, the coordinate file and Library_<ff>/ from the input
- * directory (a "continue" run also reads savedData.dat there), the system built
+ * directory (a "continue" run also reads savedData.dat from the output directory,
+ * as ReadBreakPoint does), the system built
  * as the reference's set-up builds it (src/SGThread.c:21-46), the event loop of
  * SingleThreadRun (src/SGThread.c:67-155) on the engine (FP32 screen, FP64 refine,
  * eager advance: the reference's events exactly), and at every dump -- after the
@@ -83,7 +84,7 @@ int main(int argc, const char *argv[]) {
     snprintf(pb.continue_mode, sizeof pb.continue_mode, "new");
     sdmd_saved *saved = NULL;
     if (!is_new) {
-        snprintf(path, sizeof path, "%s/%s", cli.datadir, cli.saved_in);
+        snprintf(path, sizeof path, "%s/%s", cli.savedir, cli.saved_in);   /* ReadBreakPoint reads the output folder's */
         if (sdmd_saved_read(path, &saved, err, sizeof err) != SDMD_OK) {
             fprintf(stderr, "!!ERROR!!: %s\n", err);
             return 1;
@@ -107,8 +108,17 @@ int main(int argc, const char *argv[]) {
         fprintf(stderr, "!!ERROR!!: %s\n", err);
         return 1;
     }
-    /* a new run's checkpoint: its static records as the reference's set-up leaves them */
-    if (!saved && sdmd_saved_new(hs, &p, seed, &saved, err, sizeof err) != SDMD_OK) {
+    /* the checkpoint this run writes: static records from the built system, the
+       run's own Time, Dump_Rate and cut-off, and the seed the run was started with
+       (a continue run keeps the one its checkpoint holds) */
+    uint32_t file_seed = seed;
+    if (saved) {
+        sdmd_saved_header hd;
+        sdmd_saved_info(saved, &hd);
+        file_seed = hd.seed;
+    }
+    sdmd_saved *tpl = NULL;
+    if (sdmd_saved_new(hs, &p, file_seed, &tpl, err, sizeof err) != SDMD_OK) {
         fprintf(stderr, "!!ERROR!!: %s\n", err);
         return 1;
     }
@@ -171,10 +181,8 @@ int main(int argc, const char *argv[]) {
             if (sdmd_write_cnt(f, app, sys) != SDMD_OK) { fprintf(stderr, "!!ERROR!!: %s\n", f); return 1; }
             if (cli.out_on[SDMD_OUT_HBN]) { out_path(f, sizeof f, &cli, SDMD_OUT_HBN); sdmd_write_hbn(f, app, sys); }
             if (cli.out_on[SDMD_OUT_PDB]) { out_path(f, sizeof f, &cli, SDMD_OUT_PDB); sdmd_write_pdb(f, app, sys, names, resnames); }
-            if (saved) {
-                out_path(f, sizeof f, &cli, SDMD_OUT_SAVED);
-                if (sdmd_saved_write(f, saved, sys, err, sizeof err) != SDMD_OK) { fprintf(stderr, "!!ERROR!!: %s\n", err); return 1; }
-            }
+            out_path(f, sizeof f, &cli, SDMD_OUT_SAVED);
+            if (sdmd_saved_write(f, tpl, sys, err, sizeof err) != SDMD_OK) { fprintf(stderr, "!!ERROR!!: %s\n", err); return 1; }
             frames++;
             outputrecord += p.dump_rate;
         }
@@ -201,5 +209,6 @@ int main(int argc, const char *argv[]) {
     sdmd_gpu_destroy(h);
     sdmd_host_free(hs);
     if (saved) sdmd_saved_free(saved);
+    sdmd_saved_free(tpl);
     return 0;
 }

@@ -8,7 +8,8 @@ its own main, -DDEBUG_RANDOM for the fixed seed).  The run: the ALA x 10 chain o
 the ala10_nvt fixture, Andersen NVT, Time 40 with Dump_Rate 10, and the optional
 outputs -pot -kin -tem -HBn.  Kept: the inputs (in/parameter.txt, in/sys.gro; the
 force-field library is the package's) and the outputs (expected/): the text files
-and the last checkpoint.
+and the last checkpoint.  cli_ala10_continue/ is the continue run from that
+checkpoint to Time 70 (its in/ also holds the checkpoint it reads).
 
 Usage: python tests/golden/make_cli_golden.py
 """
@@ -23,6 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 EXE = os.path.join(REPO, "oracle", "_ref", "sDMD")
 CASE = os.path.join(HERE, "cli_ala10")
+CONT = os.path.join(HERE, "cli_ala10_continue")
 FLAGS = ["-pot", "-kin", "-tem", "-HBn"]
 OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt", "savedData.dat"]
 
@@ -35,6 +37,23 @@ def parameters(text, time, dump):
         elif line.startswith("Dump_Rate"):
             lines[k] = f"Dump_Rate          {dump}"
     return "\n".join(lines) + "\n"
+
+
+def run_case(ind, case_dir, extra_inputs=()):
+    outd = tempfile.mkdtemp(prefix="sdmd_cli_out_")
+    for name in extra_inputs:   # a continue run reads its checkpoint from the output folder
+        shutil.copy(os.path.join(ind, name), os.path.join(outd, name))
+    subprocess.run([EXE, "-i", ind, "-o", outd, "-f", "sys.gro", *FLAGS], check=True, stdout=subprocess.DEVNULL,
+                   timeout=600)
+    os.makedirs(os.path.join(case_dir, "in"), exist_ok=True)
+    os.makedirs(os.path.join(case_dir, "expected"), exist_ok=True)
+    for name in ("parameter.txt", "sys.gro", *extra_inputs):
+        shutil.copy(os.path.join(ind, name), os.path.join(case_dir, "in", name))
+    for name in OUTPUTS:
+        shutil.copy(os.path.join(outd, name), os.path.join(case_dir, "expected", name))
+    with open(os.path.join(case_dir, "expected", "flags.txt"), "w") as f:
+        f.write(" ".join(FLAGS) + "\n")
+    shutil.rmtree(outd)
 
 
 def main():
@@ -51,18 +70,14 @@ def main():
         f.write(param)
     with open(os.path.join(ind, "sys.gro"), "wb") as f:
         f.write(bytes(d["meta/gro"]))
-    subprocess.run([EXE, "-i", ind, "-o", outd, "-f", "sys.gro", *FLAGS], check=True, stdout=subprocess.DEVNULL,
-                   timeout=600)
-    os.makedirs(os.path.join(CASE, "in"), exist_ok=True)
-    os.makedirs(os.path.join(CASE, "expected"), exist_ok=True)
-    shutil.copy(os.path.join(ind, "parameter.txt"), os.path.join(CASE, "in", "parameter.txt"))
-    shutil.copy(os.path.join(ind, "sys.gro"), os.path.join(CASE, "in", "sys.gro"))
-    for name in OUTPUTS:
-        shutil.copy(os.path.join(outd, name), os.path.join(CASE, "expected", name))
-    with open(os.path.join(CASE, "expected", "flags.txt"), "w") as f:
-        f.write(" ".join(FLAGS) + "\n")
+    run_case(ind, CASE)
+    # the continue run: the new run's checkpoint, Time 70 (> currenttime + Dump_Rate)
+    shutil.copy(os.path.join(CASE, "expected", "savedData.dat"), os.path.join(ind, "savedData.dat"))
+    with open(os.path.join(ind, "parameter.txt"), "w") as f:
+        f.write(parameters(param, 70, 10.0).replace("new", "continue", 1))
+    run_case(ind, CONT, ("savedData.dat",))
     shutil.rmtree(work)
-    print("wrote", CASE)
+    print("wrote", CASE, CONT)
 
 
 if __name__ == "__main__":

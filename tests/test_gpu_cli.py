@@ -8,7 +8,9 @@ inputs with the same seed (SDMD_DEBUG_RANDOM), its event loop on the GPU, and
 every output file must equal the reference's byte for byte: the trajectory, the
 connection map, the energies, the temperature and the HB counts at every dump,
 and the last checkpoint (savedData.dat, but for the bytes the reference leaves
-undefined, as tests/test_saved_data.py compares them).
+undefined, as tests/test_saved_data.py compares them).  cli_ala10_continue is the
+reference's continue run from that checkpoint (read from the output folder, as
+ReadBreakPoint does) to Time 70.
 """
 import os
 import shutil
@@ -19,18 +21,21 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CASE = os.path.join(REPO, "tests", "golden", "cli_ala10")
 OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt"]
 
 
-def test_executable_writes_the_reference_outputs(tmp_path):
+@pytest.mark.parametrize("case", ["cli_ala10", "cli_ala10_continue"])
+def test_executable_writes_the_reference_outputs(tmp_path, case):
     import __graft_entry__ as G
     G.build()
     from sdmd_gb300 import build
+    CASE = os.path.join(REPO, "tests", "golden", case)
     ind, outd = tmp_path / "in", tmp_path / "out"
     shutil.copytree(os.path.join(CASE, "in"), ind)
     shutil.copytree(os.path.join(REPO, "sdmd_gb300", "data", "Library_Ding"), ind / "Library_Ding")
     outd.mkdir()
+    if (ind / "savedData.dat").exists():      # a continue run's checkpoint
+        shutil.copy(ind / "savedData.dat", outd / "savedData.dat")
     flags = open(os.path.join(CASE, "expected", "flags.txt")).read().split()
     env = dict(os.environ, SDMD_DEBUG_RANDOM="1")
     r = subprocess.run([build.APP, "-i", str(ind), "-o", str(outd), "-f", "sys.gro", *flags], env=env,
