@@ -166,6 +166,8 @@ const char *sdmd_host_residue_names(const sdmd_host_system *h);
  * format byte for byte.  names8 / resnames8: 8-byte name records as above.
  *   sdmd_write_gro     out_trj.gro      SaveGRO           (src/DataSave.c:616-640)
  *   sdmd_write_pdb     out_pdb.pdb      SavePDB           (:588-613)
+ *   sdmd_write_xyz     out_xyz.xyz      SaveXYZ           (:488-505); timer is the
+ *                      run's start time as DisplayTime prints it (%Y_%m_%d_%H_%M_%S)
  *   sdmd_write_cnt     out_cnt.txt      SaveConnectionMap (:218-233): static bond /
  *                      constraint bits plus the formed hydrogen bonds' HB and
  *                      neighbour bits
@@ -176,6 +178,7 @@ const char *sdmd_host_residue_names(const sdmd_host_system *h);
  */
 int sdmd_write_gro(const char *path, int append, const sdmd_system *s, const char *names8, const char *resnames8);
 int sdmd_write_pdb(const char *path, int append, const sdmd_system *s, const char *names8, const char *resnames8);
+int sdmd_write_xyz(const char *path, int append, const sdmd_system *s, const char *names8, const char *timer);
 int sdmd_write_cnt(const char *path, int append, const sdmd_system *s);
 int sdmd_write_hbn(const char *path, int append, const sdmd_system *s);
 int sdmd_write_series(const char *path, int append, double time, double value);

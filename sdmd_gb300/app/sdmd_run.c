@@ -12,14 +12,16 @@
  * eager advance: the reference's events exactly), and at every dump -- after the
  * first executed event of each Dump_Rate interval, the first event of a new run
  * included -- the reference's outputs in its formats: out_trj.gro and
- * out_cnt.txt, out_pot/kin/tem.txt, out_HBn.txt and out_pdb.pdb when their flags
- * ask for them, and savedData.dat (its static records from the inputs, or from the
- * file a continue run started from).  The end-of-run statistics block is the
- * reference's (src/DMD.c:244-265).
+ * out_cnt.txt, out_pot/kin/tem.txt, out_HBn.txt and out_xyz.xyz when their flags
+ * ask for them (-pdb switches the xyz file on, as the reference's parser does),
+ * and savedData.dat (its static records from the inputs, or from the file a
+ * continue run started from).  A file already in the output folder is first
+ * renamed with the run's start time, as BackupFile does (src/DataSave.c:79-96).
+ * The end-of-run statistics block is the reference's (src/DMD.c:244-265).
  *
  * The random seed is time(NULL), as the reference's release build uses, or
  * 1575263273 (the reference's -DDEBUG_RANDOM seed) when SDMD_DEBUG_RANDOM is set.
- * out_log.txt, SysInfo.dat and out_xyz.xyz are not written.
+ * out_log.txt and SysInfo.dat are not written.
  */
 #include <stdint.h>
 #include <stdio.h>
@@ -37,6 +39,22 @@ static const char *const kDefaultOut[SDMD_CLI_NOUT] = {"savedData.dat", "out_trj
 static void out_path(char *buf, size_t len, const sdmd_cli *cli, int which) {
     const char *name = cli->out_name[which][0] ? cli->out_name[which] : kDefaultOut[which];
     snprintf(buf, len, "%s/%s", cli->savedir, name);
+}
+
+/* BackupFile / AssignName (src/DataSave.c:64-96): before an output's first write,
+   an existing file of that name becomes <name>@<start time><last 4 characters> */
+static void backup(const sdmd_cli *cli, int which, const char *timer) {
+    const char *name = cli->out_name[which][0] ? cli->out_name[which] : kDefaultOut[which];
+    char from[2400], to[2400], renamed[512];
+    snprintf(from, sizeof from, "%s/%s", cli->savedir, name);
+    FILE *f = fopen(from, "r");
+    if (!f) return;
+    fclose(f);
+    const size_t len = strlen(name);
+    if (len <= 4) return;
+    snprintf(renamed, sizeof renamed, "%.*s@%s%s", (int)(len - 4), name, timer, name + len - 4);
+    snprintf(to, sizeof to, "%s/%s", cli->savedir, renamed);
+    rename(from, to);
 }
 
 static int engine_fail(sdmd_gpu *h, int rc, const char *where) {
@@ -146,6 +164,11 @@ int main(int argc, const char *argv[]) {
     if ((rc = sdmd_gpu_create(sys, 1, &o, &h)) != SDMD_OK) return engine_fail(NULL, rc, "sdmd_gpu_create");
     if ((rc = sdmd_gpu_prepare(h, is_new ? 1 : 0)) != SDMD_OK) return engine_fail(h, rc, "sdmd_gpu_prepare");
 
+    char timer[30];   /* DisplayTime (src/ToolFunctions.c:314-322) */
+    {
+        const time_t now = time(NULL);
+        strftime(timer, sizeof timer, "%Y_%m_%d_%H_%M_%S", localtime(&now));
+    }
     const int64_t kNoLimit = (int64_t)1 << 40;
     double outputrecord = is_new ? 0 : sys->time + p.dump_rate;   /* src/DMD.c:31, src/SGThread.c:55 */
     int frames = 0;
@@ -165,6 +188,14 @@ int main(int argc, const char *argv[]) {
         if (at) {   /* SaveData for every marked file (src/SGThread.c:132-139) */
             const int app = frames > 0;
             char f[2400];
+            if (!app) {
+                static const int kMarked[] = {SDMD_OUT_TRJ, SDMD_OUT_POT, SDMD_OUT_KIN, SDMD_OUT_TEM, SDMD_OUT_CNT,
+                                              SDMD_OUT_HBN, SDMD_OUT_XYZ, SDMD_OUT_SAVED};
+                for (size_t q = 0; q < sizeof kMarked / sizeof kMarked[0]; q++)
+                    if (kMarked[q] == SDMD_OUT_TRJ || kMarked[q] == SDMD_OUT_CNT || kMarked[q] == SDMD_OUT_SAVED ||
+                        cli.out_on[kMarked[q]])
+                        backup(&cli, kMarked[q], timer);
+            }
             out_path(f, sizeof f, &cli, SDMD_OUT_TRJ);
             if (sdmd_write_gro(f, app, sys, names, resnames) != SDMD_OK) { fprintf(stderr, "!!ERROR!!: %s\n", f); return 1; }
             if (cli.out_on[SDMD_OUT_POT] || cli.out_on[SDMD_OUT_KIN] || cli.out_on[SDMD_OUT_TEM]) {
@@ -180,7 +211,7 @@ int main(int argc, const char *argv[]) {
             out_path(f, sizeof f, &cli, SDMD_OUT_CNT);
             if (sdmd_write_cnt(f, app, sys) != SDMD_OK) { fprintf(stderr, "!!ERROR!!: %s\n", f); return 1; }
             if (cli.out_on[SDMD_OUT_HBN]) { out_path(f, sizeof f, &cli, SDMD_OUT_HBN); sdmd_write_hbn(f, app, sys); }
-            if (cli.out_on[SDMD_OUT_PDB]) { out_path(f, sizeof f, &cli, SDMD_OUT_PDB); sdmd_write_pdb(f, app, sys, names, resnames); }
+            if (cli.out_on[SDMD_OUT_XYZ]) { out_path(f, sizeof f, &cli, SDMD_OUT_XYZ); sdmd_write_xyz(f, app, sys, names, timer); }
             out_path(f, sizeof f, &cli, SDMD_OUT_SAVED);
             if (sdmd_saved_write(f, tpl, sys, err, sizeof err) != SDMD_OK) { fprintf(stderr, "!!ERROR!!: %s\n", err); return 1; }
             frames++;

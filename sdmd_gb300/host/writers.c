@@ -5,7 +5,8 @@
  * Each call appends one frame to the named file (or starts it, append == 0), in
  * the reference's exact format: the trajectory (SaveGRO :616-640, SavePDB
  * :588-613), the connection map (SaveConnectionMap :218-233), the hydrogen-bond
- * counts (SaveHB :205-216) and the one-number-per-dump series of potential and
+ * counts (SaveHB :205-216), the xyz trajectory (SaveXYZ :488-505) and the
+ * one-number-per-dump series of potential and
  * kinetic energy and temperature (SavePot / SaveKin / SaveTemp :235-278).  The
  * energies are the caller's (sdmd_gpu_energies computes the reference's
  * CalPotenE / CalKinetE on the device); the writer only formats them.
@@ -47,6 +48,18 @@ int sdmd_write_gro(const char *path, int append, const sdmd_system *s, const cha
         fprintf(f, "%5i%-5s%5s%5i%8.3f%8.3f%8.3f%10.4f%10.4f%10.4f\n", s->aanum[i], name8(resnames8, i, r),
                 name8(names8, i, a), i, s->x[i] / 10, s->y[i] / 10, s->z[i] / 10, s->vx[i], s->vy[i], s->vz[i]);
     fprintf(f, "%10.5f%10.5f%10.5f\n", s->box[0] / 10, s->box[1] / 10, s->box[2] / 10);
+    return close_out(f);
+}
+
+int sdmd_write_xyz(const char *path, int append, const sdmd_system *s, const char *names8, const char *timer) {
+    if (!s || !names8) return SDMD_EINVAL;
+    FILE *f = open_out(path, append);
+    if (!f) return SDMD_EINVAL;
+    char a[8];
+    fprintf(f, "%i\n", s->n_atoms);
+    fprintf(f, "Model %s\n", timer ? timer : "");
+    for (int i = 1; i <= s->n_atoms; i++)
+        fprintf(f, "%-8s%16.6lf%16.6lf%16.6lf\n", name8(names8, i, a), s->x[i], s->y[i], s->z[i]);
     return close_out(f);
 }
 

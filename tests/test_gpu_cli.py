@@ -8,7 +8,9 @@ inputs with the same seed (SDMD_DEBUG_RANDOM), its event loop on the GPU, and
 every output file must equal the reference's byte for byte: the trajectory, the
 connection map, the energies, the temperature and the HB counts at every dump,
 and the last checkpoint (savedData.dat, but for the bytes the reference leaves
-undefined, as tests/test_saved_data.py compares them).  cli_ala10_continue is the
+undefined, as tests/test_saved_data.py compares them); an output file already in
+the folder is kept under the run's start time, as the reference's BackupFile
+does.  cli_ala10_continue is the
 reference's continue run from that checkpoint (read from the output folder, as
 ReadBreakPoint does) to Time 70.
 """
@@ -36,12 +38,15 @@ def test_executable_writes_the_reference_outputs(tmp_path, case):
     outd.mkdir()
     if (ind / "savedData.dat").exists():      # a continue run's checkpoint
         shutil.copy(ind / "savedData.dat", outd / "savedData.dat")
+    (outd / "out_trj.gro").write_text("an earlier run\n")   # kept under the run's start time
     flags = open(os.path.join(CASE, "expected", "flags.txt")).read().split()
     env = dict(os.environ, SDMD_DEBUG_RANDOM="1")
     r = subprocess.run([build.APP, "-i", str(ind), "-o", str(outd), "-f", "sys.gro", *flags], env=env,
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     assert "Finished!" in r.stdout
+    kept = [p for p in outd.iterdir() if p.name.startswith("out_trj@") and p.name.endswith(".gro")]
+    assert len(kept) == 1 and kept[0].read_text() == "an earlier run\n"     # BackupFile
     for name in OUTPUTS:
         mine = (outd / name).read_bytes()
         ref = open(os.path.join(CASE, "expected", name), "rb").read()

@@ -5,8 +5,8 @@ an engine state.  Here the reference's unmodified sources (oracle/_ref, with the
 bridge) set up a golden case, run their own loop, and write their outputs with
 SaveData (src/DataSave.c); the bridge then fills an sdmd_system from that same
 state, and the host library's writers must produce the same bytes: the
-trajectory (.gro, .pdb), the connection map (with the hydrogen bonds the run
-formed), the HB counts and the energy / temperature series (two frames each,
+trajectory (.gro, .pdb, .xyz), the connection map (with the hydrogen bonds the
+run formed), the HB counts and the energy / temperature series (two frames each,
 appended).
 """
 import ctypes as C
@@ -20,9 +20,9 @@ from tests.test_ref_bridge import LIB, REPO, _bridge, _fill, case_dir, in_child
 pytestmark = pytest.mark.skipif(not os.path.exists(LIB),
                                 reason="the reference's sources are not here (oracle/_ref not built)")
 
-TRJ, POT, KIN, TEM, CNT, HBN, PDB = 0, 1, 2, 3, 4, 5, 7   # enum FileType (src/DMD.h:212-228)
+TRJ, POT, KIN, TEM, CNT, HBN, XYZ, PDB = 0, 1, 2, 3, 4, 5, 6, 7   # enum FileType (src/DMD.h:212-228)
 NAMES = {TRJ: "out_trj.gro", POT: "out_pot.txt", KIN: "out_kin.txt", TEM: "out_tem.txt", CNT: "out_cnt.txt",
-         HBN: "out_HBn.txt", PDB: "out_pdb.pdb"}
+         HBN: "out_HBn.txt", XYZ: "out_xyz.xyz", PDB: "out_pdb.pdb"}
 
 
 def _child_frames(case, runs, q):
@@ -39,7 +39,7 @@ def _child_frames(case, runs, q):
         frames = []
         for n in runs:
             L.bd_run(n)
-            for t in (TRJ, POT, KIN, TEM, CNT, HBN, PDB):
+            for t in (TRJ, POT, KIN, TEM, CNT, HBN, XYZ, PDB):
                 L.bd_save_type(t)
             s = _fill(L)
             frames.append((s.a, s.scal, s.counters, s.time, L.bd_potential(), L.bd_kinetic(), L.bd_temperature()))
@@ -54,7 +54,7 @@ def _host_writers():
     from sdmd_gb300.system import sdmd_system
     L = lib()
     P = C.POINTER(sdmd_system)
-    for f in ("sdmd_write_gro", "sdmd_write_pdb"):
+    for f in ("sdmd_write_gro", "sdmd_write_pdb", "sdmd_write_xyz"):
         getattr(L, f).argtypes = [C.c_char_p, C.c_int, P, C.c_char_p, C.c_char_p]
     for f in ("sdmd_write_cnt", "sdmd_write_hbn"):
         getattr(L, f).argtypes = [C.c_char_p, C.c_int, P]
@@ -79,6 +79,7 @@ def test_writers_match_the_reference(case, runs, tmp_path):
         app = 1 if k else 0
         assert L.sdmd_write_gro(out[TRJ], app, st, named.names, named.resnames) == 0
         assert L.sdmd_write_pdb(out[PDB], app, st, named.names, named.resnames) == 0
+        assert L.sdmd_write_xyz(out[XYZ], app, st, named.names, b"") == 0   # no log written: the timer is empty
         assert L.sdmd_write_cnt(out[CNT], app, st) == 0
         assert L.sdmd_write_hbn(out[HBN], app, st) == 0
         for t, v in ((POT, pot), (KIN, kin), (TEM, tem)):
