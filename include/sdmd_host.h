@@ -182,6 +182,11 @@ int sdmd_write_xyz(const char *path, int append, const sdmd_system *s, const cha
 int sdmd_write_cnt(const char *path, int append, const sdmd_system *s);
 int sdmd_write_hbn(const char *path, int append, const sdmd_system *s);
 int sdmd_write_series(const char *path, int append, double time, double value);
+/*   sdmd_write_log     out_log.txt      SaveLog (src/DataSave.c:333-462): the run's
+ *                      configuration; timer as for sdmd_write_xyz, old_time the
+ *                      run's start time, wall_dyn_size / rate the -Wsz / -Wrt values */
+int sdmd_write_log(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,
+                   double old_time, uint32_t seed, double wall_dyn_size, double wall_dyn_rate);
 
 #ifdef __cplusplus
 }

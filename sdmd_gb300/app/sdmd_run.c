@@ -17,11 +17,12 @@
  * and savedData.dat (its static records from the inputs, or from the file a
  * continue run started from).  A file already in the output folder is first
  * renamed with the run's start time, as BackupFile does (src/DataSave.c:79-96).
- * The end-of-run statistics block is the reference's (src/DMD.c:244-265).
+ * out_log.txt is written at the start, as Prepare's SaveLog does.  The end-of-run
+ * statistics block is the reference's (src/DMD.c:244-265).
  *
  * The random seed is time(NULL), as the reference's release build uses, or
  * 1575263273 (the reference's -DDEBUG_RANDOM seed) when SDMD_DEBUG_RANDOM is set.
- * out_log.txt and SysInfo.dat are not written.
+ * SysInfo.dat is not written.
  */
 #include <stdint.h>
 #include <stdio.h>
@@ -168,6 +169,15 @@ int main(int argc, const char *argv[]) {
     {
         const time_t now = time(NULL);
         strftime(timer, sizeof timer, "%Y_%m_%d_%H_%M_%S", localtime(&now));
+    }
+    {   /* SaveLog in Prepare (src/SGThread.c:27-28) */
+        char f[2400];
+        backup(&cli, SDMD_OUT_LOG, timer);
+        out_path(f, sizeof f, &cli, SDMD_OUT_LOG);
+        if (sdmd_write_log(f, hs, &p, timer, sys->time, file_seed, cli.wall_dyn_size, cli.wall_dyn_rate) != SDMD_OK) {
+            fprintf(stderr, "!!ERROR!!: %s\n", f);
+            return 1;
+        }
     }
     const int64_t kNoLimit = (int64_t)1 << 40;
     double outputrecord = is_new ? 0 : sys->time + p.dump_rate;   /* src/DMD.c:31, src/SGThread.c:55 */

@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include "sdmd_host.h"
+#include "host_static.h"
 
 #define BOND_CONNECT 0x01       /* connection-map bits (src/DMD.h:59-63) */
 #define CONSTRAINT_CONNECT 0x02
@@ -151,6 +152,61 @@ int sdmd_write_hbn(const char *path, int append, const sdmd_system *s) {
     FILE *f = open_out(path, append);
     if (!f) return SDMD_EINVAL;
     fprintf(f, "%5.2lf%10i%10i\n", s->time, s->counters.hb_formed, s->counters.alpha_hb_formed);
+    return close_out(f);
+}
+
+/* SaveLog (src/DataSave.c:333-462) for the engine's configurations: no coarse
+   graining, flow, obstruction, tunnel or column obstacle, no dynamic wall */
+int sdmd_write_log(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,
+                   double old_time, uint32_t seed, double wall_dyn_size, double wall_dyn_rate) {
+    if (!path || !h || !p) return SDMD_EINVAL;
+    const sdmd_system *s = sdmd_host_view((sdmd_host_system *)h);
+    sdmd_host_static st;
+    sdmd_host_static_info(h, &st);
+    FILE *f = fopen(path, "w");
+    if (!f) return SDMD_EINVAL;
+    fprintf(f, "#Log file at %s\n", timer ? timer : "");
+    fprintf(f, "System:\n");
+    fprintf(f, "Protein Num         = %i\n", st.n_prot);
+    fprintf(f, "Protein Seq         = \n");
+    for (int k = 1; k <= st.n_prot; k++) {
+        fprintf(f, "                    ");
+        for (int n = st.pep_aa_start[k]; n <= st.pep_aa_end[k]; n++) fprintf(f, "%5s", st.aa_name + 8 * (size_t)n);
+        fprintf(f, "\n");
+    }
+    fprintf(f, "OldTime             = %-5.2lf\n", old_time);
+    fprintf(f, "TargetTime          = %-5.2lf\n", p->time);
+    fprintf(f, "TargetTemperature   = %-5.2lf\n", s->temperature);
+    fprintf(f, "OutputRate          = %-5.2lf\n", p->dump_rate);
+    fprintf(f, "CutOffR             = %-5.2lf\n", p->cutoff);
+    fprintf(f, "Method              = %s\n", p->force_field);
+    fprintf(f, "ThermostatType      = %s\n", p->thermostat);
+    fprintf(f, "ThermostatParameter = %-5.3lf\n", p->thermo_freq);
+    fprintf(f, "CGModel             = %s, %s\n", p->cg, p->cg);
+    fprintf(f, "WallExist           = %s\n", p->wall_exist);
+    fprintf(f, "WallType            = %s\n", p->wall_type);
+    fprintf(f, "WallDyn             = %s\n", p->wall_dyn);
+    fprintf(f, "WallDynSize         = %-5.2lf\n", wall_dyn_size);
+    fprintf(f, "WallDynRate         = %-5.2lf\n", wall_dyn_rate);
+    fprintf(f, "OrigBoxSize         = CurtBoxSize\n");
+    fprintf(f, "CurtBoxSize         = %-8.2lf%-8.2lf%-8.2lf\n", s->box[0], s->box[1], s->box[2]);
+    fprintf(f, "FlowType            = %-5i\n", 0);
+    fprintf(f, "                      No flow.\n");
+    fprintf(f, "Obstruct            = %-5i\n", 0);
+    fprintf(f, "                      No obstruction.\n");
+    fprintf(f, "Tunnel              = %-5i\n", 0);
+    fprintf(f, "                      No tunnel.\n");
+    fprintf(f, "ColumnObstacles     = %-5i\n", 0);
+    fprintf(f, "                      No column.\n");
+    fprintf(f, "RandomSeed          = %i\n", (int)seed);
+    /* REMDInfo's initializer (src/DMD.c:126-132): a run without -REMD */
+    fprintf(f, "REMDPortNum         = %i\n", -1);
+    fprintf(f, "REMDTemperature     = %.2lf\n", -1.0);
+    fprintf(f, "REMDTempSeq         = %i\n", -1);
+    fprintf(f, "REMDOutputRate      = %i\n", 1000);
+    fprintf(f, "REMDServerName      = %s\n", "");
+    fprintf(f, "REMDExtraName       = %s\n", "");
+    fprintf(f, "\n");
     return close_out(f);
 }
 

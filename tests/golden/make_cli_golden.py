@@ -26,7 +26,8 @@ EXE = os.path.join(REPO, "oracle", "_ref", "sDMD")
 CASE = os.path.join(HERE, "cli_ala10")
 CONT = os.path.join(HERE, "cli_ala10_continue")
 FLAGS = ["-pot", "-kin", "-tem", "-HBn"]
-OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt", "savedData.dat"]
+OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt", "savedData.dat",
+           "out_log.txt"]
 
 
 def parameters(text, time, dump):

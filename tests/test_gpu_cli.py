@@ -8,7 +8,8 @@ inputs with the same seed (SDMD_DEBUG_RANDOM), its event loop on the GPU, and
 every output file must equal the reference's byte for byte: the trajectory, the
 connection map, the energies, the temperature and the HB counts at every dump,
 and the last checkpoint (savedData.dat, but for the bytes the reference leaves
-undefined, as tests/test_saved_data.py compares them); an output file already in
+undefined, as tests/test_saved_data.py compares them) and the log (but for its
+first line, the start time); an output file already in
 the folder is kept under the run's start time, as the reference's BackupFile
 does.  cli_ala10_continue is the
 reference's continue run from that checkpoint (read from the output folder, as
@@ -51,6 +52,8 @@ def test_executable_writes_the_reference_outputs(tmp_path, case):
         mine = (outd / name).read_bytes()
         ref = open(os.path.join(CASE, "expected", name), "rb").read()
         assert mine == ref, f"{name} differs from the reference's"
+    mine, ref = (outd / "out_log.txt").read_text().splitlines(), open(os.path.join(CASE, "expected", "out_log.txt")).read().splitlines()
+    assert mine[0].startswith("#Log file at ") and mine[1:] == ref[1:]   # the first line is the start time
     from tests.test_saved_data import differing_defined_bytes
     bad = differing_defined_bytes((outd / "savedData.dat").read_bytes(),
                                   open(os.path.join(CASE, "expected", "savedData.dat"), "rb").read())

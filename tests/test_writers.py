@@ -20,7 +20,7 @@ from tests.test_ref_bridge import LIB, REPO, _bridge, _fill, case_dir, in_child
 pytestmark = pytest.mark.skipif(not os.path.exists(LIB),
                                 reason="the reference's sources are not here (oracle/_ref not built)")
 
-TRJ, POT, KIN, TEM, CNT, HBN, XYZ, PDB = 0, 1, 2, 3, 4, 5, 6, 7   # enum FileType (src/DMD.h:212-228)
+TRJ, POT, KIN, TEM, CNT, HBN, XYZ, PDB, LGF = 0, 1, 2, 3, 4, 5, 6, 7, 8   # enum FileType (src/DMD.h:212-228)
 NAMES = {TRJ: "out_trj.gro", POT: "out_pot.txt", KIN: "out_kin.txt", TEM: "out_tem.txt", CNT: "out_cnt.txt",
          HBN: "out_HBn.txt", XYZ: "out_xyz.xyz", PDB: "out_pdb.pdb"}
 
@@ -90,3 +90,39 @@ def test_writers_match_the_reference(case, runs, tmp_path):
     if case == "sheet2":
         assert frames[-1][2]["hb_formed"] > 0          # the map carries formed hydrogen bonds
         assert b" 4 " in ref_files[CNT] or b" 5 " in ref_files[CNT] or b" 12 " in ref_files[CNT]
+
+
+def _child_log(case, q):
+    try:
+        work, ind, outd = case_dir(case)
+        L = _bridge(ind, outd)
+        L.bd_save_type.argtypes = [C.c_int]
+        L.bd_save_type(LGF)                           # SaveLog, as Prepare() calls it
+        q.put(("ok", open(os.path.join(outd, "out_log.txt"), "rb").read(), ind))
+    except Exception as e:
+        q.put(("error", repr(e)))
+
+
+@pytest.mark.parametrize("case", ["ala10_nvt", "sheet2", "ala10_cyl", "mixed6"])
+def test_log_matches_the_reference(case, tmp_path):
+    """out_log.txt from the host library equals the reference's SaveLog output
+    line for line after the first, which carries the wall-clock time."""
+    from sdmd_gb300 import host as H
+    ref, ind = in_child(_child_log, case)
+    d = np.load(os.path.join(REPO, "tests", "golden", f"{case}.npz"))
+    L = H.lib()
+    L.sdmd_write_log.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_double, C.c_uint32, C.c_double,
+                                 C.c_double]
+    params = H.read_parameters(os.path.join(ind, "parameter.txt"))
+    seed = int(d["pre/seed"][0])
+    hs = C.c_void_p()
+    err = C.create_string_buffer(512)
+    assert L.sdmd_build_system_gro_text(ind.encode(), bytes(d["meta/gro"]), C.byref(params), seed, 20000, C.byref(hs),
+                                        err, 512) == 0, err.value
+    path = tmp_path / "out_log.txt"
+    assert L.sdmd_write_log(str(path).encode(), hs, C.byref(params), b"2000_01_01_00_00_00", 0.0, seed, 0.0, 0.0) == 0
+    L.sdmd_host_free(hs)
+    mine = path.read_bytes().split(b"\n")
+    theirs = ref.split(b"\n")
+    assert mine[0] == b"#Log file at 2000_01_01_00_00_00"
+    assert mine[1:] == theirs[1:]
