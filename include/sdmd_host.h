@@ -187,6 +187,11 @@ int sdmd_write_series(const char *path, int append, double time, double value);
  *                      run's start time, wall_dyn_size / rate the -Wsz / -Wrt values */
 int sdmd_write_log(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,
                    double old_time, uint32_t seed, double wall_dyn_size, double wall_dyn_rate);
+/*   sdmd_write_sysinfo SysInfo.dat      SaveSysInfo (src/DataSave.c:280-331): the
+ *                      system's static records for the analysis tools, from the built
+ *                      system; the reference's heap addresses in its pointer fields
+ *                      are written as 1 where it has a link (readers test them for NULL) */
+int sdmd_write_sysinfo(const char *path, const sdmd_host_system *h);
 
 #ifdef __cplusplus
 }

@@ -17,12 +17,12 @@
  * and savedData.dat (its static records from the inputs, or from the file a
  * continue run started from).  A file already in the output folder is first
  * renamed with the run's start time, as BackupFile does (src/DataSave.c:79-96).
- * out_log.txt is written at the start, as Prepare's SaveLog does.  The end-of-run
- * statistics block is the reference's (src/DMD.c:244-265).
+ * out_log.txt (and for a new run SysInfo.dat) is written at the start, as
+ * Prepare's SaveLog and SaveSysInfo do.  The end-of-run statistics block is the
+ * reference's (src/DMD.c:244-265).
  *
  * The random seed is time(NULL), as the reference's release build uses, or
  * 1575263273 (the reference's -DDEBUG_RANDOM seed) when SDMD_DEBUG_RANDOM is set.
- * SysInfo.dat is not written.
  */
 #include <stdint.h>
 #include <stdio.h>
@@ -177,6 +177,11 @@ int main(int argc, const char *argv[]) {
         if (sdmd_write_log(f, hs, &p, timer, sys->time, file_seed, cli.wall_dyn_size, cli.wall_dyn_rate) != SDMD_OK) {
             fprintf(stderr, "!!ERROR!!: %s\n", f);
             return 1;
+        }
+        if (is_new) {   /* SaveSysInfo (src/SGThread.c:36) */
+            backup(&cli, SDMD_OUT_SYS, timer);
+            out_path(f, sizeof f, &cli, SDMD_OUT_SYS);
+            if (sdmd_write_sysinfo(f, hs) != SDMD_OK) { fprintf(stderr, "!!ERROR!!: %s\n", f); return 1; }
         }
     }
     const int64_t kNoLimit = (int64_t)1 << 40;

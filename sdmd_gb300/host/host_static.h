@@ -21,6 +21,8 @@ typedef struct sdmd_host_static {
     const char *method;                    /* the Force_Field word, 20 bytes */
     const double *mass0;                   /* atom 0's mass and type (FindTargetAtom) */
     const int32_t *type0;
+    const double *hbpot;                   /* HBPotential: BB_r BB_v SS_r SS_v BS_r BS_v */
+    const double *charge;                  /* InitializeCharge's, per atom */
 } sdmd_host_static;
 
 void sdmd_host_static_info(const sdmd_host_system *h, sdmd_host_static *out);

@@ -158,21 +158,7 @@ int sdmd_saved_new(const sdmd_host_system *h, const sdmd_params *p, uint32_t see
         P->sequence.atomNum = i; P->sequence.proteinNum = sys->protein[i]; P->sequence.aminoacidNum = sys->aanum[i];
         s->dyn[i].HB.neighbor = sys->hb_neighbor[i];
         s->dyn[i].HB.role = (char)sys->hb_role[i];
-        /* InitializeCharge (src/Initialization.c:2092-2099) without charge-model
-           flags: "+" / "-" atoms of ARG, ASP, GLU, HIS and LYS */
-        const int res = sys->aatype[i];
-        if (res == 2 || res == 4 || res == 7 || res == 9 || res == 12) {
-            if (!strcmp(P->extraProperty[0], "+")) P->charge = 1;
-            else if (!strcmp(P->extraProperty[0], "-")) P->charge = -1;
-        }
-    }
-    /* ... and the termini (:2101-2116): each peptide's first atom of type 18 and last
-       of type 26 */
-    for (int k = 1; k <= st.n_prot; k++) {
-        for (int n = st.pep_start[k]; n <= st.pep_end[k]; n++)
-            if (sys->type[n] == 18) { s->prop[n].charge = 1; break; }
-        for (int n = st.pep_end[k]; n >= st.pep_start[k]; n--)
-            if (sys->type[n] == 26) { s->prop[n].charge = -1; break; }
+        P->charge = st.charge[i];
     }
     s->cellnum[0] = N + sys->cellnum[0] * sys->cellnum[1] * sys->cellnum[2] + 1;   /* src/Initialization.c:1068 */
     s->seed = seed;

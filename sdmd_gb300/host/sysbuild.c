@@ -61,8 +61,9 @@ struct sdmd_host_system {
     int32_t n_aa, n_prot;
     char *aa_name;
     int32_t *aa_type, *aa_start, *aa_end, *aa_prot, *pep_start, *pep_end, *pep_aa_start, *pep_aa_end;
-    double *aa_mass, *pep_mass;
+    double *aa_mass, *pep_mass, *charge;
     char method[20];
+    double hbpot[6];
 };
 
 typedef struct {
@@ -992,6 +993,24 @@ static int export_system(B *b, sdmd_host_system **out) {
             h->pep_mass[k] += strncmp(b->atom[n].name, "H", 1) == 0 ? 1 : b->atom[n].mass;
     }
     memcpy(h->method, p->force_field, strnlen(p->force_field, sizeof h->method - 1));
+    memcpy(h->hbpot, b->hbpot, sizeof h->hbpot);
+    /* InitializeCharge (src/Initialization.c:2092-2118) without charge-model flags:
+       "+" / "-" atoms of ARG, ASP, GLU, HIS and LYS, then each peptide's first atom
+       of type 18 and last of type 26 */
+    h->charge = zalloc(8 * N1);
+    for (int i = 1; i <= N; i++) {
+        const int res = b->atom[i].aatype;
+        if (res == 2 || res == 4 || res == 7 || res == 9 || res == 12) {
+            if (!strcmp(b->atom[i].ext0, "+")) h->charge[i] = 1;
+            else if (!strcmp(b->atom[i].ext0, "-")) h->charge[i] = -1;
+        }
+    }
+    for (int k = 1; k <= b->nprot; k++) {
+        for (int n = b->prot[k].start_atom; n <= b->prot[k].end_atom; n++)
+            if (b->atom[n].type == 18) { h->charge[n] = 1; break; }
+        for (int n = b->prot[k].end_atom; n >= b->prot[k].start_atom; n--)
+            if (b->atom[n].type == 26) { h->charge[n] = -1; break; }
+    }
     memcpy(h->con_step_d, b->conpool.d, sizeof(double) * ns);
     memcpy(h->con_step_e, b->conpool.e, sizeof(double) * ns);
     memcpy(h->con_step_acc, b->conpool.acc, sizeof(double) * ns);
@@ -1123,6 +1142,8 @@ void sdmd_host_static_info(const sdmd_host_system *h, sdmd_host_static *o) {
     o->pep_aa_end = h->pep_aa_end; o->pep_mass = h->pep_mass;
     o->method = h->method;
     o->mass0 = h->mass; o->type0 = h->type;
+    o->hbpot = h->hbpot;
+    o->charge = h->charge;
 }
 
 void sdmd_host_free(sdmd_host_system *h) {
@@ -1135,7 +1156,7 @@ void sdmd_host_free(sdmd_host_system *h) {
                     h->cz, h->type, h->hb_bond, h->hb_itype, h->nb_partner, h->nb_status, h->nb_pnum, h->ev_partner,
                     h->ev_type, h->ev_sub, h->cell_list, h->ev_counter, h->ev_pcounter, h->names, h->resnames,
                     h->ext, h->aa_name, h->aa_type, h->aa_start, h->aa_end, h->aa_prot, h->aa_mass, h->pep_start,
-                    h->pep_end, h->pep_aa_start, h->pep_aa_end, h->pep_mass};
+                    h->pep_end, h->pep_aa_start, h->pep_aa_end, h->pep_mass, h->charge};
     for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
     free(h);
 }

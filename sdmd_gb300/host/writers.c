@@ -155,6 +155,132 @@ int sdmd_write_hbn(const char *path, int append, const sdmd_system *s) {
     return close_out(f);
 }
 
+/* ---- SysInfo.dat (SaveSysInfo, src/DataSave.c:280-331) ----------------------------
+ * The reference's records as it lays them out (LP64), pointer fields included: a
+ * reader follows its lists while the stored pointer is non-NULL (the analysis
+ * tools' SystemInformation.c), so a list continues exactly where the reference's
+ * pointer was non-NULL.  The addresses themselves are the writing process's; here
+ * a present link is written as 1. */
+typedef struct { int32_t atomNum, proteinNum, aminoacidNum; } si_seq;
+typedef struct {
+    char name[8], extraProperty[2][16], nameofAA[8];
+    int32_t num, typeofAtom, typeofAA;
+    double charge, mass, color[3];
+    si_seq sequence;
+    uint64_t bond, constr;
+} si_property;
+typedef struct { int32_t connection; double dmin; uint64_t step; double dmax; uint64_t next; } si_constr;
+typedef struct { double d, e, accumulated; uint64_t next; } si_step;
+typedef struct { int32_t bondConnection, neighbor; char role; int32_t interactionType; } si_hb;
+typedef struct { char nameofAA[5]; int32_t type, startAtomNum, endAtomNum, proteinNum; double mass; } si_aa;
+typedef struct { int32_t startAtomNum, endAtomNum, startAANum, endAANum; double mass; } si_pep;
+_Static_assert(sizeof(si_property) == 136, "PropertyStr layout");
+_Static_assert(sizeof(si_constr) == 40, "ConstraintStr layout");
+_Static_assert(sizeof(si_step) == 32, "StepPotenStr layout");
+_Static_assert(sizeof(si_hb) == 16, "HBStr layout");
+_Static_assert(sizeof(si_aa) == 32, "AAStr layout");
+_Static_assert(sizeof(si_pep) == 24, "PepStr layout");
+
+#define NATOMTYPE 32   /* src/DMD.h:29: the tables SaveSysInfo writes are [NATOMTYPE][NATOMTYPE] */
+
+static int write_steps(FILE *f, const double *d, const double *e, const double *acc, int off, int n) {
+    int ok = 1;
+    for (int q = 0; q < n; q++) {
+        si_step st;
+        memset(&st, 0, sizeof st);
+        st.d = d[off + q]; st.e = e[off + q]; st.accumulated = acc[off + q]; st.next = q + 1 < n;
+        ok &= fwrite(&st, sizeof st, 1, f) == 1;
+    }
+    return ok;
+}
+
+/* one pair-table entry (a ConstraintStr of potentialPairCollision / potentialPairHB) */
+static int write_pair_entry(FILE *f, const sdmd_system *s, int table, int a, int c) {
+    si_constr e;
+    memset(&e, 0, sizeof e);
+    int off = 0, n = 0;
+    if (table >= 0) {
+        const int idx = (table * SDMD_NTYPES + a) * SDMD_NTYPES + c;
+        e.dmin = s->pair_dmin[idx]; e.dmax = s->pair_dmax[idx];
+        off = s->pair_step_off[idx]; n = s->pair_step_n[idx];
+        e.step = n > 0;
+    }
+    return fwrite(&e, sizeof e, 1, f) == 1 && write_steps(f, s->pair_step_d, s->pair_step_e, s->pair_step_acc, off, n);
+}
+
+int sdmd_write_sysinfo(const char *path, const sdmd_host_system *h) {
+    if (!path || !h) return SDMD_EINVAL;
+    const sdmd_system *s = sdmd_host_view((sdmd_host_system *)h);
+    sdmd_host_static st;
+    sdmd_host_static_info(h, &st);
+    FILE *f = fopen(path, "wb");
+    if (!f) return SDMD_EINVAL;
+    const int N = s->n_atoms;
+    int ok = fwrite(&s->n_atoms, 4, 1, f) == 1 && fwrite(&st.n_prot, 4, 1, f) == 1 && fwrite(&st.n_aa, 4, 1, f) == 1;
+    for (int k = 0; ok && k <= st.n_aa; k++) {
+        si_aa a;
+        memset(&a, 0, sizeof a);
+        if (k > 0) {
+            memcpy(a.nameofAA, st.aa_name + 8 * (size_t)k, 4);
+            a.type = st.aa_type[k]; a.startAtomNum = st.aa_start[k]; a.endAtomNum = st.aa_end[k];
+            a.proteinNum = st.aa_prot[k]; a.mass = st.aa_mass[k];
+        }
+        ok = fwrite(&a, sizeof a, 1, f) == 1;
+    }
+    for (int k = 0; ok && k <= st.n_prot; k++) {
+        si_pep p;
+        memset(&p, 0, sizeof p);
+        if (k > 0) {
+            p.startAtomNum = st.pep_start[k]; p.endAtomNum = st.pep_end[k];
+            p.startAANum = st.pep_aa_start[k]; p.endAANum = st.pep_aa_end[k]; p.mass = st.pep_mass[k];
+        }
+        ok = fwrite(&p, sizeof p, 1, f) == 1;
+    }
+    for (int i = 0; ok && i <= N; i++) {
+        si_property P;
+        memset(&P, 0, sizeof P);
+        memcpy(P.extraProperty, st.ext + 32 * (size_t)i, 32);
+        P.mass = s->mass[i]; P.typeofAtom = s->type[i];
+        const int nb = s->bond_off[i + 1] - s->bond_off[i], nc = s->con_off[i + 1] - s->con_off[i];
+        if (i > 0) {
+            memcpy(P.name, st.names + 8 * (size_t)i, 8);
+            P.name[7] = 0;
+            memcpy(P.nameofAA, st.resnames + 8 * (size_t)i, 8);
+            P.nameofAA[7] = 0;
+            P.num = i; P.typeofAA = s->aatype[i]; P.charge = st.charge[i];
+            P.sequence.atomNum = i; P.sequence.proteinNum = s->protein[i]; P.sequence.aminoacidNum = s->aanum[i];
+            P.bond = nb > 0; P.constr = nc > 0;
+        }
+        ok = fwrite(&P, sizeof P, 1, f) == 1;
+        for (int q = 0; ok && i > 0 && q < nc; q++) {   /* the constraint list, in list order */
+            const int k = s->con_off[i] + q;
+            si_constr e;
+            memset(&e, 0, sizeof e);
+            e.connection = s->con_j[k]; e.dmin = s->con_dmin[k]; e.dmax = s->con_dmax[k];
+            e.step = s->con_step_n[k] > 0; e.next = q + 1 < nc;
+            ok = fwrite(&e, sizeof e, 1, f) == 1 &&
+                 write_steps(f, s->con_step_d, s->con_step_e, s->con_step_acc, s->con_step_off[k], s->con_step_n[k]);
+        }
+        si_hb hb;
+        memset(&hb, 0, sizeof hb);
+        if (i > 0) {
+            hb.bondConnection = s->hb_bond[i]; hb.neighbor = s->hb_neighbor[i];
+            hb.role = (char)s->hb_role[i]; hb.interactionType = s->hb_itype[i];
+        }
+        ok = ok && fwrite(&hb, sizeof hb, 1, f) == 1;
+    }
+    ok = ok && fwrite(st.hbpot, 8, 6, f) == 6;
+    for (int a = 0; ok && a < NATOMTYPE; a++)
+        for (int c = 0; ok && c < NATOMTYPE; c++) ok = write_pair_entry(f, s, 0, a, c);
+    /* potentialPairHB[0..10] (SaveSysInfo's loop, src/DataSave.c:314-327): table 0
+       is never filled, so it is written empty */
+    for (int t = 0; ok && t < 11; t++)
+        for (int a = 0; ok && a < NATOMTYPE; a++)
+            for (int c = 0; ok && c < NATOMTYPE; c++) ok = write_pair_entry(f, s, t == 0 ? -1 : t, a, c);
+    if (fclose(f) != 0) ok = 0;
+    return ok ? SDMD_OK : SDMD_EINVAL;
+}
+
 /* SaveLog (src/DataSave.c:333-462) for the engine's configurations: no coarse
    graining, flow, obstruction, tunnel or column obstacle, no dynamic wall */
 int sdmd_write_log(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,

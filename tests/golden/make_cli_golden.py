@@ -27,7 +27,7 @@ CASE = os.path.join(HERE, "cli_ala10")
 CONT = os.path.join(HERE, "cli_ala10_continue")
 FLAGS = ["-pot", "-kin", "-tem", "-HBn"]
 OUTPUTS = ["out_trj.gro", "out_cnt.txt", "out_pot.txt", "out_kin.txt", "out_tem.txt", "out_HBn.txt", "savedData.dat",
-           "out_log.txt"]
+           "out_log.txt", "SysInfo.dat"]
 
 
 def parameters(text, time, dump):
@@ -51,7 +51,8 @@ def run_case(ind, case_dir, extra_inputs=()):
     for name in ("parameter.txt", "sys.gro", *extra_inputs):
         shutil.copy(os.path.join(ind, name), os.path.join(case_dir, "in", name))
     for name in OUTPUTS:
-        shutil.copy(os.path.join(outd, name), os.path.join(case_dir, "expected", name))
+        if os.path.exists(os.path.join(outd, name)):   # SysInfo.dat: new runs only
+            shutil.copy(os.path.join(outd, name), os.path.join(case_dir, "expected", name))
     with open(os.path.join(case_dir, "expected", "flags.txt"), "w") as f:
         f.write(" ".join(FLAGS) + "\n")
     shutil.rmtree(outd)

@@ -8,8 +8,9 @@ inputs with the same seed (SDMD_DEBUG_RANDOM), its event loop on the GPU, and
 every output file must equal the reference's byte for byte: the trajectory, the
 connection map, the energies, the temperature and the HB counts at every dump,
 and the last checkpoint (savedData.dat, but for the bytes the reference leaves
-undefined, as tests/test_saved_data.py compares them) and the log (but for its
-first line, the start time); an output file already in
+undefined, as tests/test_saved_data.py compares them), the log (but for its
+first line, the start time) and a new run's SysInfo.dat (field by field, as
+tests/test_writers.py walks it); an output file already in
 the folder is kept under the run's start time, as the reference's BackupFile
 does.  cli_ala10_continue is the
 reference's continue run from that checkpoint (read from the output folder, as
@@ -54,6 +55,11 @@ def test_executable_writes_the_reference_outputs(tmp_path, case):
         assert mine == ref, f"{name} differs from the reference's"
     mine, ref = (outd / "out_log.txt").read_text().splitlines(), open(os.path.join(CASE, "expected", "out_log.txt")).read().splitlines()
     assert mine[0].startswith("#Log file at ") and mine[1:] == ref[1:]   # the first line is the start time
+    expected_sys = os.path.join(CASE, "expected", "SysInfo.dat")      # written by a new run only
+    assert (outd / "SysInfo.dat").exists() == os.path.exists(expected_sys)
+    if os.path.exists(expected_sys):
+        from tests.test_writers import walk_sysinfo
+        walk_sysinfo((outd / "SysInfo.dat").read_bytes(), open(expected_sys, "rb").read())
     from tests.test_saved_data import differing_defined_bytes
     bad = differing_defined_bytes((outd / "savedData.dat").read_bytes(),
                                   open(os.path.join(CASE, "expected", "savedData.dat"), "rb").read())

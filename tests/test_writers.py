@@ -126,3 +126,104 @@ def test_log_matches_the_reference(case, tmp_path):
     theirs = ref.split(b"\n")
     assert mine[0] == b"#Log file at 2000_01_01_00_00_00"
     assert mine[1:] == theirs[1:]
+
+
+SYSINFO = 9   # enum FileType: sysInfo
+
+
+def _child_sysinfo(case, q):
+    try:
+        work, ind, outd = case_dir(case)
+        L = _bridge(ind, outd)
+        L.bd_save_type.argtypes = [C.c_int]
+        L.bd_save_type(SYSINFO)                       # SaveSysInfo, as Prepare() calls it for a new run
+        q.put(("ok", open(os.path.join(outd, "SysInfo.dat"), "rb").read(), ind))
+    except Exception as e:
+        q.put(("error", repr(e)))
+
+
+def walk_sysinfo(mine, ref):
+    """Walk two SysInfo.dat images record by record (src/DataSave.c:280-331), the
+    lists following the reference's non-NULL pointers, and return the first
+    difference: every defined field equal, every pointer equally NULL or not.
+    Left out: residue / peptide record 0 and a residue record's bytes past its
+    name (malloc'd), and padding."""
+    pos = [0]
+
+    def take(n):
+        a, b = mine[pos[0]:pos[0] + n], ref[pos[0]:pos[0] + n]
+        pos[0] += n
+        return a, b
+
+    def same(a, b, keep, what):
+        for lo, hi in keep:
+            if a[lo:hi] != b[lo:hi]:
+                raise AssertionError(f"{what}: bytes {lo}-{hi} differ at file offset {pos[0] - len(a) + lo}")
+
+    def ptr(a, b, off, what):
+        pa, pb = int.from_bytes(a[off:off + 8], "little"), int.from_bytes(b[off:off + 8], "little")
+        if (pa == 0) != (pb == 0):
+            raise AssertionError(f"{what}: link at byte {off} is {'set' if pa else 'NULL'} here, "
+                                 f"{'set' if pb else 'NULL'} in the reference")
+        return pb != 0
+
+    def steps(first, what):
+        more = first
+        while more:
+            a, b = take(32)
+            same(a, b, [(0, 24)], what + " step")
+            more = ptr(a, b, 24, what + " step")
+
+    def constr(what):
+        a, b = take(40)
+        same(a, b, [(0, 4), (8, 16), (24, 32)], what)
+        st = ptr(a, b, 16, what)
+        nxt = ptr(a, b, 32, what)
+        steps(st, what)
+        return nxt
+
+    a, b = take(12)
+    same(a, b, [(0, 12)], "header")
+    n_atoms, n_prot, n_aa = np.frombuffer(b, np.int32)
+    for k in range(n_aa + 1):
+        a, b = take(32)
+        if k:
+            same(a, b, [(0, 4), (8, 32)], f"aa[{k}]")
+    for k in range(n_prot + 1):
+        a, b = take(24)
+        if k:
+            same(a, b, [(0, 24)], f"pep[{k}]")
+    for i in range(n_atoms + 1):
+        a, b = take(136)
+        same(a, b, [(0, 120)], f"property[{i}]")
+        ptr(a, b, 120, f"property[{i}].bond")
+        more = ptr(a, b, 128, f"property[{i}].constr")
+        while more:
+            more = constr(f"atom {i} constraint")
+        a, b = take(16)
+        same(a, b, [(0, 9), (12, 16)], f"HB[{i}]")
+    a, b = take(48)
+    same(a, b, [(0, 48)], "HBPotential")
+    for t in range(12):
+        for k in range(32 * 32):
+            if constr(f"table {t} entry {k}"):
+                raise AssertionError("a pair-table entry with a next link")
+    assert pos[0] == len(ref) == len(mine), (pos[0], len(ref), len(mine))
+
+
+@pytest.mark.parametrize("case", ["ala10_nvt", "sheet2", "ala10_cyl", "mixed6"])
+def test_sysinfo_matches_the_reference(case, tmp_path):
+    from sdmd_gb300 import host as H
+    ref, ind = in_child(_child_sysinfo, case)
+    d = np.load(os.path.join(REPO, "tests", "golden", f"{case}.npz"))
+    L = H.lib()
+    L.sdmd_write_sysinfo.argtypes = [C.c_char_p, C.c_void_p]
+    params = H.read_parameters(os.path.join(ind, "parameter.txt"))
+    hs = C.c_void_p()
+    err = C.create_string_buffer(512)
+    assert L.sdmd_build_system_gro_text(ind.encode(), bytes(d["meta/gro"]), C.byref(params), int(d["pre/seed"][0]),
+                                        20000, C.byref(hs), err, 512) == 0, err.value
+    path = tmp_path / "SysInfo.dat"
+    assert L.sdmd_write_sysinfo(str(path).encode(), hs) == 0
+    L.sdmd_host_free(hs)
+    walk_sysinfo(path.read_bytes(), ref)
