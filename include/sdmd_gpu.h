@@ -255,6 +255,27 @@ typedef struct sdmd_remd {
 } sdmd_remd;
 int  sdmd_gpu_run_remd(sdmd_gpu *h, int64_t n_exchanges, double t_end, sdmd_remd *remd);
 
+/* The two halves of sdmd_gpu_run_remd, for a host that also dumps between
+ * exchanges, as each replica process of the reference does (REMDRun,
+ * src/REMD.c:29-126: after an executed event, the dump check, then the exchange
+ * check).
+ *
+ * sdmd_gpu_run_to_stops runs each system k until it executes an event at a time
+ * >= stop_time[k] (<= 0: no time stop), or has executed max_events[k] events
+ * (0: system k does not run), or one of sdmd_gpu_run's limits.  at_stop (may be
+ * NULL; n_systems entries) receives 1 for each system that stopped at such an
+ * event (either kind) and 0 for the others.
+ *
+ * sdmd_gpu_exchange makes one exchange now, with every system at its exchange
+ * point: CalPotenE of each, one rearrange() pass (src/Server.c:145-192) over the
+ * replicas with T != 0 (a replica whose run has ended takes no part: the
+ * reference's server skips a closed connection), and the new thermostat targets
+ * of those replicas.  num, T, rng, attempted and accepted are read and updated
+ * as by sdmd_gpu_run_remd; E (may be NULL) receives the energies. */
+int  sdmd_gpu_run_to_stops(sdmd_gpu *h, const double *stop_time, const int64_t *max_events, double t_end,
+                           int32_t *at_stop);
+int  sdmd_gpu_exchange(sdmd_gpu *h, sdmd_remd *remd);
+
 /* Kernels launched by the last sdmd_gpu_run (all of them, and event-loop kernels
  * alone) and the device time (ms) of the event-loop kernels alone, measured with
  * CUDA events around each of those launches. */

@@ -152,6 +152,24 @@ int  sdmd_saved_new(const sdmd_host_system *h, const sdmd_params *p, uint32_t se
                     int errlen);
 void sdmd_saved_free(sdmd_saved *s);
 
+/* A replica of the reference's REMD run: REMDInfo (src/DMD.h:383-390) as a
+ * client's -REMD flag sets it (src/Initialization.c:170-211) -- the server's
+ * port, the exchange period (ExchangeRate), the temperature record (reduced T
+ * and ladder index num), the server's name and the extra name that replica's
+ * file names carry (its id). */
+typedef struct sdmd_replica {
+    int32_t port, output_rate, num;
+    double  T;
+    char    server[50], extra[50];
+} sdmd_replica;
+/* Sets the REMDInfo record that sdmd_saved_write writes (flag 1 and r's
+ * fields); r NULL restores the record of a run without -REMD. */
+int  sdmd_saved_set_replica(sdmd_saved *s, const sdmd_replica *r);
+/* The file's REMDInfo record: returns its flag (1: a REMD replica's checkpoint,
+ * which a continue run takes its temperature record from, src/Initialization.c:475-476),
+ * 0 without one, or SDMD_EINVAL. */
+int  sdmd_saved_replica(const sdmd_saved *s, sdmd_replica *out);
+
 sdmd_system *sdmd_host_view(sdmd_host_system *h);
 void sdmd_host_free(sdmd_host_system *h);
 
@@ -187,6 +205,15 @@ int sdmd_write_series(const char *path, int append, double time, double value);
  *                      run's start time, wall_dyn_size / rate the -Wsz / -Wrt values */
 int sdmd_write_log(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,
                    double old_time, uint32_t seed, double wall_dyn_size, double wall_dyn_rate);
+/*   sdmd_write_log_replica  the same for a REMD replica: the REMD lines from r
+ *                      (NULL: as sdmd_write_log) */
+int sdmd_write_log_replica(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,
+                           double old_time, uint32_t seed, double wall_dyn_size, double wall_dyn_rate,
+                           const sdmd_replica *r);
+/*   sdmd_write_remd    out_REMD.txt     SaveRE (src/DataSave.c:687-700): after an
+ *                      exchange, the replica's time, new temperature and ladder
+ *                      index; nothing is written for a temperature <= 0 */
+int sdmd_write_remd(const char *path, int append, double time, double T, int32_t num);
 /*   sdmd_write_sysinfo SysInfo.dat      SaveSysInfo (src/DataSave.c:280-331): the
  *                      system's static records for the analysis tools, from the built
  *                      system; the reference's heap addresses in its pointer fields

@@ -3,6 +3,7 @@
   sdmd_gb300/libsdmd_gpu.so   CUDA kernels + C ABI (include/sdmd_gpu.h), sm_103a only
   sdmd_gb300/libsdmd_host.so  host-side C: system builder for the reference's inputs
   sdmd_gb300/sdmd-gb300       the sDMD executable on the engine (app/sdmd_run.c)
+  sdmd_gb300/sremd-gb300      the REMD launcher, all replicas in one engine batch (app/sremd_run.c)
 
 Translation units compile in parallel; nothing here uses cmake or torch.
 """
@@ -94,18 +95,23 @@ def build_host(force=False):
 
 
 APP = os.path.join(HERE, "sdmd-gb300")
-APP_SRC = os.path.join(HERE, "app", "sdmd_run.c")
+REMD_APP = os.path.join(HERE, "sremd-gb300")
+APP_DIR = os.path.join(HERE, "app")
+APP_SRC = os.path.join(APP_DIR, "sdmd_run.c")
+REMD_APP_SRC = os.path.join(APP_DIR, "sremd_run.c")
+APP_COMMON = [os.path.join(APP_DIR, "app_common.c"), os.path.join(APP_DIR, "app_common.h")]
 
 
 def build_app(force=False):
-    """The sDMD executable, linked with the two libraries beside it."""
-    deps = [APP_SRC, GPU_LIB, HOST_LIB, os.path.join(INCLUDE, "sdmd_gpu.h"), os.path.join(INCLUDE, "sdmd_host.h")]
-    if not force and _newer(APP, deps):
-        return APP
-    tmp = APP + ".tmp"
-    subprocess.check_call(["gcc", "-O2", "-std=gnu99", "-Wall", "-I" + INCLUDE, "-o", tmp, APP_SRC, "-L" + HERE,
-                           "-lsdmd_gpu", "-lsdmd_host", "-Wl,-rpath,$ORIGIN", "-lm"])
-    os.replace(tmp, APP)
+    """The sDMD executable and the REMD launcher, linked with the two libraries beside them."""
+    common = [GPU_LIB, HOST_LIB, os.path.join(INCLUDE, "sdmd_gpu.h"), os.path.join(INCLUDE, "sdmd_host.h")] + APP_COMMON
+    for out, src in ((APP, APP_SRC), (REMD_APP, REMD_APP_SRC)):
+        if not force and _newer(out, [src] + common):
+            continue
+        tmp = out + ".tmp"
+        subprocess.check_call(["gcc", "-O2", "-std=gnu99", "-Wall", "-I" + INCLUDE, "-I" + APP_DIR, "-o", tmp, src,
+                               APP_COMMON[0], "-L" + HERE, "-lsdmd_gpu", "-lsdmd_host", "-Wl,-rpath,$ORIGIN", "-lm"])
+        os.replace(tmp, out)
     return APP
 
 

@@ -49,11 +49,11 @@ struct sdmd_gpu {
     DScal *sc_all = nullptr;                       // the systems' scalar blocks, contiguous
     Adv *adv = nullptr;                            // their per-system protocol words (in the arena)
     double prep_ms = 0, run_ms = 0;
-    // energies / replica exchange scratch (one block: num, T, E, kin, warn, stop, rng, stats)
+    // energies / replica exchange scratch (one block: num, T, E, kin, warn, stop, lim, rng, stats)
     unsigned char *aux = nullptr;
     int32_t *x_num = nullptr;
     double *x_T = nullptr, *x_E = nullptr, *x_kin = nullptr, *x_stop = nullptr;
-    int64_t *x_warn = nullptr, *x_stats = nullptr;
+    int64_t *x_warn = nullptr, *x_stats = nullptr, *x_lim = nullptr;
     sdmd_rng *x_rng = nullptr;
     size_t esmem = 0;
     cudaEvent_t l0 = nullptr, l1 = nullptr;        // around each loop-kernel launch
@@ -725,7 +725,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         (r = cuda_fail(cudaEventCreate(&h->e0))) || (r = cuda_fail(cudaEventCreate(&h->e1))) ||
         (r = cuda_fail(cudaEventCreate(&h->l0))) || (r = cuda_fail(cudaEventCreate(&h->l1))) ||
         (r = cuda_fail(cudaMalloc(&h->arena, h->arena_bytes))) ||
-        (r = cuda_fail(cudaMalloc(&h->aux, 256 * 9 + (size_t)n_systems * 48))) ||
+        (r = cuda_fail(cudaMalloc(&h->aux, 256 * 10 + (size_t)n_systems * 56))) ||
         (r = cuda_fail(cudaMalloc(&h->ds, sizeof(DSys) * n_systems)))) {
         sdmd_gpu_destroy(h);
         return r;
@@ -736,6 +736,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         h->x_num = ax.take<int32_t>(n_systems); h->x_T = ax.take<double>(n_systems);
         h->x_E = ax.take<double>(n_systems); h->x_kin = ax.take<double>(n_systems);
         h->x_warn = ax.take<int64_t>(n_systems); h->x_stop = ax.take<double>(n_systems);
+        h->x_lim = ax.take<int64_t>(n_systems);
         h->x_rng = ax.take<sdmd_rng>(1); h->x_stats = ax.take<int64_t>(2);
     }
     h->esmem = energy_smem_bytes(nbcap_max);
@@ -933,6 +934,65 @@ extern "C" int sdmd_gpu_run_to_dump(sdmd_gpu *h, double dump_time, int64_t max_e
     h->run_ms = ms;
     if (at_dump)
         for (int k = 0; k < n; k++) at_dump[k] = sc[k].at_stop ? 1 : 0;
+    return collect_errors(h);
+}
+
+extern "C" int sdmd_gpu_run_to_stops(sdmd_gpu *h, const double *stop_time, const int64_t *max_events, double t_end,
+                                     int32_t *at_stop) {
+    if (!h || !stop_time || !max_events) return SDMD_EINVAL;
+    const int n = h->n_systems;
+    int64_t most = 0;
+    for (int k = 0; k < n; k++) {
+        if (max_events[k] < 0 || !(stop_time[k] == stop_time[k])) return SDMD_EINVAL;
+        most = std::max(most, max_events[k]);
+    }
+    if (at_stop)
+        for (int k = 0; k < n; k++) at_stop[k] = 0;
+    if (most == 0) return SDMD_OK;
+    CK(cudaSetDevice(h->opts.device));
+    CK(cudaEventRecord(h->e0, h->stream));
+    CK(cudaMemcpyAsync(h->x_stop, stop_time, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->x_lim, max_events, sizeof(int64_t) * n, cudaMemcpyHostToDevice, h->stream));
+    stops_round_kernel<<<n_blocks(n, 64), 64, 0, h->stream>>>(h->ds, n, h->x_lim, h->x_stop);
+    h->launches = 1; h->loop_launches = 0; h->loop_ms = 0;
+    int r = run_rounds(h, std::min<int64_t>(4 * most + 64, 1 << 16), t_end);
+    if (r) return r;
+    std::vector<DScal> sc(n);
+    CK(cudaMemcpyAsync(sc.data(), h->sc_all, sizeof(DScal) * n, cudaMemcpyDeviceToHost, h->stream));
+    remd_round_kernel<<<n_blocks(n, 64), 64, 0, h->stream>>>(h->ds, n, 0, nullptr);   // the stop points off again
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->e1, h->stream));
+    CK(cudaEventSynchronize(h->e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, h->e0, h->e1);
+    h->run_ms = ms;
+    if (at_stop)
+        for (int k = 0; k < n; k++)
+            at_stop[k] = max_events[k] > 0 && (sc[k].at_stop || sc[k].c.frame >= sc[k].target_frame) ? 1 : 0;
+    return collect_errors(h);
+}
+
+extern "C" int sdmd_gpu_exchange(sdmd_gpu *h, sdmd_remd *x) {
+    if (!h || !x || !x->num || !x->T) return SDMD_EINVAL;
+    CK(cudaSetDevice(h->opts.device));
+    const int n = h->n_systems;
+    int64_t stats[2] = {x->attempted, x->accepted};
+    CK(cudaMemcpyAsync(h->x_num, x->num, sizeof(int32_t) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->x_T, x->T, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->x_rng, &x->rng, sizeof(sdmd_rng), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->x_stats, stats, sizeof(stats), cudaMemcpyHostToDevice, h->stream));
+    energy_kernel<<<n, 32, h->esmem, h->stream>>>(h->ds, h->x_E, h->x_kin, h->x_warn);
+    remd_exchange_kernel<<<1, 1, 0, h->stream>>>(h->ds, n, h->x_num, h->x_T, h->x_E, h->x_warn, h->x_rng, h->x_stats);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(x->num, h->x_num, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(x->T, h->x_T, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    if (x->E) CK(cudaMemcpyAsync(x->E, h->x_E, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(&x->rng, h->x_rng, sizeof(sdmd_rng), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(stats, h->x_stats, sizeof(stats), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    x->attempted = stats[0];
+    x->accepted = stats[1];
+    x->exchanges_done = 1;
     return collect_errors(h);
 }
 

@@ -37,6 +37,7 @@ __global__ void sweep_fix_kernel(const DSys *systems, int full);
 size_t energy_smem_bytes(int nbcap);
 __global__ void energy_kernel(const DSys *systems, double *pot, double *kin, int64_t *warn);
 __global__ void remd_round_kernel(const DSys *systems, int n, int64_t every_events, const double *stop_time);
+__global__ void stops_round_kernel(const DSys *systems, int n, const int64_t *limit, const double *stop_time);
 __global__ void remd_exchange_kernel(DSys *systems, int n, int32_t *num, double *T, const double *E,
                                      const int64_t *warn, sdmd_rng *rng, int64_t *stats);
 

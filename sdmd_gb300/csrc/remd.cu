@@ -145,6 +145,19 @@ __global__ void remd_round_kernel(const DSys *systems, int n, int64_t every_even
     C->paused = 0;
 }
 
+// per-system stop points: an event limit (0: the system does not run) and an
+// exchange / dump time (<= 0: none)
+__global__ void stops_round_kernel(const DSys *systems, int n, const int64_t *limit, const double *stop_time) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    DScal *C = systems[k].sc;
+    const int64_t room = 0x7fffffffffffffffLL - C->c.frame;
+    C->target_frame = limit[k] < room ? C->c.frame + limit[k] : 0x7fffffffffffffffLL;
+    C->stop_time = stop_time[k] > 0 ? stop_time[k] : 0;
+    C->at_stop = 0;
+    C->paused = 0;
+}
+
 // rearrange() of the exchange server, then the replicas' new thermostat targets
 __global__ void remd_exchange_kernel(DSys *systems, int n, int32_t *num, double *T, const double *E,
                                      const int64_t *warn, sdmd_rng *rng, int64_t *stats) {
@@ -172,6 +185,7 @@ __global__ void remd_exchange_kernel(DSys *systems, int n, int32_t *num, double 
     stats[0] += att;
     stats[1] += acc;
     for (int k = 0; k < n; k++) {
+        if (!(T[k] != 0)) continue;             // a replica that has left the exchange (its run ended)
         systems[k].temperature = T[k];
         systems[k].sc->c.warnings += warn[k];   // CalPotenE's FindPair calls count warnings too
     }

@@ -22,7 +22,7 @@ ABI_FUNCS = ["sdmd_gpu_abi_version", "sdmd_gpu_device_count", "sdmd_gpu_strerror
              "sdmd_gpu_destroy", "sdmd_gpu_prepare", "sdmd_gpu_run", "sdmd_gpu_download", "sdmd_gpu_trace",
              "sdmd_gpu_last_ms", "sdmd_gpu_last_error", "sdmd_rng_seed", "sdmd_rng_next", "sdmd_rng_skip",
              "sdmd_gpu_prepare_noalloc", "sdmd_gpu_last_run_stats", "sdmd_gpu_energies", "sdmd_gpu_run_remd",
-             "sdmd_gpu_launch_info"]
+             "sdmd_gpu_launch_info", "sdmd_gpu_run_to_dump", "sdmd_gpu_run_to_stops", "sdmd_gpu_exchange"]
 LOOP_KERNELS = {0: "loop_kernel_fp64", 1: "loop_kernel_screen", 2: "loop_kernel_screen_r128",
                 3: "loop_kernel_screen_coop", 4: "loop_kernel_screen_coop512"}
 
@@ -72,6 +72,8 @@ def lib():
         L.sdmd_gpu_last_run_stats.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64), P(C.c_double)]
         L.sdmd_gpu_energies.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         L.sdmd_gpu_run_remd.argtypes = [C.c_void_p, C.c_int64, C.c_double, P(sdmd_remd)]
+        L.sdmd_gpu_run_to_stops.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), C.c_double, P(C.c_int32)]
+        L.sdmd_gpu_exchange.argtypes = [C.c_void_p, P(sdmd_remd)]
         L.sdmd_gpu_launch_info.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int32), P(C.c_int32)]
         L.sdmd_rng_seed.argtypes = [P(sdmd_rng), C.c_uint32]
         L.sdmd_rng_seed.restype = None
@@ -180,6 +182,38 @@ class Engine:
         out_rng = np.array([x.rng.tab[i] for i in range(31)] + [x.rng.front, x.rng.rear], np.int32)
         return {"num": num, "T": T, "E": E, "rng": out_rng, "attempted": x.attempted, "accepted": x.accepted,
                 "done": x.exchanges_done}
+
+    def run_to_stops(self, stop_time, max_events, t_end=0.0):
+        """Each system k runs to its first executed event at time >= stop_time[k]
+        (<= 0: none) or max_events[k] executed events (0: it does not run).
+        Returns at_stop (1 where a system stopped at such an event)."""
+        n = len(self.systems)
+        stop = np.ascontiguousarray(stop_time, np.float64)
+        lim = np.ascontiguousarray(max_events, np.int64)
+        at = np.zeros(n, np.int32)
+        self._check(lib().sdmd_gpu_run_to_stops(self.h, stop.ctypes.data_as(C.POINTER(C.c_double)),
+                                                lim.ctypes.data_as(C.POINTER(C.c_int64)), float(t_end),
+                                                at.ctypes.data_as(C.POINTER(C.c_int32))), "sdmd_gpu_run_to_stops")
+        return at
+
+    def exchange(self, num, T, rng, attempted=0, accepted=0):
+        """One exchange now (CalPotenE, one rearrange() pass over replicas with T != 0,
+        new thermostat targets).  Returns dict(num, T, E, rng, attempted, accepted)."""
+        n = len(self.systems)
+        num = np.ascontiguousarray(num, np.int32).copy()
+        T = np.ascontiguousarray(T, np.float64).copy()
+        E = np.zeros(n)
+        x = sdmd_remd()
+        x.num = num.ctypes.data_as(C.POINTER(C.c_int32))
+        x.T = T.ctypes.data_as(C.POINTER(C.c_double))
+        x.E = E.ctypes.data_as(C.POINTER(C.c_double))
+        for i in range(31):
+            x.rng.tab[i] = int(rng[i])
+        x.rng.front, x.rng.rear = int(rng[31]), int(rng[32])
+        x.attempted, x.accepted = int(attempted), int(accepted)
+        self._check(lib().sdmd_gpu_exchange(self.h, C.byref(x)), "sdmd_gpu_exchange")
+        out_rng = np.array([x.rng.tab[i] for i in range(31)] + [x.rng.front, x.rng.rear], np.int32)
+        return {"num": num, "T": T, "E": E, "rng": out_rng, "attempted": x.attempted, "accepted": x.accepted}
 
     def launch_info(self):
         """dict(threads, helper_blocks, staged, loop_kernel) of the handle's event-loop launch."""

@@ -175,6 +175,12 @@ class sdmd_remd_config(C.Structure):
                 ("T_kelvin", C.c_double * REMD_MAX), ("T", C.c_double * REMD_MAX), ("num", C.c_int32 * REMD_MAX)]
 
 
+class sdmd_replica(C.Structure):
+    """A REMD replica's REMDInfo record (include/sdmd_host.h)."""
+    _fields_ = [("port", C.c_int32), ("output_rate", C.c_int32), ("num", C.c_int32), ("T", C.c_double),
+                ("server", C.c_char * 50), ("extra", C.c_char * 50)]
+
+
 def parse_args(argv):
     """sdmd_parse_args over a list of strings (argv[0] is the program name)."""
     L = lib()

@@ -48,6 +48,7 @@ int sdmd_parse_args(int argc, const char *const *argv, sdmd_cli *c, char *errbuf
     memset(c, 0, sizeof(*c));
     snprintf(c->coordinate_file, sizeof c->coordinate_file, "%s", "coordinate.gro");
     snprintf(c->saved_in, sizeof c->saved_in, "%s", "savedData.dat");
+    c->remd_rate = 1000;   /* REMDInfo.REMD_OutputRate's initializer (src/DMD.c:130) */
     for (int i = 1; i < argc; i++) {
         const char *a = argv[i];
         if (a[0] != '-') continue;   /* the reference looks at flags only */

@@ -162,14 +162,44 @@ int sdmd_saved_new(const sdmd_host_system *h, const sdmd_params *p, uint32_t see
     }
     s->cellnum[0] = N + sys->cellnum[0] * sys->cellnum[1] * sys->cellnum[2] + 1;   /* src/Initialization.c:1068 */
     s->seed = seed;
-    /* REMDInfo's initializer (src/DMD.c:126-132): a run without -REMD */
-    s->remd.REMD_PortNum = -1;
-    s->remd.REMD_OutputRate = 1000;
-    s->remd.REMD_Temperature.num = -1;
-    s->remd.REMD_Temperature.T = -1;
+    sdmd_saved_set_replica(s, NULL);   /* a run without -REMD */
     *out = s;
     (void)err; (void)errlen;
     return SDMD_OK;
+}
+
+int sdmd_saved_set_replica(sdmd_saved *s, const sdmd_replica *r) {
+    if (!s) return SDMD_EINVAL;
+    memset(&s->remd, 0, sizeof s->remd);
+    if (!r) {   /* REMDInfo's initializer (src/DMD.c:126-132) */
+        s->remd.REMD_PortNum = -1;
+        s->remd.REMD_OutputRate = 1000;
+        s->remd.REMD_Temperature.num = -1;
+        s->remd.REMD_Temperature.T = -1;
+        return SDMD_OK;
+    }
+    s->remd.flag = 1;
+    s->remd.REMD_PortNum = r->port;
+    s->remd.REMD_OutputRate = r->output_rate;
+    /* the names as sprintf leaves them in the zeroed global: text, then zeros */
+    memcpy(s->remd.REMD_ServerName, r->server, strnlen(r->server, sizeof s->remd.REMD_ServerName - 1));
+    memcpy(s->remd.REMD_ExtraName, r->extra, strnlen(r->extra, sizeof s->remd.REMD_ExtraName - 1));
+    s->remd.REMD_Temperature.num = r->num;
+    s->remd.REMD_Temperature.T = r->T;
+    return SDMD_OK;
+}
+
+int sdmd_saved_replica(const sdmd_saved *s, sdmd_replica *out) {
+    if (!s || !out) return SDMD_EINVAL;
+    memset(out, 0, sizeof *out);
+    out->port = s->remd.REMD_PortNum;
+    out->output_rate = s->remd.REMD_OutputRate;
+    out->num = s->remd.REMD_Temperature.num;
+    out->T = s->remd.REMD_Temperature.T;
+    memcpy(out->server, s->remd.REMD_ServerName, sizeof out->server);
+    memcpy(out->extra, s->remd.REMD_ExtraName, sizeof out->extra);
+    out->server[sizeof out->server - 1] = out->extra[sizeof out->extra - 1] = 0;
+    return s->remd.flag ? 1 : 0;
 }
 
 #define RD(ptr, size, n) (fread((ptr), (size), (size_t)(n), f) == (size_t)(n))

@@ -1191,13 +1191,13 @@ static void sb_printf(sbuf *b, const char *fmt, ...) {
 
 /* library atom names of residue `res` as the .gro should list them */
 static int residue_atoms(B *b, const char *res, int first, char names[][8]) {
-    char list[20][8];
+    char list[20][8] = {{0}};
     int n = read_atom_list(b, res, list), m = 0;
     if (n < 0) return -1;
     for (int i = 0; i < n; i++) {
         if (!strcmp(res, "GLY") && !strcmp(list[i], "CB")) continue;   /* GLY uses ALA's list without CB */
         if (first && !strcmp(list[i], "H")) continue;                  /* the N-terminal N carries no H */
-        snprintf(names[m++], 8, "%s", list[i]);
+        memcpy(names[m++], list[i], 8);                                 /* tok() ends each name within 8 bytes */
     }
     return m;
 }

@@ -285,6 +285,12 @@ int sdmd_write_sysinfo(const char *path, const sdmd_host_system *h) {
    graining, flow, obstruction, tunnel or column obstacle, no dynamic wall */
 int sdmd_write_log(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,
                    double old_time, uint32_t seed, double wall_dyn_size, double wall_dyn_rate) {
+    return sdmd_write_log_replica(path, h, p, timer, old_time, seed, wall_dyn_size, wall_dyn_rate, NULL);
+}
+
+int sdmd_write_log_replica(const char *path, const sdmd_host_system *h, const sdmd_params *p, const char *timer,
+                           double old_time, uint32_t seed, double wall_dyn_size, double wall_dyn_rate,
+                           const sdmd_replica *r) {
     if (!path || !h || !p) return SDMD_EINVAL;
     const sdmd_system *s = sdmd_host_view((sdmd_host_system *)h);
     sdmd_host_static st;
@@ -325,13 +331,13 @@ int sdmd_write_log(const char *path, const sdmd_host_system *h, const sdmd_param
     fprintf(f, "ColumnObstacles     = %-5i\n", 0);
     fprintf(f, "                      No column.\n");
     fprintf(f, "RandomSeed          = %i\n", (int)seed);
-    /* REMDInfo's initializer (src/DMD.c:126-132): a run without -REMD */
-    fprintf(f, "REMDPortNum         = %i\n", -1);
-    fprintf(f, "REMDTemperature     = %.2lf\n", -1.0);
-    fprintf(f, "REMDTempSeq         = %i\n", -1);
-    fprintf(f, "REMDOutputRate      = %i\n", 1000);
-    fprintf(f, "REMDServerName      = %s\n", "");
-    fprintf(f, "REMDExtraName       = %s\n", "");
+    /* REMDInfo: the -REMD flag's values, else its initializer (src/DMD.c:126-132) */
+    fprintf(f, "REMDPortNum         = %i\n", r ? (int)r->port : -1);
+    fprintf(f, "REMDTemperature     = %.2lf\n", r ? r->T : -1.0);
+    fprintf(f, "REMDTempSeq         = %i\n", r ? (int)r->num : -1);
+    fprintf(f, "REMDOutputRate      = %i\n", r ? (int)r->output_rate : 1000);
+    fprintf(f, "REMDServerName      = %.50s\n", r ? r->server : "");
+    fprintf(f, "REMDExtraName       = %.50s\n", r ? r->extra : "");
     fprintf(f, "\n");
     return close_out(f);
 }
@@ -340,5 +346,14 @@ int sdmd_write_series(const char *path, int append, double time, double value) {
     FILE *f = open_out(path, append);
     if (!f) return SDMD_EINVAL;
     fprintf(f, "%5.2lf    %10.4lf\n", time, value);
+    return close_out(f);
+}
+
+/* SaveRE (src/DataSave.c:687-700): written after each exchange, while the
+   replica's temperature is valid */
+int sdmd_write_remd(const char *path, int append, double time, double T, int32_t num) {
+    FILE *f = open_out(path, append);
+    if (!f) return SDMD_EINVAL;
+    if (T > 0) fprintf(f, "%5.2f %8.4lf %2i\n", time, T, (int)num);
     return close_out(f);
 }

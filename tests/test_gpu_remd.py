@@ -107,3 +107,39 @@ def test_replica_exchange_matches_oracle(golden, engine_mod, screen, trigger):
             assert np.array_equal(s.a[k], r.a[k]), k
         assert s.counters == r.counters and s.time == r.time
         assert np.array_equal(s.rng, r.rng)
+
+
+def test_stops_and_exchange_make_the_same_replica_exchange(golden, engine_mod):
+    """sdmd_gpu_run_to_stops (each replica to its own exchange point) followed by
+    sdmd_gpu_exchange, repeated, is the oracle's replica exchange with the time
+    trigger; a system given no events does not move."""
+    n, n_exch = 6, 4
+    gpu, T = replicas(golden, n)
+    ref = [s.copy() for s in gpu]
+    server = glibc_rng_state(20201)
+    num, Tx, rng = np.arange(1, n + 1), T.copy(), server
+    att = acc = 0
+    with engine_mod.Engine(gpu, screen=1) as e:
+        e.prepare(full=True)
+        e.download()
+        rate = np.array([(int(s.time / 1.0) + 1) * 1.0 for s in gpu])
+        for _ in range(n_exch):
+            e.download()
+            before = [s.counters["frame"] for s in gpu]
+            held = e.run_to_stops(rate, np.zeros(n, np.int64))          # nothing runs
+            e.download()
+            assert not held.any() and [s.counters["frame"] for s in gpu] == before
+            at = e.run_to_stops(rate, np.full(n, 1 << 40, np.int64))
+            assert at.all()
+            out = e.exchange(num, Tx, rng, att, acc)
+            num, Tx, rng, att, acc = out["num"], out["T"], out["rng"], out["attempted"], out["accepted"]
+            rate += 1.0
+        e.download()
+    num_o, T_o, E_o, rng_o = oracle_remd(ref, T, server, n_exch, every_time=1.0)
+    assert np.array_equal(num, num_o) and np.array_equal(Tx, T_o)
+    assert np.array_equal(out["E"], E_o)
+    assert np.array_equal(rng, rng_o)
+    for s, r in zip(gpu, ref):
+        for k in DYN:
+            assert np.array_equal(s.a[k], r.a[k]), k
+        assert s.counters == r.counters and s.time == r.time
