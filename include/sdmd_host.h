@@ -219,6 +219,10 @@ int sdmd_write_remd(const char *path, int append, double time, double T, int32_t
  *                      system; the reference's heap addresses in its pointer fields
  *                      are written as 1 where it has a link (readers test them for NULL) */
 int sdmd_write_sysinfo(const char *path, const sdmd_host_system *h);
+/*   sdmd_write_wallinfo WallInfo.dat    SaveWallInfo (src/DataSave.c:280-292): a
+ *                      smooth wall's atom record (property and dynamic records) as
+ *                      ReadWall builds it; SDMD_EINVAL for a system without a wall */
+int sdmd_write_wallinfo(const char *path, const sdmd_host_system *h);
 
 #ifdef __cplusplus
 }

@@ -50,7 +50,8 @@ void app_timer(char *buf, size_t len);
 /* The configuration block main() prints before the run (src/DMD.c:196-214). */
 void app_print_config(const app_run *r);
 
-/* Prepare's SaveLog and, for a new run, SaveSysInfo (src/SGThread.c:27-36). */
+/* Prepare's SaveLog and, for a new run, SaveSysInfo and a smooth wall's
+   SaveWallInfo (src/SGThread.c:27-37). */
 int app_start_files(app_run *r, const char *timer);
 
 /* SaveData for every marked file at a dump (src/SGThread.c:132-139): sys is the

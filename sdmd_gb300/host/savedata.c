@@ -168,6 +168,35 @@ int sdmd_saved_new(const sdmd_host_system *h, const sdmd_params *p, uint32_t see
     return SDMD_OK;
 }
 
+/* SaveWallInfo (src/DataSave.c:280-292): the smooth wall's atom record as ReadWall
+   builds it (src/Initialization.c:1907-1931) -- its Wall.txt name, extra
+   properties and mass, the atom type it names, residue "Wall", the position from
+   the box, an invalid event -- the rest zero, as calloc leaves it */
+int sdmd_write_wallinfo(const char *path, const sdmd_host_system *h) {
+    if (!path || !h) return SDMD_EINVAL;
+    const sdmd_system *sys = sdmd_host_view((sdmd_host_system *)h);
+    if (!sys->wall) return SDMD_EINVAL;
+    sdmd_host_static st;
+    sdmd_host_static_info(h, &st);
+    sv_property P;
+    sv_dynamic D;
+    memset(&P, 0, sizeof P);
+    memset(&D, 0, sizeof D);
+    memcpy(P.name, st.wall_name, 8);
+    memcpy(P.extraProperty, st.wall_ext, 32);
+    memcpy(P.nameofAA, "Wall", 5);
+    P.typeofAtom = sys->wall_type;
+    P.mass = sys->wall_mass;
+    for (int d = 0; d < 3; d++) D.coordinate[d + 1] = sys->wall_pos[d];
+    D.event.partner = SDMD_INVALID;
+    D.event.subEventType = SDMD_SUB_INVALID;
+    D.event.eventType = SDMD_EV_INVALID;
+    FILE *f = fopen(path, "wb");
+    if (!f) return SDMD_EINVAL;
+    const int ok = fwrite(&P, sizeof P, 1, f) == 1 && fwrite(&D, sizeof D, 1, f) == 1;
+    return fclose(f) == 0 && ok ? SDMD_OK : SDMD_EINVAL;
+}
+
 int sdmd_saved_set_replica(sdmd_saved *s, const sdmd_replica *r) {
     if (!s) return SDMD_EINVAL;
     memset(&s->remd, 0, sizeof s->remd);

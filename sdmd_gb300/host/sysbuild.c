@@ -64,6 +64,7 @@ struct sdmd_host_system {
     double *aa_mass, *pep_mass, *charge;
     char method[20];
     double hbpot[6];
+    char wall_name[8], wall_ext[32];   /* the Wall.txt record of a smooth wall */
 };
 
 typedef struct {
@@ -81,6 +82,7 @@ typedef struct {
     sdmd_rng rng;
     int64_t warnings;
     int wall; int wall_type; double wall_pos[3], wall_mass;
+    char wall_name[8], wall_ext[32];
     char *err; int errlen;
 } B;
 
@@ -730,6 +732,9 @@ static int read_wall(B *b) {   /* ReadWall, smooth walls (src/Initialization.c:1
     tok(&c, s, sizeof s); tok(&c, name, sizeof name); tok(&c, tn, sizeof tn); dbl(&c, &b->wall_mass);
     tok(&c, e0, sizeof e0); tok(&c, e1, sizeof e1);
     free(c.buf);
+    memcpy(b->wall_name, name, strnlen(name, 7));
+    memcpy(b->wall_ext, e0, strnlen(e0, 15));
+    memcpy(b->wall_ext + 16, e1, strnlen(e1, 15));
     b->wall_type = atom_model(tn);
     if (b->wall_type < 0) return fail(b, "no atom type is matched to %s (Wall.txt)", tn);
     for (int d = 0; d < 3; d++) b->wall_pos[d] = b->box[d + 1] / 2;
@@ -994,6 +999,8 @@ static int export_system(B *b, sdmd_host_system **out) {
     }
     memcpy(h->method, p->force_field, strnlen(p->force_field, sizeof h->method - 1));
     memcpy(h->hbpot, b->hbpot, sizeof h->hbpot);
+    memcpy(h->wall_name, b->wall_name, sizeof h->wall_name);
+    memcpy(h->wall_ext, b->wall_ext, sizeof h->wall_ext);
     /* InitializeCharge (src/Initialization.c:2092-2118) without charge-model flags:
        "+" / "-" atoms of ARG, ASP, GLU, HIS and LYS, then each peptide's first atom
        of type 18 and last of type 26 */
@@ -1144,6 +1151,7 @@ void sdmd_host_static_info(const sdmd_host_system *h, sdmd_host_static *o) {
     o->mass0 = h->mass; o->type0 = h->type;
     o->hbpot = h->hbpot;
     o->charge = h->charge;
+    o->wall_name = h->wall_name; o->wall_ext = h->wall_ext;
 }
 
 void sdmd_host_free(sdmd_host_system *h) {

@@ -227,3 +227,37 @@ def test_sysinfo_matches_the_reference(case, tmp_path):
     assert L.sdmd_write_sysinfo(str(path).encode(), hs) == 0
     L.sdmd_host_free(hs)
     walk_sysinfo(path.read_bytes(), ref)
+
+
+WALLINFO = 10   # enum FileType: wallInfo
+
+
+def _child_wallinfo(case, q):
+    try:
+        work, ind, outd = case_dir(case)
+        L = _bridge(ind, outd)
+        L.bd_save_type.argtypes = [C.c_int]
+        L.bd_save_type(WALLINFO)                      # SaveWallInfo, as Prepare() calls it for a smooth wall
+        q.put(("ok", open(os.path.join(outd, "WallInfo.dat"), "rb").read(), ind))
+    except Exception as e:
+        q.put(("error", repr(e)))
+
+
+def test_wallinfo_matches_the_reference(tmp_path):
+    """WallInfo.dat of the cylinder-wall case equals the reference's SaveWallInfo
+    output byte for byte (the wall's atom record as ReadWall builds it)."""
+    from sdmd_gb300 import host as H
+    ref, ind = in_child(_child_wallinfo, "ala10_cyl")
+    d = np.load(os.path.join(REPO, "tests", "golden", "ala10_cyl.npz"))
+    L = H.lib()
+    L.sdmd_write_wallinfo.argtypes = [C.c_char_p, C.c_void_p]
+    params = H.read_parameters(os.path.join(ind, "parameter.txt"))
+    hs = C.c_void_p()
+    err = C.create_string_buffer(512)
+    assert L.sdmd_build_system_gro_text(ind.encode(), bytes(d["meta/gro"]), C.byref(params), int(d["pre/seed"][0]),
+                                        20000, C.byref(hs), err, 512) == 0, err.value
+    path = tmp_path / "WallInfo.dat"
+    assert L.sdmd_write_wallinfo(str(path).encode(), hs) == 0
+    L.sdmd_host_free(hs)
+    assert len(ref) == 136 + 176
+    assert path.read_bytes() == ref
