@@ -12,6 +12,9 @@ every dump, the out_REMD lines of every exchange (time, new temperature, ladder
 index), the log (but for its first line, the start time), SysInfo (field by
 field, as tests/test_writers.py walks it) and the last checkpoint (but for the
 bytes the reference leaves undefined, as tests/test_saved_data.py compares them).
+tests/golden/remd_ala10_continue is the reference's continue run from those
+checkpoints (each replica's read from the output folder, its temperature record
+with it) to Time 50.
 """
 import os
 import shutil
@@ -22,19 +25,23 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-CASE = os.path.join(REPO, "tests", "golden", "remd_ala10")
 
 
-def test_launcher_writes_the_reference_replicas_outputs(tmp_path):
+@pytest.mark.parametrize("case", ["remd_ala10", "remd_ala10_continue"])
+def test_launcher_writes_the_reference_replicas_outputs(tmp_path, case):
     import __graft_entry__ as G
     G.build()
     from sdmd_gb300 import build
     from tests.test_saved_data import differing_defined_bytes
     from tests.test_writers import walk_sysinfo
+    CASE = os.path.join(REPO, "tests", "golden", case)
     ind, outd = tmp_path / "in", tmp_path / "out"
     shutil.copytree(os.path.join(CASE, "in"), ind)
     shutil.copytree(os.path.join(REPO, "sdmd_gb300", "data", "Library_Ding"), ind / "Library_Ding")
     outd.mkdir()
+    for k in range(3):   # a continue run reads each replica's checkpoint from the output folder
+        if (ind / f"savedData{k}.dat").exists():
+            shutil.copy(ind / f"savedData{k}.dat", outd / f"savedData{k}.dat")
     launch = dict(line.split(" ", 1) for line in open(os.path.join(CASE, "expected", "launch.txt")).read().splitlines())
     env = dict(os.environ, SDMD_DEBUG_RANDOM="1", SDMD_SERVER_SEED=launch["server_seed"].strip())
     cmd = [build.REMD_APP, "-f", str(ind / "REMDConfig.txt"), "-args", "sDMD", "-i", str(ind), "-o", str(outd), "-f",
@@ -50,8 +57,10 @@ def test_launcher_writes_the_reference_replicas_outputs(tmp_path):
         mine = (outd / f"out_log{k}.txt").read_text().splitlines()
         ref = open(os.path.join(CASE, "expected", f"out_log{k}.txt")).read().splitlines()
         assert mine[0].startswith("#Log file at ") and mine[1:] == ref[1:]
-        walk_sysinfo((outd / f"SysInfo{k}.dat").read_bytes(),
-                     open(os.path.join(CASE, "expected", "SysInfo0.dat"), "rb").read())
+        expected_sys = os.path.join(CASE, "expected", "SysInfo0.dat")   # a new run's only
+        assert (outd / f"SysInfo{k}.dat").exists() == os.path.exists(expected_sys)
+        if os.path.exists(expected_sys):
+            walk_sysinfo((outd / f"SysInfo{k}.dat").read_bytes(), open(expected_sys, "rb").read())
         bad = differing_defined_bytes((outd / f"savedData{k}.dat").read_bytes(),
                                       open(os.path.join(CASE, "expected", f"savedData{k}.dat"), "rb").read())
         assert len(bad) == 0, f"savedData{k}.dat differs at {bad[:5]}"
