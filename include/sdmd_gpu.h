@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SDMD_ABI_VERSION 1
+#define SDMD_ABI_VERSION 2
 
 /* ---- status codes ---------------------------------------------------------- */
 #define SDMD_OK              0
@@ -48,7 +48,7 @@ extern "C" {
 /* ---- event / sub-event enums (values of src/DMD.h:162-190) ----------------- */
 enum {
     SDMD_EV_COLLISION = 0, SDMD_EV_BOND = 1, SDMD_EV_HB = 2, SDMD_EV_HBNEIGHBOR = 3,
-    SDMD_EV_THERMOSTAT = 4, SDMD_EV_WALL = 5, SDMD_EV_PCC = 10, SDMD_EV_INVALID = 15
+    SDMD_EV_THERMOSTAT = 4, SDMD_EV_WALL = 5, SDMD_EV_SPHOBST = 9, SDMD_EV_PCC = 10, SDMD_EV_INVALID = 15
 };
 enum {
     SDMD_SUB_CORE = 0, SDMD_SUB_WELL_BOUNCE = 1, SDMD_SUB_WELL_CAPTURE = 2,
@@ -61,6 +61,7 @@ enum { SDMD_WALL_NONE = 0, SDMD_WALL_PARALLEL = 1, SDMD_WALL_CYLINDER = 2, SDMD_
 #define SDMD_NTYPES   33     /* NATOMTYPE + 1 (src/DMD.h:29) */
 #define SDMD_NTABLES  12     /* table 0: collision pairs; 1..11: HB classes (src/DMD.c:98-99) */
 #define SDMD_INVALID  (-111) /* src/DMD.h:28 */
+#define SDMD_MAX_SPHOBST 64  /* spherical obstacles per system */
 #define SDMD_INFINIT  1e8    /* src/DMD.h:26 */
 #define SDMD_ZERO     1e-8   /* src/DMD.h:27 */
 
@@ -150,6 +151,13 @@ typedef struct sdmd_system {
     double        time;            /* currenttime */
     sdmd_rng      rng;
     sdmd_counters counters;
+
+    /* ---- spherical obstacles (SphObst?, src/Initialization.c:703-724), ABI 2 ----
+     * Fixed hard spheres: SphObstTime / SphObstEvent (src/TimePrediction.c:1020-1071,
+     * src/Events.c:752-795); an atom's event with obstacle n has partner -1000 n
+     * and counts as a wall event.  sphobst: x, y, z, radius per obstacle. */
+    int32_t        n_sphobst;      /* 0 .. SDMD_MAX_SPHOBST */
+    const double  *sphobst;
 } sdmd_system;
 
 /* one record per popped event; same fields as the reference trace */

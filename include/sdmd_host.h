@@ -35,7 +35,9 @@ typedef struct sdmd_params {
     char   wall_exist[20];         /* "no" or "smooth" */
     char   wall_type[20];          /* "no", "parallel", "cylinder", "sphere" */
     char   wall_dyn[16];           /* "no" */
-    char   flow[32], obstruct[32], tunnel[32], sphobst[32];   /* "no" */
+    char   flow[32], obstruct[32], tunnel[32], sphobst[32];   /* "no", or the count of spherical obstacles */
+    int32_t n_sphobst;                              /* SphObst?: x y z diameter per obstacle, stored */
+    double  sphobst_xyzr[4 * SDMD_MAX_SPHOBST];     /* as x, y, z, radius (src/Initialization.c:703-724) */
 } sdmd_params;
 
 typedef struct sdmd_host_system sdmd_host_system;   /* owns every array of an sdmd_system */

@@ -600,6 +600,27 @@ static void wall_time(sdmd_system *s, int i) {
     job_assign(s, i, 0, &c, SDMD_EV_WALL);
 }
 
+/* SphObstTime (src/TimePrediction.c:1020-1071): a core collision with each fixed
+ * sphere the atom approaches (absolute coordinates, no periodic image); the event's
+ * partner becomes -1000 n when obstacle n gives the new earliest event. */
+static void sphobst_time(sdmd_system *s, int i) {
+    for (int n = 0; n < s->n_sphobst; n++) {
+        const double *o = s->sphobst + 4 * n;
+        kin k;
+        k.rx = s->x[i] - o[0]; k.ry = s->y[i] - o[1]; k.rz = s->z[i] - o[2];
+        const double vx = s->vx[i] - 0.0, vy = s->vy[i] - 0.0, vz = s->vz[i] - 0.0;
+        k.r2 = k.rx * k.rx + k.ry * k.ry + k.rz * k.rz;
+        k.b = k.rx * vx + k.ry * vy + k.rz * vz;
+        k.v2 = vx * vx + vy * vy + vz * vz;
+        const double lo = o[3] * o[3];
+        if (!(k.b < 0 && disc(&k, lo) > 0)) continue;
+        cand c = {INFINIT, 0, SDMD_SUB_CORE};
+        c.time = root(&k, -1, lo);
+        if (c.time < 0) { fail(SDMD_ENEGTIME, i); return; }
+        if (job_assign(s, i, 0, &c, SDMD_EV_SPHOBST)) s->ev_partner[i] = -1000 * n;
+    }
+}
+
 /* Predict (src/SGThread.c:158-211) with ResetTarget (src/ToolFunctions.c:504-514) */
 static void predict(sdmd_system *s, const int *list, int n) {
     for (int q = 0; q < n; q++) {
@@ -615,6 +636,7 @@ static void predict(sdmd_system *s, const int *list, int n) {
         hb_time(s, i);
         hbnb_time(s, i);
         if (s->wall) wall_time(s, i);
+        if (s->n_sphobst) sphobst_time(s, i);
     }
 }
 
@@ -857,6 +879,23 @@ static void wall_event(sdmd_system *s, int t) {
     s->vx[t] = s->vx[t] + phi * r[0]; s->vy[t] = s->vy[t] + phi * r[1]; s->vz[t] = s->vz[t] + phi * r[2];
 }
 
+/* SphObstEvent (src/Events.c:752-795): the core bounce off fixed sphere
+ * -partner / 1000 */
+static void sphobst_event(sdmd_system *s, int t) {
+    const int n = s->ev_partner[t] / -1000;
+    if (n < 0 || n >= s->n_sphobst || s->ev_sub[t] != SDMD_SUB_CORE) { fail(SDMD_EEVENTTYPE, t); return; }
+    const double *o = s->sphobst + 4 * n;
+    double r[3] = {s->x[t] - o[0], s->y[t] - o[1], s->z[t] - o[2]};
+    double w[3] = {s->vx[t] - 0.0, s->vy[t] - 0.0, s->vz[t] - 0.0};
+    double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    double b = r[0] * w[0] + r[1] * w[1] + r[2] * w[2];
+    const double pot = 0;
+    const int sv = 1;
+    double phi = (-1 * b + sv * sqrt(b * b - 2 * d2 * pot / s->mass[t])) / d2;
+    if (isnan(phi)) { fail(SDMD_ENAN, t); return; }
+    s->vx[t] = s->vx[t] + phi * r[0]; s->vy[t] = s->vy[t] + phi * r[1]; s->vz[t] = s->vz[t] + phi * r[2];
+}
+
 /* DoEvent (src/Events.c:25-114) */
 static void do_event(sdmd_system *s, int t, int p) {
     switch (s->ev_type[t]) {
@@ -872,6 +911,7 @@ static void do_event(sdmd_system *s, int t, int p) {
         case SDMD_EV_THERMOSTAT: thermostat_event(s, t); s->counters.thermostat++; break;
         case SDMD_EV_PCC: pcc_event(s, t); s->counters.pcc++; break;
         case SDMD_EV_WALL: wall_event(s, t); s->counters.wall++; break;
+        case SDMD_EV_SPHOBST: sphobst_event(s, t); s->counters.wall++; break;   /* walleventsum */
         default: fail(SDMD_EEVENTTYPE, t); break;
     }
 }

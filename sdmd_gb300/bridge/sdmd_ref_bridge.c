@@ -78,6 +78,10 @@ int sdmd_bridge_fill(sdmd_system *s, sdmd_bridge **owner) {
     } else if (strcmp(wallExist, "no")) {
         return SDMD_EUNSUPPORTED;
     }
+    /* outside the engine: obstructions, tunnels, flow, CG models, dynamic walls */
+    if (obstObj.mark || tunlObj.mark || flow.mark || CG.mark || strcmp(wallDyn.mark, "no") ||
+        (SphObstObj.mark && (SphObstObj.num < 0 || SphObstObj.num > SDMD_MAX_SPHOBST)))
+        return SDMD_EUNSUPPORTED;
     sdmd_bridge *b = calloc(1, sizeof *b);
     if (!b) return SDMD_ENOMEM;
     memset(s, 0, sizeof *s);
@@ -106,6 +110,15 @@ int sdmd_bridge_fill(sdmd_system *s, sdmd_bridge **owner) {
     s->hb_barrier[2] = HBPotential.SS_v;
 
 #define T(type, n) ((type *)take(b, sizeof(type) * (size_t)(n)))
+    if (SphObstObj.mark) {   /* spherical obstacles: x, y, z, radius each */
+        double *sph = T(double, 4 * (size_t)SphObstObj.num);
+        for (int k = 0; k < SphObstObj.num; k++) {
+            for (int d = 0; d < 3; d++) sph[4 * k + d] = SphObstObj.position[k][d + 1];
+            sph[4 * k + 3] = SphObstObj.radius[k];
+        }
+        s->n_sphobst = SphObstObj.num;
+        s->sphobst = sph;
+    }
     double *mass = T(double, N1);
     int32_t *protein = T(int32_t, N1), *aanum = T(int32_t, N1), *aatype = T(int32_t, N1);
     int32_t *hb_neighbor = T(int32_t, N1), *hb_role = T(int32_t, N1), *ncode = T(int32_t, N1);

@@ -21,7 +21,7 @@
 using namespace sdmd;
 
 struct SysMeta {
-    int32_t n, ncell, n_bonds, n_cons, n_con_steps, n_conn, n_pair_steps, nbcap;
+    int32_t n, ncell, n_bonds, n_cons, n_con_steps, n_conn, n_pair_steps, nbcap, n_sph;
 };
 
 struct sdmd_gpu {
@@ -116,6 +116,11 @@ static int validate(const sdmd_system &s) {
         (s.n_conn && (!s.conn_j || !s.conn_bits)))
         return SDMD_EINVAL;
     if (s.wall < 0 || s.wall > SDMD_WALL_SPHERE || s.thermostat < 0 || s.thermostat > 1) return SDMD_EUNSUPPORTED;
+    if (s.n_sphobst < 0 || s.n_sphobst > SDMD_MAX_SPHOBST || (s.n_sphobst && !s.sphobst)) return SDMD_EINVAL;
+    for (int k = 0; k < s.n_sphobst; k++)
+        if (!(s.sphobst[4 * k + 3] > 0) || !std::isfinite(s.sphobst[4 * k]) || !std::isfinite(s.sphobst[4 * k + 1]) ||
+            !std::isfinite(s.sphobst[4 * k + 2]))
+            return SDMD_EINVAL;
     // the RNG must be a reachable glibc state: never all zero
     bool nz = false;
     for (int k = 0; k < 31; k++) nz |= s.rng.tab[k] != 0;
@@ -447,6 +452,7 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             d.pair_thr32 = o.pair_thr32; d.pair_step32 = o.pair_step32;
             d.pair_key = o.pair_key; d.pair_stepkey = o.pair_stepkey; d.rp_idx = o.rp_idx;
         }
+        d.sph = m.n_sph ? cv.take<double>(4 * (size_t)m.n_sph) : nullptr;
         d.con_thr32 = cv.take<float>(((size_t)m.n_cons + 1) * 8);
         d.con_step32 = cv.take<float>(((size_t)m.n_con_steps + 1) * 6);
         d.bond32 = cv.take<float>(((size_t)m.n_bonds + 1) * 4);
@@ -478,6 +484,7 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
         if (copies) {
             auto &c = *copies;
             put(c, (double *)d.mass, s.mass, N1);
+            if (m.n_sph) put(c, (double *)d.sph, s.sphobst, 4 * (size_t)m.n_sph);
             put(c, (int32_t *)d.protein, s.protein, N1); put(c, (int32_t *)d.aanum, s.aanum, N1);
             put(c, (int32_t *)d.aatype, s.aatype, N1); put(c, (int32_t *)d.hb_neighbor, s.hb_neighbor, N1);
             put(c, (int32_t *)d.hb_role, s.hb_role, N1); put(c, (int32_t *)d.name_code, s.name_code, N1);
@@ -645,6 +652,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         m.ncell = s.cellnum[0] * s.cellnum[1] * s.cellnum[2];
         m.n_bonds = s.n_bonds; m.n_cons = s.n_cons; m.n_con_steps = s.n_con_steps; m.n_conn = s.n_conn;
         m.n_pair_steps = s.n_pair_steps;
+        m.n_sph = s.n_sphobst;
         m.nbcap = cap_of(k, head_num, head_den);
         nbcap_max = std::max(nbcap_max, m.nbcap);
         DSys &d = h->hs[k];
@@ -655,6 +663,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
             d.wall_pos[q] = s.wall_pos[q]; d.wall_vel[q] = s.wall_vel[q]; d.hb_barrier[q] = s.hb_barrier[q];
         }
         d.thermostat = s.thermostat; d.wall = s.wall; d.wall_type = s.wall_type;
+        d.n_sph = s.n_sphobst;
         d.cutoff = s.cutoff; d.temperature = s.temperature; d.thermo_freq = s.thermo_freq; d.t_end = s.t_end;
         d.nbcap = m.nbcap;
         d.n_bonds = s.n_bonds; d.n_cons = s.n_cons; d.n_con_steps = s.n_con_steps; d.n_conn = s.n_conn;

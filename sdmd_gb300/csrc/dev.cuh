@@ -74,6 +74,8 @@ struct DSys {
     int32_t thermostat, wall, wall_type;
     double box[3], cs[3], cutoff, temperature, thermo_freq, t_end;
     double wall_pos[3], wall_vel[3], hb_barrier[3];
+    int32_t n_sph;                 // spherical obstacles: x, y, z, radius each
+    const double *sph;
     // static
     const double *mass;
     const int32_t *protein, *aanum, *aatype, *hb_neighbor, *hb_role, *name_code;

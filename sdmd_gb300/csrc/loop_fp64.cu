@@ -440,6 +440,27 @@ __device__ __noinline__ void wall_time(const DSys &S, int i, Cur &c, Blk &B, int
     job_assign(S, c, 0, t, pot, sub, SDMD_EV_WALL);
 }
 
+// SphObstTime, spherical obstacles (src/TimePrediction.c:1020-1071): a core
+// collision with each fixed sphere the atom approaches (absolute coordinates, no
+// periodic image); the partner becomes -1000 n when obstacle n gives the new
+// earliest event
+__device__ __noinline__ void sphobst_time(const DSys &S, int i, Cur &c, Blk &B) {
+    for (int n = 0; n < S.n_sph; n++) {
+        const double *o = S.sph + 4 * n;
+        Kin k;
+        k.rx = S.x[i] - o[0]; k.ry = S.y[i] - o[1]; k.rz = S.z[i] - o[2];
+        const double vx = S.vx[i] - 0.0, vy = S.vy[i] - 0.0, vz = S.vz[i] - 0.0;
+        k.r2 = k.rx * k.rx + k.ry * k.ry + k.rz * k.rz;
+        k.b = k.rx * vx + k.ry * vy + k.rz * vz;
+        k.v2 = vx * vx + vy * vy + vz * vz;
+        const double lo = o[3] * o[3];
+        if (!(k.b < 0 && disc(k, lo) > 0)) continue;
+        const double t = root(k, -1, lo);
+        if (t < 0) { set_err(B, SDMD_ENEGTIME, i); return; }
+        if (job_assign(S, c, 0, t, 0.0, SDMD_SUB_CORE, SDMD_EV_SPHOBST)) c.partner = -1000 * n;
+    }
+}
+
 // ---- Predict for one atom (ResetTarget already applied) ---------------------
 struct Shm {
     int32_t *nbj, *cnt;
@@ -494,6 +515,7 @@ __device__ __noinline__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, 
     if (tid == 0) {
         hbnb_time(S, i, c, B, &bad);
         if (S.wall) wall_time(S, i, c, B, &bad);
+        if (S.n_sph) sphobst_time(S, i, c, B);
         cur_store(S, i, c);
     }
     if (bad) set_err(B, SDMD_EHBMAP, i);
@@ -735,6 +757,22 @@ __device__ void wall_event(const DSys &S, int t, Blk &B) {
     S.vx[t] = S.vx[t] + phi * r[0]; S.vy[t] = S.vy[t] + phi * r[1]; S.vz[t] = S.vz[t] + phi * r[2];
 }
 
+// SphObstEvent (src/Events.c:752-795): the core bounce off fixed sphere -partner / 1000
+__device__ void sphobst_event(const DSys &S, int t, Blk &B) {
+    const int n = S.ev_partner[t] / -1000;
+    if (n < 0 || n >= S.n_sph || S.ev_sub[t] != SDMD_SUB_CORE) { set_err(B, SDMD_EEVENTTYPE, t); return; }
+    const double *o = S.sph + 4 * n;
+    const double r[3] = {S.x[t] - o[0], S.y[t] - o[1], S.z[t] - o[2]};
+    const double w[3] = {S.vx[t] - 0.0, S.vy[t] - 0.0, S.vz[t] - 0.0};
+    const double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    const double b = r[0] * w[0] + r[1] * w[1] + r[2] * w[2];
+    const double pot = 0;
+    const int sv = 1;
+    const double phi = (-1 * b + sv * sqrt(b * b - 2 * d2 * pot / S.mass[t])) / d2;
+    if (isnan(phi)) { set_err(B, SDMD_ENAN, t); return; }
+    S.vx[t] = S.vx[t] + phi * r[0]; S.vy[t] = S.vy[t] + phi * r[1]; S.vz[t] = S.vz[t] + phi * r[2];
+}
+
 // DoEvent (src/Events.c:25-114)
 __device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, int32_t *moved = nullptr) {
     int bad = 0;
@@ -751,6 +789,7 @@ __device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, int32_t 
         case SDMD_EV_THERMOSTAT: thermostat_event(S, t, C, B); C.c.thermostat++; break;
         case SDMD_EV_PCC: pcc_event(S, t, B, moved); C.c.pcc++; break;
         case SDMD_EV_WALL: wall_event(S, t, B); C.c.wall++; break;
+        case SDMD_EV_SPHOBST: sphobst_event(S, t, B); C.c.wall++; break;   // walleventsum
         default: set_err(B, SDMD_EEVENTTYPE, t); break;
     }
     if (bad) set_err(B, SDMD_EHBMAP, t);

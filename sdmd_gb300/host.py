@@ -22,7 +22,8 @@ class sdmd_params(C.Structure):
                 ("force_field", C.c_char * 20), ("thermostat", C.c_char * 20), ("thermo_freq", C.c_double),
                 ("cg", C.c_char * 16), ("wall_exist", C.c_char * 20), ("wall_type", C.c_char * 20),
                 ("wall_dyn", C.c_char * 16), ("flow", C.c_char * 32), ("obstruct", C.c_char * 32),
-                ("tunnel", C.c_char * 32), ("sphobst", C.c_char * 32)]
+                ("tunnel", C.c_char * 32), ("sphobst", C.c_char * 32),
+                ("n_sphobst", C.c_int32), ("sphobst_xyzr", C.c_double * (4 * 64))]
 
 
 _lib = None
@@ -96,6 +97,9 @@ def _copy_out(view, names_ptr, res_ptr):
                     wall_mass=s.wall_mass, wall_type=s.wall_type, hb_barrier=list(s.hb_barrier),
                     n_bonds=s.n_bonds, n_cons=s.n_cons, n_con_steps=s.n_con_steps, n_conn=s.n_conn,
                     n_pair_steps=s.n_pair_steps)
+    nsph = s.n_sphobst if s.sphobst else 0
+    out.a["sphobst"] = np.array(np.ctypeslib.as_array(s.sphobst, shape=(4 * nsph,)), np.float64) if nsph \
+        else np.zeros(0)
     out.pull_scalars(s)
     out.names = C.string_at(names_ptr, 8 * (n + 1)) if names_ptr else None
     out.resnames = C.string_at(res_ptr, 8 * (n + 1)) if res_ptr else None

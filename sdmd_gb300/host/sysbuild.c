@@ -65,6 +65,7 @@ struct sdmd_host_system {
     char method[20];
     double hbpot[6];
     char wall_name[8], wall_ext[32];   /* the Wall.txt record of a smooth wall */
+    double sphobst[4 * SDMD_MAX_SPHOBST];
 };
 
 typedef struct {
@@ -241,8 +242,29 @@ int sdmd_read_parameters(const char *path, sdmd_params *p) {
     for (int k = 0; k < 4; k++) {
         getline_(&c, line, sizeof line);
         char v[32] = "";
-        if (sscanf(line, "%1023s %31s", s, v) < 2) ok = 0;
+        int pos = 0;
+        if (sscanf(line, "%1023s %31s%n", s, v, &pos) < 2) ok = 0;
         snprintf(dst[k], 32, "%s", v);
+        if (k == 3 && ok && strcmp(v, "no")) {
+            /* the count, then "x y z diameter" per obstacle with a separator token
+               between them; the radius is kept (src/Initialization.c:703-724) */
+            const int n = atoi(v);
+            if (n < 0 || n > SDMD_MAX_SPHOBST) { ok = 0; break; }
+            const char *q = line + pos;
+            for (int i = 0; i < n && ok; i++) {
+                double *o = &p->sphobst_xyzr[4 * i];
+                int used = 0;
+                if (sscanf(q, "%lf%lf%lf%lf%n", &o[0], &o[1], &o[2], &o[3], &used) < 4) { ok = 0; break; }
+                o[3] /= 2;
+                q += used;
+                if (i != n - 1) {
+                    char sep[64];
+                    if (sscanf(q, "%63s%n", sep, &used) < 1) { ok = 0; break; }
+                    q += used;
+                }
+            }
+            p->n_sphobst = n;
+        }
     }
     free(c.buf);
     return ok ? SDMD_OK : SDMD_EINVAL;
@@ -898,6 +920,11 @@ static int export_system(B *b, sdmd_host_system **out) {
     s->t_end = p->time;
     s->thermostat = strcmp(p->thermostat, "no") ? 1 : 0;
     s->wall = b->wall; s->wall_type = b->wall_type; s->wall_mass = b->wall_mass;
+    if (strcmp(p->sphobst, "no")) {   /* SphObst? (src/Initialization.c:703-724) */
+        s->n_sphobst = p->n_sphobst;
+        memcpy(h->sphobst, p->sphobst_xyzr, sizeof(double) * 4 * (size_t)p->n_sphobst);
+        s->sphobst = h->sphobst;
+    }
     s->hb_barrier[0] = b->hbpot[1]; s->hb_barrier[1] = b->hbpot[5]; s->hb_barrier[2] = b->hbpot[3];
 #define A(name, T, cnt) h->name = zalloc(sizeof(T) * (cnt)); s->name = h->name
     A(mass, double, N1); A(protein, int32_t, N1); A(aanum, int32_t, N1); A(aatype, int32_t, N1);
@@ -1066,8 +1093,8 @@ static int build(B *b, cur *coords, uint32_t seed, int emin, sdmd_host_system **
     if (strcmp(p->continue_mode, "new")) return fail(b, "only \"new\" runs are built here (continue runs load a checkpoint)");
     if (strncmp(p->force_field, "Ding", 1)) return fail(b, "only the Ding force field is supported");
     if (strcmp(p->cg, "no") || strcmp(p->flow, "no") || strcmp(p->obstruct, "no") || strcmp(p->tunnel, "no") ||
-        strcmp(p->sphobst, "no") || strcmp(p->wall_dyn, "no"))
-        return fail(b, "CG models, flow, obstructions, tunnels, spherical obstacles and dynamic walls are outside the engine's scope");
+        strcmp(p->wall_dyn, "no"))
+        return fail(b, "CG models, flow, obstructions, tunnels and dynamic walls are outside the engine's scope");
     snprintf(b->ff, sizeof b->ff, "%s", p->force_field);
     b->wall = 0;
     if (strcmp(p->wall_exist, "no")) {

@@ -328,8 +328,19 @@ int sdmd_write_log_replica(const char *path, const sdmd_host_system *h, const sd
     fprintf(f, "                      No obstruction.\n");
     fprintf(f, "Tunnel              = %-5i\n", 0);
     fprintf(f, "                      No tunnel.\n");
-    fprintf(f, "ColumnObstacles     = %-5i\n", 0);
-    fprintf(f, "                      No column.\n");
+    const int columns = strcmp(p->sphobst, "no") != 0;   /* SphObstObj.mark */
+    fprintf(f, "ColumnObstacles     = %-5i\n", columns);
+    if (!columns) {
+        fprintf(f, "                      No column.\n");
+    } else {
+        fprintf(f, "ColumnInfo          =");
+        for (int i = 0; i < p->n_sphobst; i++) {
+            const double *o = &p->sphobst_xyzr[4 * i];
+            fprintf(f, "%-8.2lf%-8.2lf%-8.2lf%-8.2lf\n", o[0], o[1], o[2], o[3] * 2);
+            if (i < p->n_sphobst - 1) fprintf(f, ", ");
+        }
+        fprintf(f, "\n");
+    }
     fprintf(f, "RandomSeed          = %i\n", (int)seed);
     /* REMDInfo: the -REMD flag's values, else its initializer (src/DMD.c:126-132) */
     fprintf(f, "REMDPortNum         = %i\n", r ? (int)r->port : -1);

@@ -66,7 +66,10 @@ class sdmd_system(C.Structure):
     _fields_ = (_SCALARS_HEAD
                 + [(n, _PTR[t]) for n, t in STATIC_ARRAYS]
                 + [(n, _PTR[t]) for n, t in DYNAMIC_ARRAYS]
-                + [("time", C.c_double), ("rng", sdmd_rng), ("counters", sdmd_counters)])
+                + [("time", C.c_double), ("rng", sdmd_rng), ("counters", sdmd_counters)]
+                + [("n_sphobst", C.c_int32), ("sphobst", f64p)])
+
+MAX_SPHOBST = 64   # SDMD_MAX_SPHOBST
 
 
 class sdmd_trace_rec(C.Structure):
@@ -185,6 +188,12 @@ class System:
             self._ptrs = np.array([arr.__array_interface__["data"][0] for arr in arrs], np.uint64)
             self._ptr_arrays = arrs
         np.frombuffer(s, np.uint64, C.sizeof(sdmd_system) // 8)[_SLOT_INDEX] = self._ptrs
+        sph = self.a.get("sphobst")
+        if sph is not None and len(sph):   # spherical obstacles: x, y, z, radius each
+            if sph.dtype != np.float64 or not sph.flags.c_contiguous or len(sph) % 4:
+                raise ValueError("array sphobst: need C-contiguous float64, 4 per obstacle")
+            s.n_sphobst = len(sph) // 4
+            s.sphobst = sph.ctypes.data_as(f64p)
         s.time = self.time
         rng = np.ascontiguousarray(self.rng, np.int32)
         C.memmove(C.addressof(s.rng), rng.ctypes.data, 33 * 4)
@@ -269,12 +278,30 @@ def from_fixture(npz, stage="pre", dynamic_stage=None):
     a["bond_off"][0] = 0
     a["con_off"][0] = 0
     a["conn_off"], a["conn_j"], a["conn_bits"] = _conn_rows(n, g("connmap"))
+    a["sphobst"] = sphobst_from_parameters(bytes(d["meta/parameter"]).decode()) if "meta/parameter" in d.files \
+        else np.zeros(0)
     _load_dynamic(s, d, ds)
     s.rng = d["meta/rng_pre"].astype(np.int32).copy() if ds == "pre" else np.zeros(33, np.int32)
     for k, v in [("n_bonds", len(a["bond_j"])), ("n_cons", len(a["con_j"])), ("n_con_steps", len(a["con_step_d"])),
                  ("n_conn", len(a["conn_j"])), ("n_pair_steps", len(a["pair_step_d"]))]:
         s.scal[k] = int(v)
     return s
+
+
+def sphobst_from_parameters(text):
+    """The SphObst? line of parameter.txt (its 16th line) as the reference reads it
+    (src/Initialization.c:703-724): the count, then x y z diameter per obstacle with
+    a separator token between them; returned as x, y, z, radius per obstacle."""
+    lines = text.splitlines()
+    words = lines[15].split() if len(lines) > 15 else []
+    if len(words) < 2 or words[1] == "no":
+        return np.zeros(0)
+    n, out, q = int(words[1]), [], 2
+    for i in range(n):
+        x, y, z, dia = (float(v) for v in words[q:q + 4])
+        out += [x, y, z, dia / 2]
+        q += 4 + (1 if i != n - 1 else 0)
+    return np.array(out, np.float64)
 
 
 def _load_dynamic(s, d, ds):

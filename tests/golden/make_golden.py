@@ -50,7 +50,7 @@ WallDyn            no
 Flow               no
 Obstruct?          no
 Tunnel?            no
-SphObst?           no
+SphObst?           {sphobst}
 """
 
 _DT = {"d": np.float64, "q": np.int64, "i": np.int32, "b": np.uint8}
@@ -172,7 +172,7 @@ def rng_state_after(seed, calls):
 
 def base_params(**kw):
     p = dict(time=5000, temp=0.6, dump=1e9, cutoff=9.0, thermostat="Andersen", thermo_freq=6.0,
-             wall_exist="no", wall_type="no")
+             wall_exist="no", wall_type="no", sphobst="no")
     p.update(kw)
     return p
 

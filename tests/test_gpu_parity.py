@@ -41,7 +41,7 @@ def assert_state_equal(a, ref, keys=DYN):
 
 
 @SCREENS
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "ala10_sph"])
 def test_sweep_matches_reference(golden, engine_mod, case, screen):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -53,7 +53,7 @@ def test_sweep_matches_reference(golden, engine_mod, case, screen):
 
 
 @SCREENS
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "ala10_sph"])
 def test_loop_matches_reference_event_for_event(golden, engine_mod, case, screen):
     d = golden(case)
     ids, dts = d["trace/ids"], d["trace/dt"]
@@ -77,6 +77,8 @@ def test_loop_matches_reference_event_for_event(golden, engine_mod, case, screen
     assert s.time == ref["_time"]
     if case == "ala10_cyl":   # WallTime / WallEvent in the cylinder (axis x)
         assert s.counters["wall"] > 0
+    if case == "ala10_sph":   # SphObstTime / SphObstEvent
+        assert ((ids[:, 2] == 9) & (ids[:, 4] == 1)).sum() > 0
 
 
 @SCREENS

@@ -28,7 +28,8 @@ def assert_state_equal(sys_, ref, keys=DYN):
             raise AssertionError(f"{k} differs at {idx}: {a[idx]} vs {b[idx]}")
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "mixed6", "sheet2"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "mixed6", "sheet2",
+                                  "ala10_sph"])
 def test_sweep_and_tree(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -39,7 +40,7 @@ def test_sweep_and_tree(golden, case):
     assert np.array_equal(node, d["cbt/cbt_node"]) and np.array_equal(leaf, d["cbt/cbt_leaf"])
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "mixed6"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "mixed6", "ala10_sph"])
 def test_trace_event_for_event(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -61,6 +62,8 @@ def test_trace_event_for_event(golden, case):
     assert s.counters == ref["_counters"] and s.time == ref["_time"]
     if case == "ala10_cyl":   # the smooth cylinder wall (WallTime / WallEvent) is exercised
         assert s.counters["wall"] > 0
+    if case == "ala10_sph":   # spherical obstacles (SphObstTime / SphObstEvent) are exercised
+        assert ((ids[:, 2] == 9) & (ids[:, 4] == 1)).sum() > 0 and s.counters["wall"] > 0
 
 
 @pytest.mark.parametrize("case", ["ala10_nvt_long", "sheet2"])

@@ -103,7 +103,7 @@ def _child_log(case, q):
         q.put(("error", repr(e)))
 
 
-@pytest.mark.parametrize("case", ["ala10_nvt", "sheet2", "ala10_cyl", "mixed6"])
+@pytest.mark.parametrize("case", ["ala10_nvt", "sheet2", "ala10_cyl", "mixed6", "ala10_sph"])
 def test_log_matches_the_reference(case, tmp_path):
     """out_log.txt from the host library equals the reference's SaveLog output
     line for line after the first, which carries the wall-clock time."""
