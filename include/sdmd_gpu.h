@@ -48,7 +48,8 @@ extern "C" {
 /* ---- event / sub-event enums (values of src/DMD.h:162-190) ----------------- */
 enum {
     SDMD_EV_COLLISION = 0, SDMD_EV_BOND = 1, SDMD_EV_HB = 2, SDMD_EV_HBNEIGHBOR = 3,
-    SDMD_EV_THERMOSTAT = 4, SDMD_EV_WALL = 5, SDMD_EV_SPHOBST = 9, SDMD_EV_PCC = 10, SDMD_EV_INVALID = 15
+    SDMD_EV_THERMOSTAT = 4, SDMD_EV_WALL = 5, SDMD_EV_OBST = 6, SDMD_EV_SPHOBST = 9, SDMD_EV_PCC = 10,
+    SDMD_EV_INVALID = 15
 };
 enum {
     SDMD_SUB_CORE = 0, SDMD_SUB_WELL_BOUNCE = 1, SDMD_SUB_WELL_CAPTURE = 2,
@@ -62,6 +63,7 @@ enum { SDMD_WALL_NONE = 0, SDMD_WALL_PARALLEL = 1, SDMD_WALL_CYLINDER = 2, SDMD_
 #define SDMD_NTABLES  12     /* table 0: collision pairs; 1..11: HB classes (src/DMD.c:98-99) */
 #define SDMD_INVALID  (-111) /* src/DMD.h:28 */
 #define SDMD_MAX_SPHOBST 64  /* spherical obstacles per system */
+#define SDMD_MAX_OBST    16  /* obstruction walls per system */
 #define SDMD_INFINIT  1e8    /* src/DMD.h:26 */
 #define SDMD_ZERO     1e-8   /* src/DMD.h:27 */
 
@@ -158,6 +160,16 @@ typedef struct sdmd_system {
      * and counts as a wall event.  sphobst: x, y, z, radius per obstacle. */
     int32_t        n_sphobst;      /* 0 .. SDMD_MAX_SPHOBST */
     const double  *sphobst;
+
+    /* ---- obstruction walls (Obstruct?, src/Initialization.c:634-672), ABI 2 ----
+     * Planes across one axis: ObstTime / ObstEvent (src/TimePrediction.c:740-829,
+     * src/Events.c:543-617) with the potential steps of the pair (atom type,
+     * wall_type); obst holds position[1..3] of each obstacle, -1 on the axes it
+     * does not cross.  An atom's event with obstacle n across axis d (1..3) has
+     * partner -d - 10 n and counts as a wall event.  Obstacles with holes (tunnels)
+     * are outside the engine. */
+    int32_t        n_obst;         /* 0 .. SDMD_MAX_OBST */
+    const double  *obst;
 } sdmd_system;
 
 /* one record per popped event; same fields as the reference trace */

@@ -38,6 +38,8 @@ typedef struct sdmd_params {
     char   flow[32], obstruct[32], tunnel[32], sphobst[32];   /* "no", or the count of spherical obstacles */
     int32_t n_sphobst;                              /* SphObst?: x y z diameter per obstacle, stored */
     double  sphobst_xyzr[4 * SDMD_MAX_SPHOBST];     /* as x, y, z, radius (src/Initialization.c:703-724) */
+    int32_t n_obst;                                 /* Obstruct?: an axis letter and a position per */
+    double  obst_pos[3 * SDMD_MAX_OBST];            /* obstacle, stored as position[1..3], -1 elsewhere */
 } sdmd_params;
 
 typedef struct sdmd_host_system sdmd_host_system;   /* owns every array of an sdmd_system */
@@ -225,6 +227,9 @@ int sdmd_write_sysinfo(const char *path, const sdmd_host_system *h);
  *                      smooth wall's atom record (property and dynamic records) as
  *                      ReadWall builds it; SDMD_EINVAL for a system without a wall */
 int sdmd_write_wallinfo(const char *path, const sdmd_host_system *h);
+/*   sdmd_write_obstinfo ObstInfo.dat    SaveObstInfo (src/DataSave.c:294-308): each
+ *                      obstruction wall's atom record; SDMD_EINVAL without one */
+int sdmd_write_obstinfo(const char *path, const sdmd_host_system *h);
 
 #ifdef __cplusplus
 }

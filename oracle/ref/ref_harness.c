@@ -276,6 +276,14 @@ static void dump_static(void) {
         sec_i("wall_type", wall[0].property->typeofAtom);
         sec_d("wall_mass", wall[0].property->mass);
     }
+    if (obstObj.mark && obstObj.num > 0) {   /* obstruction walls: their atom type and planes */
+        sec_i("obst_type", obstObj.obst[0].property->typeofAtom);
+        double *op = calloc(3 * (size_t)obstObj.num, sizeof(double));
+        for (int n = 0; n < obstObj.num; n++)
+            for (int k = 0; k < 3; k++) op[3 * n + k] = obstObj.position[n][k + 1];
+        sec("obst_pos", 'd', 3 * obstObj.num, op);
+        free(op);
+    }
     free(v); free(d);
 }
 

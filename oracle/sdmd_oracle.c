@@ -600,6 +600,44 @@ static void wall_time(sdmd_system *s, int i) {
     job_assign(s, i, 0, &c, SDMD_EV_WALL);
 }
 
+/* ObstTime (src/TimePrediction.c:740-829): for each plane n across axis d, the
+ * axis component alone (the others zeroed, as the reference zeroes them) against
+ * the potential steps of the pair (atom type, wall type); the partner becomes
+ * -d - 10 n when that plane gives the new earliest event. */
+static void obst_time(sdmd_system *s, int i) {
+    const double p[3] = {s->x[i], s->y[i], s->z[i]}, v[3] = {s->vx[i], s->vy[i], s->vz[i]};
+    for (int n = 0; n < s->n_obst; n++) {
+        for (int dim = 0; dim < 3; dim++) {
+            const double pos = s->obst[3 * n + dim];
+            if (pos < 0) continue;
+            double pi[3] = {0, 0, 0}, pj[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, vj[3] = {0, 0, 0};
+            pi[dim] = p[dim]; pj[dim] = pos; vi[dim] = v[dim];
+            kin k;
+            k.rx = pi[0] - pj[0]; k.ry = pi[1] - pj[1]; k.rz = pi[2] - pj[2];
+            const double wx = vi[0] - vj[0], wy = vi[1] - vj[1], wz = vi[2] - vj[2];
+            k.r2 = k.rx * k.rx + k.ry * k.ry + k.rz * k.rz;
+            k.b = k.rx * wx + k.ry * wy + k.rz * wz;
+            k.v2 = wx * wx + wy * wy + wz * wz;
+            pairlim L;
+            const int cs = find_pair(s, i, 0, K_COLLISION, k.b, k.r2, &L, 0, 0, s->wall_type);
+            if (L.lopot == 0 && L.uppot == 0) continue;   /* inside the holes */
+            cand c = {INFINIT, 0, SDMD_SUB_INVALID};
+            int st; double d2;
+            if (k.b < 0) {
+                c.sub = cs == 0 ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
+                st = -1; d2 = L.lo; c.potential = L.lopot;
+            } else {
+                if (cs == 1) continue;
+                c.sub = SDMD_SUB_TBD_ESCAPE;
+                st = 1; d2 = L.up; c.potential = L.uppot;
+            }
+            c.time = root(&k, st, d2);
+            if (c.time < 0) { fail(SDMD_ENEGTIME, i); return; }
+            if (job_assign(s, i, 0, &c, SDMD_EV_OBST)) s->ev_partner[i] = -(dim + 1) - 10 * n;
+        }
+    }
+}
+
 /* SphObstTime (src/TimePrediction.c:1020-1071): a core collision with each fixed
  * sphere the atom approaches (absolute coordinates, no periodic image); the event's
  * partner becomes -1000 n when obstacle n gives the new earliest event. */
@@ -636,6 +674,7 @@ static void predict(sdmd_system *s, const int *list, int n) {
         hb_time(s, i);
         hbnb_time(s, i);
         if (s->wall) wall_time(s, i);
+        if (s->n_obst) obst_time(s, i);
         if (s->n_sphobst) sphobst_time(s, i);
     }
 }
@@ -879,6 +918,37 @@ static void wall_event(sdmd_system *s, int t) {
     s->vx[t] = s->vx[t] + phi * r[0]; s->vy[t] = s->vy[t] + phi * r[1]; s->vz[t] = s->vz[t] + phi * r[2];
 }
 
+/* ObstEvent (src/Events.c:543-617): plane -partner / 10 across axis -partner % 10 */
+static void obst_event(sdmd_system *s, int t) {
+    const int part = s->ev_partner[t];
+    const int n = part / -10, dim = (part * -1) % 10;
+    if (n < 0 || n >= s->n_obst || dim < 1 || dim > 3) { fail(SDMD_EEVENTTYPE, t); return; }
+    double pi[3] = {0, 0, 0}, pj[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, vj[3] = {0, 0, 0};
+    pi[dim - 1] = dim == 1 ? s->x[t] : dim == 2 ? s->y[t] : s->z[t];
+    vi[dim - 1] = dim == 1 ? s->vx[t] : dim == 2 ? s->vy[t] : s->vz[t];
+    pj[dim - 1] = s->obst[3 * n + dim - 1];
+    const double r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+    const double w[3] = {vi[0] - vj[0], vi[1] - vj[1], vi[2] - vj[2]};
+    const double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    const double b = r[0] * w[0] + r[1] * w[1] + r[2] * w[2];
+    const double mu = s->mass[t];
+    double pot = s->ev_potential[t];
+    int sv;
+    switch (s->ev_sub[t]) {
+        case SDMD_SUB_CORE: sv = 1; pot = 0; break;
+        case SDMD_SUB_TBD_CAPTURE:
+            if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = 1; } else sv = -1;
+            break;
+        case SDMD_SUB_TBD_ESCAPE:
+            if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = -1; } else sv = 1;
+            break;
+        default: fail(SDMD_EEVENTTYPE, t); return;
+    }
+    const double phi = (-1 * b + sv * sqrt(b * b - 2 * d2 * pot / s->mass[t])) / d2;
+    if (isnan(phi)) { fail(SDMD_ENAN, t); return; }
+    s->vx[t] = s->vx[t] + phi * r[0]; s->vy[t] = s->vy[t] + phi * r[1]; s->vz[t] = s->vz[t] + phi * r[2];
+}
+
 /* SphObstEvent (src/Events.c:752-795): the core bounce off fixed sphere
  * -partner / 1000 */
 static void sphobst_event(sdmd_system *s, int t) {
@@ -911,6 +981,7 @@ static void do_event(sdmd_system *s, int t, int p) {
         case SDMD_EV_THERMOSTAT: thermostat_event(s, t); s->counters.thermostat++; break;
         case SDMD_EV_PCC: pcc_event(s, t); s->counters.pcc++; break;
         case SDMD_EV_WALL: wall_event(s, t); s->counters.wall++; break;
+        case SDMD_EV_OBST: obst_event(s, t); s->counters.wall++; break;         /* walleventsum */
         case SDMD_EV_SPHOBST: sphobst_event(s, t); s->counters.wall++; break;   /* walleventsum */
         default: fail(SDMD_EEVENTTYPE, t); break;
     }

@@ -196,6 +196,16 @@ int app_start_files(app_run *r, const char *timer) {
             fprintf(stderr, "!!ERROR!!: %s\n", f);
             return 1;
         }
+        if (r->sys->n_obst) {   /* SaveObstInfo for obstruction walls (src/SGThread.c:38) */
+            char name[400];
+            with_extra(name, sizeof name, "ObstInfo.dat", r->extra);
+            backup_name(r, name, timer);
+            snprintf(f, sizeof f, "%s/%s", r->cli.savedir, name);
+            if (sdmd_write_obstinfo(f, r->hs) != SDMD_OK) {
+                fprintf(stderr, "!!ERROR!!: %s\n", f);
+                return 1;
+            }
+        }
         if (r->sys->wall) {   /* SaveWallInfo for a smooth wall (src/SGThread.c:37) */
             char name[400];
             with_extra(name, sizeof name, "WallInfo.dat", r->extra);

@@ -78,9 +78,11 @@ int sdmd_bridge_fill(sdmd_system *s, sdmd_bridge **owner) {
     } else if (strcmp(wallExist, "no")) {
         return SDMD_EUNSUPPORTED;
     }
-    /* outside the engine: obstructions, tunnels, flow, CG models, dynamic walls */
-    if (obstObj.mark || tunlObj.mark || flow.mark || CG.mark || strcmp(wallDyn.mark, "no") ||
-        (SphObstObj.mark && (SphObstObj.num < 0 || SphObstObj.num > SDMD_MAX_SPHOBST)))
+    /* outside the engine: tunnels (and so obstructions with holes), flow, CG models,
+       dynamic walls */
+    if (tunlObj.mark || flow.mark || CG.mark || strcmp(wallDyn.mark, "no") ||
+        (SphObstObj.mark && (SphObstObj.num < 0 || SphObstObj.num > SDMD_MAX_SPHOBST)) ||
+        (obstObj.mark && (obstObj.num < 0 || obstObj.num > SDMD_MAX_OBST)))
         return SDMD_EUNSUPPORTED;
     sdmd_bridge *b = calloc(1, sizeof *b);
     if (!b) return SDMD_ENOMEM;
@@ -110,6 +112,14 @@ int sdmd_bridge_fill(sdmd_system *s, sdmd_bridge **owner) {
     s->hb_barrier[2] = HBPotential.SS_v;
 
 #define T(type, n) ((type *)take(b, sizeof(type) * (size_t)(n)))
+    if (obstObj.mark && obstObj.num > 0) {   /* obstruction walls: position[1..3] each */
+        double *ob = T(double, 3 * (size_t)obstObj.num);
+        for (int k = 0; k < obstObj.num; k++)
+            for (int d = 0; d < 3; d++) ob[3 * k + d] = obstObj.position[k][d + 1];
+        s->n_obst = obstObj.num;
+        s->obst = ob;
+        if (wall_kind == SDMD_WALL_NONE) s->wall_type = obstObj.obst[0].property->typeofAtom;
+    }
     if (SphObstObj.mark) {   /* spherical obstacles: x, y, z, radius each */
         double *sph = T(double, 4 * (size_t)SphObstObj.num);
         for (int k = 0; k < SphObstObj.num; k++) {

@@ -21,7 +21,7 @@
 using namespace sdmd;
 
 struct SysMeta {
-    int32_t n, ncell, n_bonds, n_cons, n_con_steps, n_conn, n_pair_steps, nbcap, n_sph;
+    int32_t n, ncell, n_bonds, n_cons, n_con_steps, n_conn, n_pair_steps, nbcap, n_sph, n_obst;
 };
 
 struct sdmd_gpu {
@@ -121,6 +121,8 @@ static int validate(const sdmd_system &s) {
         if (!(s.sphobst[4 * k + 3] > 0) || !std::isfinite(s.sphobst[4 * k]) || !std::isfinite(s.sphobst[4 * k + 1]) ||
             !std::isfinite(s.sphobst[4 * k + 2]))
             return SDMD_EINVAL;
+    if (s.n_obst < 0 || s.n_obst > SDMD_MAX_OBST || (s.n_obst && !s.obst)) return SDMD_EINVAL;
+    for (int k = 0; k < 3 * s.n_obst; k++) if (!std::isfinite(s.obst[k])) return SDMD_EINVAL;
     // the RNG must be a reachable glibc state: never all zero
     bool nz = false;
     for (int k = 0; k < 31; k++) nz |= s.rng.tab[k] != 0;
@@ -146,7 +148,7 @@ static int validate(const sdmd_system &s) {
         if (s.bond_off[k] < s.bond_off[k - 1] || s.con_off[k] < s.con_off[k - 1] || s.conn_off[k] < s.conn_off[k - 1])
             return SDMD_EINVAL;
     }
-    if (s.wall && (s.wall_type < 0 || s.wall_type >= SDMD_NTYPES)) return SDMD_EINVAL;
+    if ((s.wall || s.n_obst) && (s.wall_type < 0 || s.wall_type >= SDMD_NTYPES)) return SDMD_EINVAL;
     long ncell = (long)s.cellnum[0] * s.cellnum[1] * s.cellnum[2];
     for (long k = 0; k <= N + ncell; k++) if (!atom_ok(s.cell_list[k])) return SDMD_EINVAL;
     // every atom must sit in a valid cell, with in-range ids and types
@@ -453,6 +455,7 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             d.pair_key = o.pair_key; d.pair_stepkey = o.pair_stepkey; d.rp_idx = o.rp_idx;
         }
         d.sph = m.n_sph ? cv.take<double>(4 * (size_t)m.n_sph) : nullptr;
+        d.obst = m.n_obst ? cv.take<double>(3 * (size_t)m.n_obst) : nullptr;
         d.con_thr32 = cv.take<float>(((size_t)m.n_cons + 1) * 8);
         d.con_step32 = cv.take<float>(((size_t)m.n_con_steps + 1) * 6);
         d.bond32 = cv.take<float>(((size_t)m.n_bonds + 1) * 4);
@@ -485,6 +488,7 @@ static size_t layout(sdmd_gpu *h, const sdmd_system *sys, unsigned char *base,
             auto &c = *copies;
             put(c, (double *)d.mass, s.mass, N1);
             if (m.n_sph) put(c, (double *)d.sph, s.sphobst, 4 * (size_t)m.n_sph);
+            if (m.n_obst) put(c, (double *)d.obst, s.obst, 3 * (size_t)m.n_obst);
             put(c, (int32_t *)d.protein, s.protein, N1); put(c, (int32_t *)d.aanum, s.aanum, N1);
             put(c, (int32_t *)d.aatype, s.aatype, N1); put(c, (int32_t *)d.hb_neighbor, s.hb_neighbor, N1);
             put(c, (int32_t *)d.hb_role, s.hb_role, N1); put(c, (int32_t *)d.name_code, s.name_code, N1);
@@ -653,6 +657,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         m.n_bonds = s.n_bonds; m.n_cons = s.n_cons; m.n_con_steps = s.n_con_steps; m.n_conn = s.n_conn;
         m.n_pair_steps = s.n_pair_steps;
         m.n_sph = s.n_sphobst;
+        m.n_obst = s.n_obst;
         m.nbcap = cap_of(k, head_num, head_den);
         nbcap_max = std::max(nbcap_max, m.nbcap);
         DSys &d = h->hs[k];
@@ -664,6 +669,7 @@ extern "C" int sdmd_gpu_create(const sdmd_system *systems, int32_t n_systems, co
         }
         d.thermostat = s.thermostat; d.wall = s.wall; d.wall_type = s.wall_type;
         d.n_sph = s.n_sphobst;
+        d.n_obst = s.n_obst;
         d.cutoff = s.cutoff; d.temperature = s.temperature; d.thermo_freq = s.thermo_freq; d.t_end = s.t_end;
         d.nbcap = m.nbcap;
         d.n_bonds = s.n_bonds; d.n_cons = s.n_cons; d.n_con_steps = s.n_con_steps; d.n_conn = s.n_conn;

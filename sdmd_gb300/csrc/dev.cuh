@@ -76,6 +76,8 @@ struct DSys {
     double wall_pos[3], wall_vel[3], hb_barrier[3];
     int32_t n_sph;                 // spherical obstacles: x, y, z, radius each
     const double *sph;
+    int32_t n_obst;                // obstruction walls: position[1..3] each, -1 off their axis
+    const double *obst;
     // static
     const double *mass;
     const int32_t *protein, *aanum, *aatype, *hb_neighbor, *hb_role, *name_code;

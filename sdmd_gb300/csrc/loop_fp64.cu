@@ -440,6 +440,45 @@ __device__ __noinline__ void wall_time(const DSys &S, int i, Cur &c, Blk &B, int
     job_assign(S, c, 0, t, pot, sub, SDMD_EV_WALL);
 }
 
+// ObstTime, obstruction walls (src/TimePrediction.c:740-829): for each plane n
+// across axis d, the axis component alone (the others zeroed, as the reference
+// zeroes them) against the potential steps of the pair (atom type, wall type);
+// the partner becomes -d - 10 n when that plane gives the new earliest event
+__device__ __noinline__ void obst_time(const DSys &S, int i, Cur &c, Blk &B, int *bad) {
+    const double p[3] = {S.x[i], S.y[i], S.z[i]}, v[3] = {S.vx[i], S.vy[i], S.vz[i]};
+    for (int n = 0; n < S.n_obst; n++) {
+        for (int dim = 0; dim < 3; dim++) {
+            const double pos = S.obst[3 * n + dim];
+            if (pos < 0) continue;
+            double pi[3] = {0, 0, 0}, pj[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, vj[3] = {0, 0, 0};
+            pi[dim] = p[dim]; pj[dim] = pos; vi[dim] = v[dim];
+            Kin k;
+            k.rx = pi[0] - pj[0]; k.ry = pi[1] - pj[1]; k.rz = pi[2] - pj[2];
+            const double wx = vi[0] - vj[0], wy = vi[1] - vj[1], wz = vi[2] - vj[2];
+            k.r2 = k.rx * k.rx + k.ry * k.ry + k.rz * k.rz;
+            k.b = k.rx * wx + k.ry * wy + k.rz * wz;
+            k.v2 = wx * wx + wy * wy + wz * wz;
+            Lim o; int warn = 0;
+            const int cs = find_pair(S, i, 0, K_COLLISION, k.b, k.r2, o, 0, 0, S.wall_type, &warn, bad);
+            B.warn += warn;
+            if (o.lopot == 0 && o.uppot == 0) continue;   // inside the holes
+            int st, sub; double d2, pot;
+            if (k.b < 0) {   // approaching
+                sub = cs == 0 ? SDMD_SUB_CORE : SDMD_SUB_TBD_CAPTURE;
+                st = -1; d2 = o.lo; pot = o.lopot;
+            } else {         // leaving
+                if (cs == 1) continue;
+                sub = SDMD_SUB_TBD_ESCAPE;
+                st = 1; d2 = o.up; pot = o.uppot;
+            }
+            const double t = root(k, st, d2);
+            if (t < 0) { set_err(B, SDMD_ENEGTIME, i); return; }
+            if (!(t > 0)) continue;   // no root (NaN): JobAssign's time > 0 test fails
+            if (job_assign(S, c, 0, t, pot, sub, SDMD_EV_OBST)) c.partner = -(dim + 1) - 10 * n;
+        }
+    }
+}
+
 // SphObstTime, spherical obstacles (src/TimePrediction.c:1020-1071): a core
 // collision with each fixed sphere the atom approaches (absolute coordinates, no
 // periodic image); the partner becomes -1000 n when obstacle n gives the new
@@ -515,6 +554,7 @@ __device__ __noinline__ void predict_atom(const DSys &S, int i, Shm &M, Blk &B, 
     if (tid == 0) {
         hbnb_time(S, i, c, B, &bad);
         if (S.wall) wall_time(S, i, c, B, &bad);
+        if (S.n_obst) obst_time(S, i, c, B, &bad);
         if (S.n_sph) sphobst_time(S, i, c, B);
         cur_store(S, i, c);
     }
@@ -757,6 +797,33 @@ __device__ void wall_event(const DSys &S, int t, Blk &B) {
     S.vx[t] = S.vx[t] + phi * r[0]; S.vy[t] = S.vy[t] + phi * r[1]; S.vz[t] = S.vz[t] + phi * r[2];
 }
 
+// ObstEvent (src/Events.c:543-617): plane -partner / 10 across axis -partner % 10
+__device__ void obst_event(const DSys &S, int t, Blk &B) {
+    const int part = S.ev_partner[t];
+    const int n = part / -10, dim = (part * -1) % 10;
+    if (n < 0 || n >= S.n_obst || dim < 1 || dim > 3) { set_err(B, SDMD_EEVENTTYPE, t); return; }
+    double pi[3] = {0, 0, 0}, pj[3] = {0, 0, 0}, vi[3] = {0, 0, 0}, vj[3] = {0, 0, 0};
+    pi[dim - 1] = dim == 1 ? S.x[t] : dim == 2 ? S.y[t] : S.z[t];
+    vi[dim - 1] = dim == 1 ? S.vx[t] : dim == 2 ? S.vy[t] : S.vz[t];
+    pj[dim - 1] = S.obst[3 * n + dim - 1];
+    const double r[3] = {pi[0] - pj[0], pi[1] - pj[1], pi[2] - pj[2]};
+    const double w[3] = {vi[0] - vj[0], vi[1] - vj[1], vi[2] - vj[2]};
+    const double d2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+    const double b = r[0] * w[0] + r[1] * w[1] + r[2] * w[2];
+    const double mu = S.mass[t];
+    double pot = S.ev_potential[t];
+    int sv;
+    switch (S.ev_sub[t]) {
+        case SDMD_SUB_CORE: sv = 1; pot = 0; break;
+        case SDMD_SUB_TBD_CAPTURE: if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = 1; } else sv = -1; break;
+        case SDMD_SUB_TBD_ESCAPE: if (b * b - 2 * d2 * pot / mu <= 0) { pot = 0; sv = -1; } else sv = 1; break;
+        default: set_err(B, SDMD_EEVENTTYPE, t); return;
+    }
+    const double phi = (-1 * b + sv * sqrt(b * b - 2 * d2 * pot / S.mass[t])) / d2;
+    if (isnan(phi)) { set_err(B, SDMD_ENAN, t); return; }
+    S.vx[t] = S.vx[t] + phi * r[0]; S.vy[t] = S.vy[t] + phi * r[1]; S.vz[t] = S.vz[t] + phi * r[2];
+}
+
 // SphObstEvent (src/Events.c:752-795): the core bounce off fixed sphere -partner / 1000
 __device__ void sphobst_event(const DSys &S, int t, Blk &B) {
     const int n = S.ev_partner[t] / -1000;
@@ -789,6 +856,7 @@ __device__ void do_event(const DSys &S, DScal &C, int t, int p, Blk &B, int32_t 
         case SDMD_EV_THERMOSTAT: thermostat_event(S, t, C, B); C.c.thermostat++; break;
         case SDMD_EV_PCC: pcc_event(S, t, B, moved); C.c.pcc++; break;
         case SDMD_EV_WALL: wall_event(S, t, B); C.c.wall++; break;
+        case SDMD_EV_OBST: obst_event(S, t, B); C.c.wall++; break;         // walleventsum
         case SDMD_EV_SPHOBST: sphobst_event(S, t, B); C.c.wall++; break;   // walleventsum
         default: set_err(B, SDMD_EEVENTTYPE, t); break;
     }

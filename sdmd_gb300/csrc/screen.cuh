@@ -1021,6 +1021,7 @@ __device__ void fold_atom(const DSys &S, int a, int tnew, ShmS &M, PairScal &PS,
     }
     if (PS.A[a].nbs > 0) hbnb_time(S, i, c, B, &bad);   // its loop runs over nb_status[i] partners
     if (S.wall) wall_time(S, i, c, B, &bad);
+    if (S.n_obst) obst_time(S, i, c, B, &bad);
     if (S.n_sph) sphobst_time(S, i, c, B);
     S.hb_itype[i] = SDMD_HB_NOEVENT;    // HBSkip is one-shot (src/TimePrediction.c:309-327)
     cur_store(S, i, c);

@@ -23,7 +23,8 @@ class sdmd_params(C.Structure):
                 ("cg", C.c_char * 16), ("wall_exist", C.c_char * 20), ("wall_type", C.c_char * 20),
                 ("wall_dyn", C.c_char * 16), ("flow", C.c_char * 32), ("obstruct", C.c_char * 32),
                 ("tunnel", C.c_char * 32), ("sphobst", C.c_char * 32),
-                ("n_sphobst", C.c_int32), ("sphobst_xyzr", C.c_double * (4 * 64))]
+                ("n_sphobst", C.c_int32), ("sphobst_xyzr", C.c_double * (4 * 64)),
+                ("n_obst", C.c_int32), ("obst_pos", C.c_double * (3 * 16))]
 
 
 _lib = None
@@ -100,6 +101,8 @@ def _copy_out(view, names_ptr, res_ptr):
     nsph = s.n_sphobst if s.sphobst else 0
     out.a["sphobst"] = np.array(np.ctypeslib.as_array(s.sphobst, shape=(4 * nsph,)), np.float64) if nsph \
         else np.zeros(0)
+    nob = s.n_obst if s.obst else 0
+    out.a["obst"] = np.array(np.ctypeslib.as_array(s.obst, shape=(3 * nob,)), np.float64) if nob else np.zeros(0)
     out.pull_scalars(s)
     out.names = C.string_at(names_ptr, 8 * (n + 1)) if names_ptr else None
     out.resnames = C.string_at(res_ptr, 8 * (n + 1)) if res_ptr else None

@@ -24,6 +24,7 @@ typedef struct sdmd_host_static {
     const double *hbpot;                   /* HBPotential: BB_r BB_v SS_r SS_v BS_r BS_v */
     const double *charge;                  /* InitializeCharge's, per atom */
     const char *wall_name, *wall_ext;      /* a smooth wall's Wall.txt record: name (8), extraProperty (2 x 16) */
+    double wall_lib_mass;                  /* and its mass (obstruction walls' atoms are the same record) */
 } sdmd_host_static;
 
 void sdmd_host_static_info(const sdmd_host_system *h, sdmd_host_static *out);

@@ -197,6 +197,38 @@ int sdmd_write_wallinfo(const char *path, const sdmd_host_system *h) {
     return fclose(f) == 0 && ok ? SDMD_OK : SDMD_EINVAL;
 }
 
+/* SaveObstInfo (src/DataSave.c:294-308): each obstruction wall's atom record as
+   the reference builds it (src/Initialization.c:1981-2013) -- the Wall.txt name,
+   extra properties and mass, the atom type it names, residue "Wall", the plane's
+   position[1..3] (-1 off its axis), an invalid event -- the rest zero */
+int sdmd_write_obstinfo(const char *path, const sdmd_host_system *h) {
+    if (!path || !h) return SDMD_EINVAL;
+    const sdmd_system *sys = sdmd_host_view((sdmd_host_system *)h);
+    if (!sys->n_obst) return SDMD_EINVAL;
+    sdmd_host_static st;
+    sdmd_host_static_info(h, &st);
+    FILE *f = fopen(path, "wb");
+    if (!f) return SDMD_EINVAL;
+    int ok = 1;
+    for (int n = 0; n < sys->n_obst; n++) {
+        sv_property P;
+        sv_dynamic D;
+        memset(&P, 0, sizeof P);
+        memset(&D, 0, sizeof D);
+        memcpy(P.name, st.wall_name, 8);
+        memcpy(P.extraProperty, st.wall_ext, 32);
+        memcpy(P.nameofAA, "Wall", 5);
+        P.typeofAtom = sys->wall_type;
+        P.mass = st.wall_lib_mass;
+        for (int d = 0; d < 3; d++) D.coordinate[d + 1] = sys->obst[3 * n + d];
+        D.event.partner = SDMD_INVALID;
+        D.event.subEventType = SDMD_SUB_INVALID;
+        D.event.eventType = SDMD_EV_INVALID;
+        ok &= fwrite(&P, sizeof P, 1, f) == 1 && fwrite(&D, sizeof D, 1, f) == 1;
+    }
+    return fclose(f) == 0 && ok ? SDMD_OK : SDMD_EINVAL;
+}
+
 int sdmd_saved_set_replica(sdmd_saved *s, const sdmd_replica *r) {
     if (!s) return SDMD_EINVAL;
     memset(&s->remd, 0, sizeof s->remd);

@@ -65,7 +65,9 @@ struct sdmd_host_system {
     char method[20];
     double hbpot[6];
     char wall_name[8], wall_ext[32];   /* the Wall.txt record of a smooth wall */
+    double wall_lib_mass;
     double sphobst[4 * SDMD_MAX_SPHOBST];
+    double obst[3 * SDMD_MAX_OBST];
 };
 
 typedef struct {
@@ -245,6 +247,28 @@ int sdmd_read_parameters(const char *path, sdmd_params *p) {
         int pos = 0;
         if (sscanf(line, "%1023s %31s%n", s, v, &pos) < 2) ok = 0;
         snprintf(dst[k], 32, "%s", v);
+        if (k == 1 && ok && strcmp(v, "no")) {
+            /* the count, then an axis letter and a position per obstacle with a
+               separator token between them (src/Initialization.c:634-672) */
+            const int n = atoi(v);
+            if (n < 0 || n > SDMD_MAX_OBST) { ok = 0; break; }
+            const char *q = line + pos;
+            for (int i = 0; i < 3 * n; i++) p->obst_pos[i] = -1;
+            for (int i = 0; i < n && ok; i++) {
+                char axis[64];
+                int used = 0, dim;
+                if (sscanf(q, "%63s%n", axis, &used) < 1) { ok = 0; break; }
+                q += used;
+                dim = axis[0] == 'x' ? 0 : axis[0] == 'y' ? 1 : axis[0] == 'z' ? 2 : -1;
+                if (dim < 0 || sscanf(q, "%lf%n", &p->obst_pos[3 * i + dim], &used) < 1) { ok = 0; break; }
+                q += used;
+                if (i != n - 1) {
+                    if (sscanf(q, "%63s%n", axis, &used) < 1) { ok = 0; break; }
+                    q += used;
+                }
+            }
+            p->n_obst = n;
+        }
         if (k == 3 && ok && strcmp(v, "no")) {
             /* the count, then "x y z diameter" per obstacle with a separator token
                between them; the radius is kept (src/Initialization.c:703-724) */
@@ -759,6 +783,7 @@ static int read_wall(B *b) {   /* ReadWall, smooth walls (src/Initialization.c:1
     memcpy(b->wall_ext + 16, e1, strnlen(e1, 15));
     b->wall_type = atom_model(tn);
     if (b->wall_type < 0) return fail(b, "no atom type is matched to %s (Wall.txt)", tn);
+    if (!b->wall) return SDMD_OK;
     for (int d = 0; d < 3; d++) b->wall_pos[d] = b->box[d + 1] / 2;
     if (b->wall == SDMD_WALL_PARALLEL) b->wall_pos[0] = b->wall_pos[2] = 0;
     else if (b->wall == SDMD_WALL_CYLINDER) b->wall_pos[0] = 0;
@@ -919,7 +944,13 @@ static int export_system(B *b, sdmd_host_system **out) {
     s->thermo_freq = p->thermo_freq;
     s->t_end = p->time;
     s->thermostat = strcmp(p->thermostat, "no") ? 1 : 0;
-    s->wall = b->wall; s->wall_type = b->wall_type; s->wall_mass = b->wall_mass;
+    s->wall = b->wall; s->wall_type = b->wall_type; s->wall_mass = b->wall ? b->wall_mass : 0;
+    h->wall_lib_mass = b->wall_mass;   /* obstruction walls' atoms carry it too (ObstInfo.dat) */
+    if (strcmp(p->obstruct, "no")) {   /* Obstruct? (src/Initialization.c:634-672) */
+        s->n_obst = p->n_obst;
+        memcpy(h->obst, p->obst_pos, sizeof(double) * 3 * (size_t)p->n_obst);
+        s->obst = h->obst;
+    }
     if (strcmp(p->sphobst, "no")) {   /* SphObst? (src/Initialization.c:703-724) */
         s->n_sphobst = p->n_sphobst;
         memcpy(h->sphobst, p->sphobst_xyzr, sizeof(double) * 4 * (size_t)p->n_sphobst);
@@ -1092,9 +1123,8 @@ static int build(B *b, cur *coords, uint32_t seed, int emin, sdmd_host_system **
     const sdmd_params *p = b->p;
     if (strcmp(p->continue_mode, "new")) return fail(b, "only \"new\" runs are built here (continue runs load a checkpoint)");
     if (strncmp(p->force_field, "Ding", 1)) return fail(b, "only the Ding force field is supported");
-    if (strcmp(p->cg, "no") || strcmp(p->flow, "no") || strcmp(p->obstruct, "no") || strcmp(p->tunnel, "no") ||
-        strcmp(p->wall_dyn, "no"))
-        return fail(b, "CG models, flow, obstructions, tunnels and dynamic walls are outside the engine's scope");
+    if (strcmp(p->cg, "no") || strcmp(p->flow, "no") || strcmp(p->tunnel, "no") || strcmp(p->wall_dyn, "no"))
+        return fail(b, "CG models, flow, tunnels and dynamic walls are outside the engine's scope");
     snprintf(b->ff, sizeof b->ff, "%s", p->force_field);
     b->wall = 0;
     if (strcmp(p->wall_exist, "no")) {
@@ -1114,7 +1144,7 @@ static int build(B *b, cur *coords, uint32_t seed, int emin, sdmd_host_system **
     if ((r = read_model(b))) return r;
     if ((r = read_tables(b))) return r;
     for (int i = 1; i <= b->n; i++) hb_neighbor_assign(b, i);
-    if (b->wall && (r = read_wall(b))) return r;
+    if ((b->wall || b->p->n_obst) && (r = read_wall(b))) return r;   /* obstacles are Wall.txt atoms too */
     generate_velocity(b, p->temperature);
     if (emin > 0 && (r = energy_min(b, emin))) return r;
     /* PBC("full") (src/Events.c:207-229) */
@@ -1178,7 +1208,7 @@ void sdmd_host_static_info(const sdmd_host_system *h, sdmd_host_static *o) {
     o->mass0 = h->mass; o->type0 = h->type;
     o->hbpot = h->hbpot;
     o->charge = h->charge;
-    o->wall_name = h->wall_name; o->wall_ext = h->wall_ext;
+    o->wall_name = h->wall_name; o->wall_ext = h->wall_ext; o->wall_lib_mass = h->wall_lib_mass;
 }
 
 void sdmd_host_free(sdmd_host_system *h) {

@@ -324,8 +324,18 @@ int sdmd_write_log_replica(const char *path, const sdmd_host_system *h, const sd
     fprintf(f, "CurtBoxSize         = %-8.2lf%-8.2lf%-8.2lf\n", s->box[0], s->box[1], s->box[2]);
     fprintf(f, "FlowType            = %-5i\n", 0);
     fprintf(f, "                      No flow.\n");
-    fprintf(f, "Obstruct            = %-5i\n", 0);
-    fprintf(f, "                      No obstruction.\n");
+    fprintf(f, "Obstruct            = %-5i\n", (int)p->n_obst);   /* obstObj.num */
+    if (!p->n_obst) {
+        fprintf(f, "                      No obstruction.\n");
+    } else {
+        fprintf(f, "ObstructionPosition = ");
+        for (int i = 0; i < p->n_obst; i++) {
+            const double *o = &p->obst_pos[3 * i];
+            fprintf(f, "%.1lf%5.1lf%5.1lf", o[0], o[1], o[2]);
+            if (i < p->n_obst - 1) fprintf(f, ", ");
+        }
+        fprintf(f, "\n");
+    }
     fprintf(f, "Tunnel              = %-5i\n", 0);
     fprintf(f, "                      No tunnel.\n");
     const int columns = strcmp(p->sphobst, "no") != 0;   /* SphObstObj.mark */

@@ -67,7 +67,7 @@ class sdmd_system(C.Structure):
                 + [(n, _PTR[t]) for n, t in STATIC_ARRAYS]
                 + [(n, _PTR[t]) for n, t in DYNAMIC_ARRAYS]
                 + [("time", C.c_double), ("rng", sdmd_rng), ("counters", sdmd_counters)]
-                + [("n_sphobst", C.c_int32), ("sphobst", f64p)])
+                + [("n_sphobst", C.c_int32), ("sphobst", f64p), ("n_obst", C.c_int32), ("obst", f64p)])
 
 MAX_SPHOBST = 64   # SDMD_MAX_SPHOBST
 
@@ -194,6 +194,12 @@ class System:
                 raise ValueError("array sphobst: need C-contiguous float64, 4 per obstacle")
             s.n_sphobst = len(sph) // 4
             s.sphobst = sph.ctypes.data_as(f64p)
+        ob = self.a.get("obst")
+        if ob is not None and len(ob):     # obstruction walls: position[1..3] each
+            if ob.dtype != np.float64 or not ob.flags.c_contiguous or len(ob) % 3:
+                raise ValueError("array obst: need C-contiguous float64, 3 per obstacle")
+            s.n_obst = len(ob) // 3
+            s.obst = ob.ctypes.data_as(f64p)
         s.time = self.time
         rng = np.ascontiguousarray(self.rng, np.int32)
         C.memmove(C.addressof(s.rng), rng.ctypes.data, 33 * 4)
@@ -280,6 +286,9 @@ def from_fixture(npz, stage="pre", dynamic_stage=None):
     a["conn_off"], a["conn_j"], a["conn_bits"] = _conn_rows(n, g("connmap"))
     a["sphobst"] = sphobst_from_parameters(bytes(d["meta/parameter"]).decode()) if "meta/parameter" in d.files \
         else np.zeros(0)
+    a["obst"] = g("obst_pos").astype(np.float64) if "pre/obst_pos" in d.files else np.zeros(0)
+    if "pre/obst_type" in d.files and not wall:
+        s.scal["wall_type"] = int(g("obst_type")[0])   # obstacles are Wall.txt atoms
     _load_dynamic(s, d, ds)
     s.rng = d["meta/rng_pre"].astype(np.int32).copy() if ds == "pre" else np.zeros(33, np.int32)
     for k, v in [("n_bonds", len(a["bond_j"])), ("n_cons", len(a["con_j"])), ("n_con_steps", len(a["con_step_d"])),

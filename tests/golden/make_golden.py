@@ -48,7 +48,7 @@ WallExist?         {wall_exist}
 WallType           {wall_type}
 WallDyn            no
 Flow               no
-Obstruct?          no
+Obstruct?          {obstruct}
 Tunnel?            no
 SphObst?           {sphobst}
 """
@@ -172,7 +172,7 @@ def rng_state_after(seed, calls):
 
 def base_params(**kw):
     p = dict(time=5000, temp=0.6, dump=1e9, cutoff=9.0, thermostat="Andersen", thermo_freq=6.0,
-             wall_exist="no", wall_type="no", sphobst="no")
+             wall_exist="no", wall_type="no", sphobst="no", obstruct="no")
     p.update(kw)
     return p
 

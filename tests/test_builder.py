@@ -28,7 +28,7 @@ def steps(s, kind, k):
     return [(s.a[f"{kind}_step_d"][q], s.a[f"{kind}_step_e"][q], s.a[f"{kind}_step_acc"][q]) for q in range(off, off + n)]
 
 
-@pytest.mark.parametrize("case", ["ala10_nvt", "ala10_nve", "ala10_cyl", "mixed6", "sheet2", "ala10_sph"])
+@pytest.mark.parametrize("case", ["ala10_nvt", "ala10_nve", "ala10_cyl", "mixed6", "sheet2", "ala10_sph", "ala10_obst"])
 def test_builder_reproduces_the_reference_initial_state(golden, case, tmp_path):
     d = golden(case)
     lib = tmp_path / "Library_Ding"

@@ -50,7 +50,8 @@ def bench_engine(engine_mod, systems, helpers=0, **kw):
 
 
 @HELPERS
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "mixed6", "ala10_sph"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "mixed6", "ala10_sph",
+                                  "ala10_obst"])
 def test_bench_path_follows_the_reference_trace(golden, engine_mod, case, helpers):
     """Every pop of the golden run: (target, partner, type, sub-type, executed) and
     dt equal; the first pops' clock and target velocities equal; every checkpoint

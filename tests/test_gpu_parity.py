@@ -41,7 +41,8 @@ def assert_state_equal(a, ref, keys=DYN):
 
 
 @SCREENS
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "ala10_sph"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "ala10_sph",
+                                  "ala10_obst"])
 def test_sweep_matches_reference(golden, engine_mod, case, screen):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -53,7 +54,7 @@ def test_sweep_matches_reference(golden, engine_mod, case, screen):
 
 
 @SCREENS
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "ala10_sph"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "ala10_sph", "ala10_obst"])
 def test_loop_matches_reference_event_for_event(golden, engine_mod, case, screen):
     d = golden(case)
     ids, dts = d["trace/ids"], d["trace/dt"]

@@ -29,7 +29,7 @@ def assert_state_equal(sys_, ref, keys=DYN):
 
 
 @pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_nvt_long", "ala10_cyl", "mixed6", "sheet2",
-                                  "ala10_sph"])
+                                  "ala10_sph", "ala10_obst"])
 def test_sweep_and_tree(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -40,7 +40,7 @@ def test_sweep_and_tree(golden, case):
     assert np.array_equal(node, d["cbt/cbt_node"]) and np.array_equal(leaf, d["cbt/cbt_leaf"])
 
 
-@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "mixed6", "ala10_sph"])
+@pytest.mark.parametrize("case", ["ala10_nve", "ala10_nvt", "ala10_cyl", "mixed6", "ala10_sph", "ala10_obst"])
 def test_trace_event_for_event(golden, case):
     d = golden(case)
     s = from_fixture(d, "pre")
@@ -64,6 +64,9 @@ def test_trace_event_for_event(golden, case):
         assert s.counters["wall"] > 0
     if case == "ala10_sph":   # spherical obstacles (SphObstTime / SphObstEvent) are exercised
         assert ((ids[:, 2] == 9) & (ids[:, 4] == 1)).sum() > 0 and s.counters["wall"] > 0
+    if case == "ala10_obst":  # obstruction walls (ObstTime / ObstEvent), capture and escape
+        ob = ids[(ids[:, 2] == 6) & (ids[:, 4] == 1)]
+        assert set(ob[:, 3]) >= {4, 5} and set(ob[:, 1]) == {-1, -13}
 
 
 @pytest.mark.parametrize("case", ["ala10_nvt_long", "sheet2"])

@@ -134,7 +134,7 @@ def steps(a, kind, k):
     return [(a[f"{kind}_step_d"][q], a[f"{kind}_step_e"][q], a[f"{kind}_step_acc"][q]) for q in range(off, off + n)]
 
 
-@pytest.mark.parametrize("case", ["ala10_nvt", "ala10_cyl", "mixed6", "sheet2"])
+@pytest.mark.parametrize("case", ["ala10_nvt", "ala10_cyl", "mixed6", "sheet2", "ala10_sph", "ala10_obst"])
 def test_fill_equals_the_host_builder(case):
     from sdmd_gb300.host import build_system
     a, scal, rng, counters, time = in_child(_child_fill, case)

@@ -103,7 +103,7 @@ def _child_log(case, q):
         q.put(("error", repr(e)))
 
 
-@pytest.mark.parametrize("case", ["ala10_nvt", "sheet2", "ala10_cyl", "mixed6", "ala10_sph"])
+@pytest.mark.parametrize("case", ["ala10_nvt", "sheet2", "ala10_cyl", "mixed6", "ala10_sph", "ala10_obst"])
 def test_log_matches_the_reference(case, tmp_path):
     """out_log.txt from the host library equals the reference's SaveLog output
     line for line after the first, which carries the wall-clock time."""
@@ -260,4 +260,38 @@ def test_wallinfo_matches_the_reference(tmp_path):
     assert L.sdmd_write_wallinfo(str(path).encode(), hs) == 0
     L.sdmd_host_free(hs)
     assert len(ref) == 136 + 176
+    assert path.read_bytes() == ref
+
+
+OBSTINFO = 11   # enum FileType: obstInfo
+
+
+def _child_obstinfo(case, q):
+    try:
+        work, ind, outd = case_dir(case)
+        L = _bridge(ind, outd)
+        L.bd_save_type.argtypes = [C.c_int]
+        L.bd_save_type(OBSTINFO)                      # SaveObstInfo, as Prepare() calls it for obstruction walls
+        q.put(("ok", open(os.path.join(outd, "ObstInfo.dat"), "rb").read(), ind))
+    except Exception as e:
+        q.put(("error", repr(e)))
+
+
+def test_obstinfo_matches_the_reference(tmp_path):
+    """ObstInfo.dat of the two-plane case equals the reference's SaveObstInfo output
+    byte for byte (each obstruction wall's atom record)."""
+    from sdmd_gb300 import host as H
+    ref, ind = in_child(_child_obstinfo, "ala10_obst")
+    d = np.load(os.path.join(REPO, "tests", "golden", "ala10_obst.npz"))
+    L = H.lib()
+    L.sdmd_write_obstinfo.argtypes = [C.c_char_p, C.c_void_p]
+    params = H.read_parameters(os.path.join(ind, "parameter.txt"))
+    hs = C.c_void_p()
+    err = C.create_string_buffer(512)
+    assert L.sdmd_build_system_gro_text(ind.encode(), bytes(d["meta/gro"]), C.byref(params), int(d["pre/seed"][0]),
+                                        20000, C.byref(hs), err, 512) == 0, err.value
+    path = tmp_path / "ObstInfo.dat"
+    assert L.sdmd_write_obstinfo(str(path).encode(), hs) == 0
+    L.sdmd_host_free(hs)
+    assert len(ref) == 2 * (136 + 176)
     assert path.read_bytes() == ref
