@@ -4,6 +4,7 @@
  */
 #include "app_common.h"
 
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -267,6 +268,42 @@ int app_dump(app_run *r, const sdmd_system *sys, double pot, double kin, const c
 fail:
     fprintf(stderr, "!!ERROR!!: cannot write %s\n", f);
     return 1;
+}
+
+int64_t app_event_total(const sdmd_counters *c) {
+    return c->collision + c->bond + c->hb + c->hbneighbor + c->thermostat + c->pcc + c->wall;
+}
+
+double app_time_estimate(const app_run *r) {
+    char f[2400];
+    snprintf(f, sizeof f, "%s/timeEvaluation.dat", r->cli.savedir);
+    FILE *t = r->is_new ? NULL : fopen(f, "rb");
+    if (!t) {
+        printf("Time evaluation is unavailable this time!\n");
+        return 0;
+    }
+    double old = 0;
+    if (fread(&old, sizeof old, 1, t) != 1) old = 0;
+    fclose(t);
+    const double est = (r->p.time - r->sys->time) / 100 * old;
+    const double hours = floor(est / 3600), mins = floor((est - hours * 3600) / 60);
+    printf("This simulation may take %.0lf hours %.0lf mins %.0lf sec\n", hours, mins, est - hours * 3600 - mins * 60);
+    return old;
+}
+
+void app_time_record(const app_run *r, double old_record, double old_time, double seconds, long events) {
+    const double hours = floor(seconds / 3600), mins = floor((seconds - hours * 3600) / 60);
+    double sec = seconds - hours * 3600 - mins * 60;
+    printf("\nTotal time taken: %.0f hours %.0f mins %.0f sec\n", hours, mins, sec);
+    printf("Calculate event times: %li\n", events);
+    sec += hours * 3600 + mins * 60;
+    const double record = (sec + old_record * old_time / 100) / r->p.time * 100;
+    char f[2400];
+    snprintf(f, sizeof f, "%s/timeEvaluation.dat", r->cli.savedir);
+    FILE *t = fopen(f, "wb");
+    if (!t) return;
+    fwrite(&record, sizeof record, 1, t);
+    fclose(t);
 }
 
 void app_print_stats(const sdmd_counters *c) {

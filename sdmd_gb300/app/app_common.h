@@ -65,6 +65,14 @@ int app_save_re(app_run *r, double time, const char *timer);
 /* The end-of-run statistics block (src/DMD.c:244-265). */
 void app_print_stats(const sdmd_counters *c);
 
+/* timeEvaluation.dat (src/DMD.c:220-231, 267-277): a continue run prints the
+   estimate from the seconds per 100 time units that the last run recorded and
+   returns that record (0 when unavailable); at the end, the run's time and event
+   count are printed and the record updated. */
+double app_time_estimate(const app_run *r);
+void app_time_record(const app_run *r, double old_record, double old_time, double seconds, long events);
+int64_t app_event_total(const sdmd_counters *c);
+
 int app_engine_fail(sdmd_gpu *h, int rc, const char *where);
 
 #endif

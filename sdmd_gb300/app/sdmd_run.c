@@ -19,7 +19,9 @@
  * renamed with the run's start time, as BackupFile does (src/DataSave.c:79-96).
  * out_log.txt (and for a new run SysInfo.dat) is written at the start, as
  * Prepare's SaveLog and SaveSysInfo do.  The end-of-run statistics block is the
- * reference's (src/DMD.c:244-265).
+ * reference's (src/DMD.c:244-265), and so is timeEvaluation.dat, the seconds per
+ * 100 time units that a continue run's estimate is printed from
+ * (src/DMD.c:220-231, 267-277).
  *
  * The random seed is time(NULL), as the reference's release build uses, or
  * 1575263273 (the reference's -DDEBUG_RANDOM seed) when SDMD_DEBUG_RANDOM is set.
@@ -48,11 +50,15 @@ int main(int argc, const char *argv[]) {
         fprintf(stderr, "!!ERROR!!: replica exchange runs all replicas in one process: use sremd-gb300\n");
         return 1;
     }
+    const clock_t st0 = clock();
     const uint32_t seed = getenv("SDMD_DEBUG_RANDOM") ? APP_DEBUG_SEED : (uint32_t)time(NULL);
     app_run run;
     if (app_setup(&run, &cli, seed)) return 1;
     sdmd_system *sys = run.sys;
+    const double old_time = sys->time;
+    const int64_t old_events = app_event_total(&sys->counters);
     app_print_config(&run);
+    const double old_record = app_time_estimate(&run);
     printf("\nSimulation starts...\n");
     fflush(stdout);
 
@@ -94,6 +100,8 @@ int main(int argc, const char *argv[]) {
     }
     const double secs = (double)(clock() - st) / CLOCKS_PER_SEC;
     app_print_stats(&sys->counters);
+    app_time_record(&run, old_record, old_time, (double)(clock() - st0) / CLOCKS_PER_SEC,
+                    (long)(app_event_total(&sys->counters) - old_events));
     printf("\nHost time of the loop and dumps: %.2f s, %d dumps\n", secs, run.frames);
     sdmd_gpu_destroy(h);
     app_free(&run);

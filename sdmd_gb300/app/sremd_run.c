@@ -50,6 +50,7 @@ static int usage(const char *me) {
 }
 
 int main(int argc, const char *argv[]) {
+    const clock_t st0 = clock();
     const char *config = NULL;
     const char *args[MAX_ARGS];
     int nargs = 0;
@@ -111,6 +112,9 @@ int main(int argc, const char *argv[]) {
             return 1;
         }
     app_print_config(&run[0]);
+    const double old_time = sys[0].time, old_record = app_time_estimate(&run[0]);
+    int64_t old_events = 0;
+    for (int k = 0; k < n; k++) old_events += app_event_total(&sys[k].counters);
     printf("%d replicas, exchange every %s time units\n\nSimulation starts...\n", n, rate_txt);
     fflush(stdout);
 
@@ -220,6 +224,9 @@ int main(int argc, const char *argv[]) {
     }
     printf("\nExchanges: %lld, pair attempts %lld, swaps %lld\n", (long long)exchanges, (long long)x.attempted,
            (long long)x.accepted);
+    int64_t events = -old_events;
+    for (int k = 0; k < n; k++) events += app_event_total(&sys[k].counters);
+    app_time_record(&run[0], old_record, old_time, (double)(clock() - st0) / CLOCKS_PER_SEC, (long)events);
     printf("Host time of the loop, dumps and exchanges: %.2f s\n", secs);
     sdmd_gpu_destroy(h);
     for (int k = 0; k < n; k++) app_free(&run[k]);
