@@ -148,8 +148,13 @@ int main(int argc, const char *argv[]) {
         fprintf(stderr, "!!ERROR!!: ExchangeRate must be positive\n");
         return 1;
     }
-    for (int k = 0; k < n; k++)   /* rate = ((int)(currenttime / outputRate) + 1) * outputRate */
+    for (int k = 0; k < n; k++) {   /* rate = ((int)(currenttime / outputRate) + 1) * outputRate */
+        if (run[k].rep.output_rate <= 0) {   /* a continue run takes it from the replica's checkpoint */
+            fprintf(stderr, "!!ERROR!!: replica %d: exchange period %d must be positive\n", k, run[k].rep.output_rate);
+            return 1;
+        }
         rate[k] = ((int64_t)(int)(sys[k].time / run[k].rep.output_rate) + 1) * run[k].rep.output_rate;
+    }
     const int64_t kNoLimit = (int64_t)1 << 40;
     int energies = 0;
     for (int k = 0; k < n; k++)

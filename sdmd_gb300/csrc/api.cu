@@ -963,7 +963,10 @@ extern "C" int sdmd_gpu_run_to_stops(sdmd_gpu *h, const double *stop_time, const
     }
     if (at_stop)
         for (int k = 0; k < n; k++) at_stop[k] = 0;
-    if (most == 0) return SDMD_OK;
+    if (most == 0) {   // nothing runs
+        h->launches = 0; h->loop_launches = 0; h->loop_ms = 0; h->run_ms = 0;
+        return SDMD_OK;
+    }
     CK(cudaSetDevice(h->opts.device));
     CK(cudaEventRecord(h->e0, h->stream));
     CK(cudaMemcpyAsync(h->x_stop, stop_time, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
