@@ -175,3 +175,36 @@ def test_handoff_to_the_reference_loop_and_back(case, k, m):
     assert ca["frame"] == k + m
     if case == "sheet2":
         assert ca["hb"] > 0
+
+
+def _child_obstacles(ind, outd, q):
+    try:
+        s = _fill(_bridge(ind, outd))
+        q.put(("ok", s.a["sphobst"], s.a["obst"], s.scal.get("wall_type")))
+    except Exception as e:
+        q.put(("error", repr(e)))
+
+
+@pytest.mark.parametrize("obstruct,sphobst", [
+    ("1 y 60.0", "1 70 70 70 8"),
+    ("3 z 90.25 ; x 58 ; y 91.5", "2   60.5 61.5 62.5 9.0 and 95 96 97 10.5"),
+    ("no", "3 55 55 55 6 , 99 99 99 6 , 55 99 55 7.25"),
+])
+def test_obstacle_lines_read_as_the_reference_reads_them(obstruct, sphobst):
+    """The Obstruct? and SphObst? lines, with other spacings and separator tokens:
+    the host library's parse (through its builder) equals the reference's
+    ReadParameter (src/Initialization.c:634-724) as the bridge fills it."""
+    from sdmd_gb300.host import build_system
+    work, ind, outd = case_dir("ala10_obst")
+    text = open(os.path.join(ind, "parameter.txt")).read().splitlines()
+    text = [(f"Obstruct?          {obstruct}" if l.startswith("Obstruct?") else
+             f"SphObst?           {sphobst}" if l.startswith("SphObst?") else l) for l in text]
+    with open(os.path.join(ind, "parameter.txt"), "w") as f:
+        f.write("\n".join(text) + "\n")
+    sph, obst, wall_type = in_child(_child_obstacles, ind, outd)
+    d = np.load(os.path.join(REPO, "tests", "golden", "ala10_obst.npz"))
+    mine = build_system(ind, gro_text=bytes(d["meta/gro"]).decode(), seed=int(d["pre/seed"][0]))
+    assert np.array_equal(mine.a["sphobst"], sph) and len(sph) == 4 * int(sphobst.split()[0])
+    assert np.array_equal(mine.a["obst"], obst)
+    if obstruct != "no":
+        assert len(obst) == 3 * int(obstruct.split()[0]) and mine.scal["wall_type"] == wall_type
