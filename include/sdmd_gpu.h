@@ -170,6 +170,17 @@ typedef struct sdmd_system {
      * are outside the engine. */
     int32_t        n_obst;         /* 0 .. SDMD_MAX_OBST */
     const double  *obst;
+
+    /* ---- a dynamic smooth wall (WallDyn, -Wsz, -Wrt), ABI 2 ----
+     * DoWallDyn (src/Events.c:502-541) after each executed event, and WallTime's
+     * widening of the box while an atom is outside a compressed wall
+     * (src/TimePrediction.c:674-697); both change box[] as the run goes.  The
+     * fields hold DynamicWallStr (src/DMD.h:393-402).  The oracle runs it; the
+     * engine returns SDMD_EUNSUPPORTED for wall_dyn != 0. */
+    int32_t        wall_dyn;       /* 0 none, 1 compress, 2 expand, 3 pulse */
+    int32_t        wall_dyn_sign, wall_dyn_touch;
+    double         wall_dyn_size, wall_dyn_rate, wall_dyn_step, wall_dyn_cur_time;
+    double         wall_dyn_orig_box[3];
 } sdmd_system;
 
 /* one record per popped event; same fields as the reference trace */

@@ -94,6 +94,16 @@ static void dump_dynamic(void) {
     sec_i("HBnumformed", HBnumformed);
     sec_i("alphaHBformed", alphaHBformed);
     sec_q("warningsum", warningsum);
+    if (strcmp(wallDyn.mark, "no") || wallDyn.step != 0) {   /* a dynamic wall: the box moves */
+        sec("box_now", 'd', 3, &boxDimension[1]);
+        int mark = !strcmp(wallDyn.mark, "compress") ? 1 : !strcmp(wallDyn.mark, "expand") ? 2 :
+                   !strcmp(wallDyn.mark, "pulse") ? 3 : 0;
+        int wi[3] = {mark, wallDyn.sign, wallDyn.touch};
+        sec("wall_dyn_i", 'i', 3, wi);
+        double wd[7] = {wallDyn.size, wallDyn.rate, wallDyn.step, wallDyn.curTime, wallDyn.origBoxDim[1],
+                        wallDyn.origBoxDim[2], wallDyn.origBoxDim[3]};
+        sec("wall_dyn_d", 'd', 7, wd);
+    }
     /* the reference's own observables (src/ToolFunctions.c:626-752); CalPotenE
        may count warnings, which are restored so the dump does not perturb state */
     {
@@ -382,6 +392,7 @@ int main(int argc, const char *argv[]) {
                 partner->dynamic->event.counter++;
             Predict(renewList, thisList);
             UpdateCBT(renewList);
+            if (strcmp(wallDyn.mark, "no")) DoWallDyn();   /* src/SGThread.c:129 */
             r->executed = 1;
         } else {
             renewList[0] = 1; renewList[2] = 0; renewList[3] = 0;

@@ -571,6 +571,7 @@ static void hbnb_time(sdmd_system *s, int i) {
 
 /* WallTime, smooth walls (src/TimePrediction.c:635-737) */
 static void wall_time(sdmd_system *s, int i) {
+recal:;
     cand c = {INFINIT, 0, SDMD_SUB_INVALID};
     double p[3] = {s->x[i], s->y[i], s->z[i]}, v[3] = {s->vx[i], s->vy[i], s->vz[i]};
     if (s->wall == SDMD_WALL_PARALLEL) { p[0] = p[2] = 0; v[0] = v[2] = 0; }
@@ -585,7 +586,23 @@ static void wall_time(sdmd_system *s, int i) {
     double dist2 = L2 * L2 * 0.25 + k.r2 - L2 * sqrt(k.r2);
     pairlim L;
     int cs = find_pair(s, i, 0, K_COLLISION, -1 * k.b, dist2, &L, 0, 0, s->wall_type);
-    if (L.lopot == 0 && L.uppot == 0) { fail(SDMD_EWALL, i); return; }
+    if (L.lopot == 0 && L.uppot == 0) {
+        if (s->wall_dyn) {   /* the moving wall passed the atom: widen the box, predict again
+                                (src/TimePrediction.c:674-697) */
+            s->wall_dyn_touch++;
+            if (s->wall == SDMD_WALL_PARALLEL) {
+                s->box[1] += s->wall_dyn_step;
+            } else if (s->wall == SDMD_WALL_CYLINDER) {
+                s->box[1] += s->wall_dyn_step; s->box[2] += s->wall_dyn_step;
+            } else if (s->wall == SDMD_WALL_SPHERE) {
+                s->box[0] += s->wall_dyn_step; s->box[1] += s->wall_dyn_step; s->box[2] += s->wall_dyn_step;
+            }
+            if (s->box[1] > s->wall_dyn_orig_box[1]) { fail(SDMD_EWALL, i); return; }
+            goto recal;
+        }
+        fail(SDMD_EWALL, i);
+        return;
+    }
     int st; double d2;
     if (k.b < 0 && disc(&k, L.lo) > 0) {
         if (cs == 1) return;
@@ -966,6 +983,42 @@ static void sphobst_event(sdmd_system *s, int t) {
     s->vx[t] = s->vx[t] + phi * r[0]; s->vy[t] = s->vy[t] + phi * r[1]; s->vz[t] = s->vz[t] + phi * r[2];
 }
 
+/* DoWallDyn (src/Events.c:502-541), after each executed event: once per time
+ * unit the wall moves by sign * step (a pulse turns at its extremes), the atoms
+ * heading for the wall have their events invalidated, and a compression or an
+ * expansion that is complete stops. */
+static void do_wall_dyn(sdmd_system *s) {
+    if (!(s->time >= s->wall_dyn_cur_time)) return;
+    const double *o = s->wall_dyn_orig_box;
+    if (s->wall_dyn == 3) {
+        if ((o[1] - s->box[1] >= s->wall_dyn_size) || (o[1] == s->box[1])) {
+            s->wall_dyn_sign *= -1;
+            s->wall_dyn_touch = 0;
+        } else if (fabs(s->box[1] + (int)(s->time / s->wall_dyn_rate + 1) * s->wall_dyn_size -
+                        (s->time - 1) * s->wall_dyn_step - o[1]) <= s->wall_dyn_step &&
+                   s->wall_dyn_touch >= 5) {
+            s->wall_dyn_sign *= -1;
+            s->wall_dyn_touch = 0;
+        }
+    }
+    s->wall_dyn_cur_time += 1;
+    if (s->wall == SDMD_WALL_PARALLEL) {
+        s->box[1] += s->wall_dyn_sign * s->wall_dyn_step;
+    } else if (s->wall == SDMD_WALL_CYLINDER) {
+        s->box[1] += s->wall_dyn_sign * s->wall_dyn_step;
+        s->box[2] += s->wall_dyn_sign * s->wall_dyn_step;
+    } else if (s->wall == SDMD_WALL_SPHERE) {
+        s->box[0] += s->wall_dyn_sign * s->wall_dyn_step;
+        s->box[1] += s->wall_dyn_sign * s->wall_dyn_step;
+        s->box[2] += s->wall_dyn_sign * s->wall_dyn_step;
+    }
+    for (int i = 1; i <= s->n_atoms; i++)
+        if (s->ev_type[i] == SDMD_EV_WALL) s->ev_counter[i]++;
+    if ((o[1] - s->box[1] >= s->wall_dyn_size && s->wall_dyn == 1) ||
+        (o[1] - s->box[1] <= s->wall_dyn_step && s->wall_dyn == 2))
+        s->wall_dyn = 0;
+}
+
 /* DoEvent (src/Events.c:25-114) */
 static void do_event(sdmd_system *s, int t, int p) {
     switch (s->ev_type[t]) {
@@ -1080,6 +1133,7 @@ static int run_loop(oracle_loop *L, int64_t max_events, double t_end, double sto
         }
         predict(s, list, n);
         for (int q = 0; q < n; q++) cbt_update(L, list[q]);
+        if (!hazard && s->wall_dyn) do_wall_dyn(s);
         if (trace && pops < trace_cap) {
             sdmd_trace_rec *r = &trace[pops];
             memset(r, 0, sizeof(*r));

@@ -116,6 +116,7 @@ static int validate(const sdmd_system &s) {
         (s.n_conn && (!s.conn_j || !s.conn_bits)))
         return SDMD_EINVAL;
     if (s.wall < 0 || s.wall > SDMD_WALL_SPHERE || s.thermostat < 0 || s.thermostat > 1) return SDMD_EUNSUPPORTED;
+    if (s.wall_dyn != 0) return SDMD_EUNSUPPORTED;   // dynamic walls: the oracle only
     if (s.n_sphobst < 0 || s.n_sphobst > SDMD_MAX_SPHOBST || (s.n_sphobst && !s.sphobst)) return SDMD_EINVAL;
     for (int k = 0; k < s.n_sphobst; k++)
         if (!(s.sphobst[4 * k + 3] > 0) || !std::isfinite(s.sphobst[4 * k]) || !std::isfinite(s.sphobst[4 * k + 1]) ||

@@ -67,7 +67,10 @@ class sdmd_system(C.Structure):
                 + [(n, _PTR[t]) for n, t in STATIC_ARRAYS]
                 + [(n, _PTR[t]) for n, t in DYNAMIC_ARRAYS]
                 + [("time", C.c_double), ("rng", sdmd_rng), ("counters", sdmd_counters)]
-                + [("n_sphobst", C.c_int32), ("sphobst", f64p), ("n_obst", C.c_int32), ("obst", f64p)])
+                + [("n_sphobst", C.c_int32), ("sphobst", f64p), ("n_obst", C.c_int32), ("obst", f64p)]
+                + [("wall_dyn", C.c_int32), ("wall_dyn_sign", C.c_int32), ("wall_dyn_touch", C.c_int32),
+                   ("wall_dyn_size", C.c_double), ("wall_dyn_rate", C.c_double), ("wall_dyn_step", C.c_double),
+                   ("wall_dyn_cur_time", C.c_double), ("wall_dyn_orig_box", C.c_double * 3)])
 
 MAX_SPHOBST = 64   # SDMD_MAX_SPHOBST
 
@@ -216,6 +219,11 @@ class System:
         self.rng[32] = s.rng.rear
         for k, _ in sdmd_counters._fields_:
             self.counters[k] = getattr(s.counters, k)
+        if "wall_dyn" in self.scal:   # a dynamic wall moves the box as the run goes
+            self.scal["box"] = list(s.box)
+            for k in ("wall_dyn", "wall_dyn_sign", "wall_dyn_touch", "wall_dyn_size", "wall_dyn_rate", "wall_dyn_step",
+                      "wall_dyn_cur_time"):
+                self.scal[k] = getattr(s, k)
 
     def state_digest(self):
         """Everything the loop mutates, for exact comparisons."""
@@ -289,6 +297,12 @@ def from_fixture(npz, stage="pre", dynamic_stage=None):
     a["obst"] = g("obst_pos").astype(np.float64) if "pre/obst_pos" in d.files else np.zeros(0)
     if "pre/obst_type" in d.files and not wall:
         s.scal["wall_type"] = int(g("obst_type")[0])   # obstacles are Wall.txt atoms
+    if f"{ds}/wall_dyn_i" in d.files:   # a dynamic wall: its state and the box it has moved to
+        wi, wd = h("wall_dyn_i"), h("wall_dyn_d")
+        s.scal.update(wall_dyn=int(wi[0]), wall_dyn_sign=int(wi[1]), wall_dyn_touch=int(wi[2]),
+                      wall_dyn_size=float(wd[0]), wall_dyn_rate=float(wd[1]), wall_dyn_step=float(wd[2]),
+                      wall_dyn_cur_time=float(wd[3]), wall_dyn_orig_box=[float(v) for v in wd[4:7]],
+                      box=[float(v) for v in h("box_now")])
     _load_dynamic(s, d, ds)
     s.rng = d["meta/rng_pre"].astype(np.int32).copy() if ds == "pre" else np.zeros(33, np.int32)
     for k, v in [("n_bonds", len(a["bond_j"])), ("n_cons", len(a["con_j"])), ("n_con_steps", len(a["con_step_d"])),
@@ -341,4 +355,8 @@ def fixture_dynamic(npz, stage):
     out = dict(s.a)
     out["_time"] = s.time
     out["_counters"] = s.counters
+    if f"{stage}/box_now" in npz.files:   # a dynamic wall's box and state
+        out["_box"] = [float(v) for v in npz[f"{stage}/box_now"]]
+        out["_wall_dyn_i"] = [int(v) for v in npz[f"{stage}/wall_dyn_i"]]
+        out["_wall_dyn_d"] = [float(v) for v in npz[f"{stage}/wall_dyn_d"]]
     return out

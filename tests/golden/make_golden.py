@@ -46,7 +46,7 @@ Thermo_Freq        {thermo_freq}
 CGModel            no
 WallExist?         {wall_exist}
 WallType           {wall_type}
-WallDyn            no
+WallDyn            {wall_dyn}
 Flow               no
 Obstruct?          {obstruct}
 Tunnel?            no
@@ -78,7 +78,7 @@ def build_harness():
     subprocess.check_call(["make", "-s", "-C", os.path.join(REPO, "oracle", "ref")])
 
 
-def run_case(name, gro_text, params, n_events, ckpts, wall_lib=None, keep_trace_full=4000, sparse=False):
+def run_case(name, gro_text, params, n_events, ckpts, wall_lib=None, keep_trace_full=4000, sparse=False, args=()):
     work = tempfile.mkdtemp(prefix="sdmd_golden_")
     try:
         ind, outd, dumpd = (os.path.join(work, d) for d in ("in", "out", "dump"))
@@ -100,7 +100,7 @@ def run_case(name, gro_text, params, n_events, ckpts, wall_lib=None, keep_trace_
         with open(os.path.join(ind, "sys.gro"), "w") as f:
             f.write(gro_text)
         ck = ",".join(str(c) for c in ckpts) if ckpts else "-"
-        r = subprocess.run([HARNESS, dumpd, str(n_events), ck, "--", "-i", ind, "-o", outd, "-f", "sys.gro"],
+        r = subprocess.run([HARNESS, dumpd, str(n_events), ck, "--", "-i", ind, "-o", outd, "-f", "sys.gro", *args],
                            capture_output=True, text=True, cwd=work)
         if r.returncode != 0:
             raise RuntimeError(f"harness failed for {name}: {r.stdout[-2000:]} {r.stderr[-2000:]}")
@@ -139,6 +139,8 @@ def run_case(name, gro_text, params, n_events, ckpts, wall_lib=None, keep_trace_
         arrays["meta/parameter"] = np.frombuffer(PARAM_TEMPLATE.format(**params).encode(), np.uint8)
         if wall_lib is not None:
             arrays["meta/wall_lib"] = np.frombuffer(wall_lib.encode(), np.uint8)
+        if args:
+            arrays["meta/args"] = np.frombuffer(" ".join(args).encode(), np.uint8)
         out = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(out, **arrays)
         print(f"{name}: {summary[0] if summary else ''} -> {os.path.getsize(out) / 1024:.0f} KiB")
@@ -172,7 +174,7 @@ def rng_state_after(seed, calls):
 
 def base_params(**kw):
     p = dict(time=5000, temp=0.6, dump=1e9, cutoff=9.0, thermostat="Andersen", thermo_freq=6.0,
-             wall_exist="no", wall_type="no", sphobst="no", obstruct="no")
+             wall_exist="no", wall_type="no", sphobst="no", obstruct="no", wall_dyn="no")
     p.update(kw)
     return p
 

@@ -160,3 +160,32 @@ def test_energy_functions_match_reference(golden, case):
         s = from_fixture(d, "pre", dynamic_stage=None if st == "pre" else st)
         assert O.kinetic_energy(s) == d[f"{st}/kinE"][0]
         assert O.potential_energy(s) == d[f"{st}/potE"][0]
+
+
+def test_dynamic_wall_follows_the_reference(golden):
+    """A compressing cylinder wall (WallDyn compress, -Wsz 2 -Wrt 10): DoWallDyn
+    moves the wall once per time unit and invalidates the events of atoms heading
+    for it, until the compression is complete.  Every pop of the reference's run,
+    and at each checkpoint the state, the box and the wall's own state, equal."""
+    d = golden("ala10_cyldyn")
+    s = from_fixture(d, "pre")
+    assert s.scal["wall_dyn"] == 1
+    O.predict_all(s)
+    loop = O.Loop(s)
+    ids, dts = d["trace/ids"], d["trace/dt"]
+    done, pops = 0, []
+    for c in [int(v) for v in d["meta/ckpts"]] + [int(d["meta/n_events"][0])]:
+        rc, tr, n = loop.run(c - done, trace_cap=len(ids) + 10)
+        assert rc == 0
+        pops.append(tr[:n])
+        done = c
+        stage = f"ckpt{c}" if f"ckpt{c}/x" in d.files else "final"
+        ref = fixture_dynamic(d, stage)
+        assert_state_equal(s, ref)
+        assert s.scal["box"] == ref["_box"], (c, s.scal["box"], ref["_box"])
+        assert [s.scal["wall_dyn"], s.scal["wall_dyn_sign"], s.scal["wall_dyn_touch"]] == ref["_wall_dyn_i"]
+        assert s.scal["wall_dyn_cur_time"] == ref["_wall_dyn_d"][3]
+    tr = np.concatenate(pops)
+    mine = np.stack([tr["target"], tr["partner"], tr["type"], tr["sub"], tr["executed"]], 1)
+    assert np.array_equal(mine, ids) and np.array_equal(tr["dt"], dts)
+    assert s.scal["box"][1] < d["pre/box"][1] and s.scal["wall_dyn"] == 0   # compressed, then stopped
